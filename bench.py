@@ -1,0 +1,396 @@
+"""Benchmark of the satsuma2 cross-correlation path on GB300.
+
+Metric: chunk-pairs/s (4096 bp x 4096 bp, both strands), the batched uniform
+workload (4096 seeded pairs, homolog length U[200,3500], identity U[70,95]%, 25%
+unrelated, 25% reverse-complemented; FFT length 8192, cutoff 1.8).  One "step" =
+one pass over that batch.
+
+JSON line (rank 0):
+  value         device-resident batch throughput (inputs already in HBM),
+                CUDA events on the launching stream, L2 flushed before each step
+  e2e           the same through xc_align_pairs with host buffers (pinned
+                staging copy, H2D, kernels, D2H and t_result assembly timed)
+  plain / served   one pair per call vs continuous-batching serving, and the
+                served p50/p99 request latency
+  roofline      correlation kernel's FP32 work against the FP32 pipe peak
+  cpu_baseline  the reference CPU path on this host's cores (bounded sample)
+
+--impl reference runs the reference's CPU implementation on the host cores
+(the compiled reference when it loads here, else the oracle restatement) and
+prints the same metric.
+
+Multi-GPU: the path has no exchange step, so N GPUs run N independent replicas
+of the batch ("replicas only"); value = pairs of all ranks / max rank time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "chunk-pairs/s (4096bp, both strands) served vs plain on 1 GB300; p50/p99 ms"
+UNIT = "chunk-pairs/s"
+N_PAIRS = 4096
+SEED = 42
+TARGET_TOTAL = 4096.0 * 4096   # sum of the target lengths of the workload
+L2_FLUSH_BYTES = 512 << 20
+
+
+def workload():
+    from satsuma2_gb300 import workloads as W
+    return W.uniform_batch(N_PAIRS, seed=SEED)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def fft_flops_per_pair(L=8192):
+    """Algorithmic FP32 work of one pair, both strands: 4 target + 8 query
+    forward real FFTs + 2 inverse (channel sum by linearity) at 2.5 L log2 L
+    each, plus the 4-channel conjugate product-sum (8 flops per bin)."""
+    F = 2.5 * L * np.log2(L)
+    return 14 * F + 2 * 4 * (L // 2) * 8
+
+
+def cpu_baseline(items, seconds=12.0, impl_hint=None):
+    """Reference CPU path on a bounded sample, all host threads."""
+    import oracle
+    threads = os.cpu_count() or 1
+    kind = "port"
+    sample = items[: max(threads * 4, 64)]
+    ref = None
+    try:
+        if os.path.exists(oracle.REF_SO):
+            ref = oracle.Reference()
+            kind = "reference"
+    except OSError:
+        ref = None
+    if ref is not None:
+        # reference CPU code, one pair per call across a thread pool
+        from concurrent.futures import ThreadPoolExecutor
+
+        def one(tq):
+            ref.align_pair(tq[0], tq[1], 8192, target_total=TARGET_TOTAL)
+            return 1
+        done, t0 = 0, time.time()
+        with ThreadPoolExecutor(threads) as ex:
+            while time.time() - t0 < seconds:
+                done += sum(ex.map(one, sample))
+        dt = time.time() - t0
+        return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": kind,
+                "sample": "%d uniform 4096x4096 pairs (FFT 8192), %d threads, %.1f s" % (done, threads, dt)}
+    O = oracle.Oracle()
+    P = O.params(target_total=TARGET_TOTAL)
+    pairs = [O.pair(t, q) for t, q in sample]
+    done, t0 = 0, time.time()
+    while time.time() - t0 < seconds:
+        O.align_batch(P, pairs, threads)
+        done += len(pairs)
+    dt = time.time() - t0
+    return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": "%d uniform 4096x4096 pairs (FFT 8192) through the C restatement of the reference "
+                      "CPU path, %d threads, %.1f s" % (done, threads, dt)}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    items = workload()
+    vals = []
+    for _ in range(args.warmup):
+        pass
+    info = None
+    for _ in range(args.steps):
+        info = cpu_baseline(items, seconds=args.ref_seconds)
+        vals.append(info["value"])
+    v = float(np.mean(vals))
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * N_PAIRS / v,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+           "data": "synthetic (seeded)",
+           "config": {"workload": "batched uniform: %d pairs 4096x4096 bp, FFT 8192, cutoff 1.8, seed %d"
+                                  % (N_PAIRS, SEED), "parallelism": "host threads"},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": info["kind"],
+                            "sample": info["sample"]},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def serve_run(x, items, n_threads=4, req_pairs=64, total=16384, rate=None):
+    """Submits requests from n_threads threads; rate (pairs/s) None = as fast as
+    admission allows.  Returns (pairs/s, p50, p99)."""
+    import satsuma2_gb300 as sg
+    reqs = [items[(i * req_pairs) % len(items):(i * req_pairs) % len(items) + req_pairs]
+            for i in range(total // req_pairs)]
+    lat = []
+    lock = threading.Lock()
+    t_start = time.perf_counter()
+    per_thread = [reqs[k::n_threads] for k in range(n_threads)]
+    arrivals = None
+    if rate:
+        rng = np.random.default_rng(7)
+        gaps = rng.exponential(req_pairs / rate, size=len(reqs))
+        arrivals = np.cumsum(gaps)
+
+    def worker(k):
+        tickets = []
+        for j, r in enumerate(per_thread[k]):
+            if arrivals is not None:
+                due = arrivals[k + j * n_threads]
+                now = time.perf_counter() - t_start
+                if due > now:
+                    time.sleep(due - now)
+            while True:
+                try:
+                    t0 = time.perf_counter()
+                    tickets.append((x.submit(r), t0))
+                    break
+                except sg.XCError as e:
+                    if e.code != -8:
+                        raise
+                    time.sleep(0.0005)
+            # keep a bounded number in flight per thread
+            while len(tickets) > 8:
+                tk, t0 = tickets.pop(0)
+                x.wait(tk, timeout_ms=120000)
+                with lock:
+                    lat.append(time.perf_counter() - t0)
+        for tk, t0 in tickets:
+            x.wait(tk, timeout_ms=120000)
+            with lock:
+                lat.append(time.perf_counter() - t0)
+
+    th = [threading.Thread(target=worker, args=(k,)) for k in range(n_threads)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    dt = time.perf_counter() - t_start
+    lat_ms = sorted(1000.0 * v for v in lat)
+    p50 = lat_ms[len(lat_ms) // 2]
+    p99 = lat_ms[min(len(lat_ms) - 1, int(round(0.99 * (len(lat_ms) - 1))))]
+    return len(reqs) * req_pairs / dt, p50, p99
+
+
+def run_ours(args):
+    import torch
+    import satsuma2_gb300 as sg
+    from satsuma2_gb300 import build
+    rank, world, local = dist_env()
+    if world > 1 and not torch.distributed.is_initialized():
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    build.build()
+    items = workload()
+    x = sg.XCorr(target_total=TARGET_TOTAL, device=local)
+    # A dedicated stream: the library captures its launches into a CUDA graph,
+    # which the legacy default stream does not allow.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    batch = x.upload(items)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        batch.run(sptr)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- timed region: K device-resident steps ----
+    step_ms, stage = [], []
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            stage.append(batch.run_timed(sptr))
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = float(np.mean(step_ms))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = N_PAIRS * world / (ms / 1000.0)
+    launches = args.steps * batch.launches()
+    res_dev = batch.results()
+
+    # ---- end to end through the C ABI with host buffers ----
+    arr, keep = sg.make_pairs(items)
+    cap = max(64, 32 * len(items))
+    out = np.zeros(cap, sg.RESULT_DTYPE)
+    n_out = ctypes.c_size_t()
+    for _ in range(2):
+        sg._check(x.lib.xc_align_pairs(x.ctx, arr, len(arr), out.ctypes.data, cap, ctypes.byref(n_out), None), "e2e")
+    e2e_t = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sg._check(x.lib.xc_align_pairs(x.ctx, arr, len(arr), out.ctypes.data, cap, ctypes.byref(n_out), None), "e2e")
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    h2d, d2h = x.transfer_stats()
+    e2e_val = N_PAIRS * world / float(np.mean(e2e_t))
+    same = n_out.value == len(res_dev)
+
+    # ---- plain: one pair per call ----
+    plain_n = 256
+    x.align([items[0]])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for it in items[:plain_n]:
+        sg._check(x.lib.xc_align_pairs(x.ctx, sg.make_pairs([it])[0], 1, out.ctypes.data, cap,
+                                       ctypes.byref(n_out), None), "plain")
+    plain = plain_n / (time.perf_counter() - t0)
+
+    # ---- served: continuous batching, saturating and at a fixed arrival rate ----
+    xs = sg.XCorr(target_total=TARGET_TOTAL, device=local, max_batch=2048)
+    serve_run(xs, items, total=4096)   # warm
+    served, p50_sat, p99_sat = serve_run(xs, items, n_threads=8, req_pairs=64, total=32768)
+    rate = 200000.0
+    _, p50, p99 = serve_run(xs, items, n_threads=8, req_pairs=16, total=16384, rate=rate)
+    xs.close()
+
+    peaks, peak_kind = measured_peaks()
+    corr_ms = float(np.mean([s[0] for s in stage]))
+    scan_ms = float(np.mean([s[1] for s in stage]))
+    fin_ms = float(np.mean([s[2] for s in stage]))
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    flops = fft_flops_per_pair() * N_PAIRS
+    achieved = flops / (corr_ms / 1000.0) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("corr_kernel_dram_bytes_per_launch")
+    clocks = clk.summary()
+
+    if rank != 0:
+        return 0
+    cpu = cpu_baseline(items, seconds=args.ref_seconds) if (world == 1 and not args.no_cpu) else None
+    out_line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded uniform batch, seed %d)" % SEED,
+        "config": {"workload": "batched uniform: %d chunk pairs 4096x4096 bp, both strands, FFT 8192, "
+                               "cutoff 1.8, min_prob 0.99 (slave-faithful)" % N_PAIRS,
+                   "pairs_per_step": N_PAIRS, "fft_len": 8192, "target_total": TARGET_TOTAL,
+                   "l2": "512 MB buffer written before every timed step",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "results_match_device_run": bool(same)},
+        "plain_pairs_per_s": plain, "served_pairs_per_s": served, "served_vs_plain": served / plain,
+        "served_p50_ms_saturated": p50_sat, "served_p99_ms_saturated": p99_sat,
+        "p50_ms": p50, "p99_ms": p99, "latency_arrival_rate_pairs_per_s": rate,
+        "stage_ms": {"corr_findtop": corr_ms, "scan_filter": scan_ms, "finalize": fin_ms},
+        "roofline": {"bound": "fp32", "kernel": "corr_kernel<13>", "achieved": achieved, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
+                     "peak_source": "FP32 FMA pipe: 152 SMs x 128 lanes x 2 x %s sm_max_mhz (%s)"
+                                    % (sm_max, peak_kind),
+                     "algorithmic_flops_per_launch": flops},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+        "results_per_step": len(res_dev),
+    }
+    print(json.dumps(out_line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

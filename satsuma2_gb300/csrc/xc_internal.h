@@ -1,0 +1,114 @@
+// Internal definitions shared by the kernels (xc_kernels.cu) and the host
+// runtime (xc_runtime.cu).  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace xc {
+
+constexpr int MIN_LOG2L = 10;    // FFT length 1024
+constexpr int MAX_LOG2L = 14;    // FFT length 16384 (shared-memory resident)
+constexpr int NT_CORR = 512;     // threads of the correlation kernel
+constexpr int NT_SCAN = 128;     // threads of the scan kernel
+constexpr int OFF_CHUNK = 1024;  // offsets staged per scan round
+constexpr int WINDOW = 46;       // DoOne window: m_minLen + 1 positions (CrossCorr.cc:701-705)
+constexpr int MIN_HITS = 19;     // ACGT windows pass when 100*hits > 1889 (CrossCorr.cc:675)
+
+// Pair flags written by the correlation kernel, read by the scan kernel.
+enum : uint32_t {
+  PF_FAST = 1u,        // use cutoff_fast
+  PF_GENERIC = 2u,     // some byte outside A/C/G/T: byte-table scan path
+  PF_INVALID = 4u,     // some byte >= 128: pair rejected
+};
+
+struct __align__(16) PairDesc {
+  uint32_t t_off, q_off;   // byte offsets of the chunks in the sequence pool
+  int32_t tlen, qlen;
+  int32_t log2L;           // FFT length
+  uint32_t flags;          // PF_FAST from the host
+  uint32_t off_base;       // FindTop offsets: strand s at off_base + s*L
+  uint32_t pad;
+};
+
+// Per-FFT-length device tables (host-built in double, rounded once).
+struct LTables {
+  const float2* twN;       // exp(-2*pi*i*k/N), k < N, N = L/2
+  const float2* twL;       // exp(-2*pi*i*k/L), k < N
+  const uint16_t* pos_of;  // DIF output position of bin k, k < N
+  const double* ent;       // Ent(p) for p = (a4/4)/k: [k][a4], k <= win, a4 <= 4*win
+};
+
+// One kept match, strand-local coordinates.  key = FindTop offset index.
+struct __align__(16) DevResult {
+  int32_t key;
+  int32_t tstart;
+  int32_t qstart;
+  int32_t len;
+  double prob;
+  double ident;
+};
+
+struct __align__(16) DevResultX {   // overflow record
+  int32_t slot;                     // pair*2 + strand
+  int32_t pad[3];
+  DevResult r;
+};
+
+struct __align__(16) DbgSeg {
+  int32_t slot, key, tstart, qstart, len, pad[3];
+};
+
+struct CorrParams {
+  const PairDesc* pairs;
+  const uint8_t* pool;
+  int first;                // first pair index of this launch (bucket)
+  LTables tab;
+  double cutoff, cutoff_fast;
+  int* off_list;            // offsets output
+  int* off_cnt;             // [pair*2 + strand]
+  uint32_t* pair_flags;     // [pair]
+  float* dbg_sig;           // optional: [pair*2+strand][2][4][L]
+  float* dbg_xc;            // optional: [pair*2+strand][L]
+};
+
+struct ScanParams {
+  const PairDesc* pairs;
+  const uint8_t* pool;
+  int first;
+  const int* off_list;
+  const int* off_cnt;
+  const uint32_t* pair_flags;
+  const int8_t* score;      // [128*128] (int)(DNA_EqualAmb*100+0.5)
+  const double* eq;         // [128*128] DNA_Equal
+  const double* gcw;        // [128] DNA_C + DNA_G
+  const double* ptable;     // ProbTable [512*2048] or nullptr
+  double ptable_cutoff;
+  double min_prob;
+  double target_total;
+  float screen_expect;      // -log(min_prob) * 1.01 (FP32 screen bound), +inf if min_prob <= 0
+  float target_total_f;
+  int min_len;
+  int slots;                // result slots per pair strand
+  DevResult* res;           // [pair*2+strand][slots]
+  int* res_cnt;             // [pair*2+strand]
+  DevResultX* ovf;
+  int* ovf_cnt;
+  int ovf_cap;
+  int* err;                 // bit 0: overflow pool full; bit 1: debug buffer full
+  DbgSeg* dbg;              // optional raw segments
+  int* dbg_cnt;
+  int dbg_cap;
+};
+
+// Launchers (xc_kernels.cu).
+cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t s);
+cudaError_t launch_scan(int log2L, const ScanParams& p, int npairs, cudaStream_t s);
+cudaError_t launch_finalize(const int* res_cnt, const DevResult* res, int slots, int nslots,
+                            int* dense_base, DevResult* dense, int* scan_tmp, cudaStream_t s);
+cudaError_t upload_constants(const unsigned char* rc256, const uchar4* w4q128,
+                             const double* w4d /*4*128*/);
+size_t corr_smem_bytes(int log2L);
+size_t scan_smem_bytes(int log2L);
+cudaError_t prepare_kernels();
+
+}  // namespace xc

@@ -1,0 +1,807 @@
+// Host runtime of libsatsuma2_gb300.so: device tables, batch packing,
+// launch sequencing (graph-captured), result assembly and the C ABI declared in
+// include/satsuma2_xcorr.h.
+#include "satsuma2_xcorr.h"
+#include "xc_internal.h"
+#include "xc_runtime.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+static_assert(sizeof(xc_result) == 72, "xc_result must match t_result (72 bytes)");
+static_assert(sizeof(xc_block) == 28, "xc_block must match t_pair (28 bytes)");
+
+namespace xc {
+
+// ---------------------------------------------------------------------------
+// DNA codec: DNACodec::DNACodec (analysis/DNAVector.cc:13-58)
+// ---------------------------------------------------------------------------
+struct Codec {
+  double w[4][256];
+  unsigned char rc[256];
+  Codec() {
+    memset(w, 0, sizeof(w));
+    memset(rc, 0, sizeof(rc));
+    const double third = 1. / 3.;
+    set('A', 1., 0., 0., 0., 'T');
+    set('C', 0., 1., 0., 0., 'G');
+    set('G', 0., 0., 1., 0., 'C');
+    set('T', 0., 0., 0., 1., 'A');
+    set('K', 0., 0., 0.5, 0.5, 'M');
+    set('M', 0.5, 0.5, 0., 0., 'K');
+    set('R', 0.5, 0., 0.5, 0., 'Y');
+    set('Y', 0., 0.5, 0., 0.5, 'R');
+    set('S', 0., 0.5, 0.5, 0., 'S');
+    set('W', 0.5, 0., 0., 0.5, 'W');
+    set('B', 0., third, third, third, 'V');
+    set('V', third, third, third, 0., 'B');
+    set('H', third, third, 0., third, 'D');
+    set('D', third, 0., third, third, 'H');
+    set('-', 0., 0., 0., 0., '-');
+    set('N', 0.25, 0.25, 0.25, 0.25, 'N');
+    set('X', 0.25, 0.25, 0.25, 0.25, 'X');
+  }
+  void set(int l, double a, double c, double g, double t, int r) {
+    w[0][l] = a; w[1][l] = c; w[2][l] = g; w[3][l] = t; rc[l] = (unsigned char)r;
+  }
+  // DNA_Equal (DNAVector.cc:390-403)
+  double equal(int a, int b) const {
+    double s = w[0][a] * w[0][b];
+    s = s + w[1][a] * w[1][b];
+    s = s + w[2][a] * w[2][b];
+    s = s + w[3][a] * w[3][b];
+    return s + 0.;
+  }
+  // DNA_EqualAmb (DNAVector.cc:372-387)
+  double equal_amb(int a, int b) const {
+    if (a == b && a != 'N') return 1.;
+    return equal(a, b);
+  }
+};
+
+static const Codec& codec() {
+  static Codec c;
+  return c;
+}
+
+// Radix plan of the N-point transforms (must match fft_forward in the kernels).
+static std::vector<int> radix_plan(int log2N) {
+  switch (log2N) {
+    case 9: return {8, 8, 8};
+    case 10: return {16, 16, 4};
+    case 11: return {16, 16, 8};
+    case 12: return {16, 16, 16};
+    case 13: return {16, 16, 16, 2};
+  }
+  return {};
+}
+
+// Bin k held at DIF output position p: p = d0*r0 + p', k = r0 + R0*k(p').
+static std::vector<uint16_t> dif_positions(int log2N) {
+  const int N = 1 << log2N;
+  std::vector<int> R = radix_plan(log2N);
+  std::vector<uint16_t> pos_of(N);
+  for (int p = 0; p < N; p++) {
+    int k = 0, mult = 1, span = N, rem = p;
+    for (int r : R) {
+      const int d = span / r;
+      const int dig = rem / d;
+      rem %= d;
+      k += dig * mult;
+      mult *= r;
+      span = d;
+    }
+    pos_of[k] = (uint16_t)p;
+  }
+  return pos_of;
+}
+
+static int cuda_err(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return XC_OK;
+  fprintf(stderr, "satsuma2_gb300: %s: %s\n", what, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? XC_ERR_NOMEM : XC_ERR_CUDA;
+}
+#define XC_CHECK(call)                                        \
+  do {                                                        \
+    int _r = cuda_err((call), #call);                         \
+    if (_r != XC_OK) return _r;                               \
+  } while (0)
+
+static int build_tables(Ctx* c) {
+  for (int lg = MIN_LOG2L; lg <= MAX_LOG2L; lg++) {
+    const int L = 1 << lg, N = L / 2, win = L / 512;
+    std::vector<float2> twN(N), twL(N);
+    for (int k = 0; k < N; k++) {
+      const double a = -2.0 * M_PI * (double)k / (double)N;
+      twN[k] = make_float2((float)cos(a), (float)sin(a));
+      const double b = -2.0 * M_PI * (double)k / (double)L;
+      twL[k] = make_float2((float)cos(b), (float)sin(b));
+    }
+    std::vector<uint16_t> pos = dif_positions(lg - 1);
+    // Ent(p) for p = (a4/4)/k (CrossCorr.cc:28-33,80-84), same double ops.
+    const int row = 4 * win + 1;
+    std::vector<double> ent((size_t)(win + 1) * row, 0.0);
+    for (int k = 1; k <= win; k++)
+      for (int a4 = 0; a4 <= 4 * k; a4++) {
+        double p = (double)a4 * 0.25;
+        p /= (double)k;
+        ent[(size_t)k * row + a4] = p < 0.001 ? 0.0 : p * log(p) / 0.69314718056;
+      }
+    DevTables& t = c->tab[lg];
+    XC_CHECK(cudaMalloc(&t.twN, N * sizeof(float2)));
+    XC_CHECK(cudaMalloc(&t.twL, N * sizeof(float2)));
+    XC_CHECK(cudaMalloc(&t.pos_of, N * sizeof(uint16_t)));
+    XC_CHECK(cudaMalloc(&t.ent, ent.size() * sizeof(double)));
+    XC_CHECK(cudaMemcpy(t.twN, twN.data(), N * sizeof(float2), cudaMemcpyHostToDevice));
+    XC_CHECK(cudaMemcpy(t.twL, twL.data(), N * sizeof(float2), cudaMemcpyHostToDevice));
+    XC_CHECK(cudaMemcpy(t.pos_of, pos.data(), N * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    XC_CHECK(cudaMemcpy(t.ent, ent.data(), ent.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  const Codec& cd = codec();
+  std::vector<int8_t> score(128 * 128);
+  std::vector<double> eq(128 * 128), gcw(128);
+  for (int a = 0; a < 128; a++) {
+    for (int b = 0; b < 128; b++) {
+      score[a * 128 + b] = (int8_t)(int)(cd.equal_amb(a, b) * 100.0 + 0.5);   // CrossCorr.cc:547-553
+      eq[a * 128 + b] = cd.equal(a, b);
+    }
+    gcw[a] = cd.w[1][a] + cd.w[2][a];   // DNA_C + DNA_G (AlignProbability.cc:88)
+  }
+  XC_CHECK(cudaMalloc(&c->d_score, score.size()));
+  XC_CHECK(cudaMalloc(&c->d_eq, eq.size() * sizeof(double)));
+  XC_CHECK(cudaMalloc(&c->d_gcw, gcw.size() * sizeof(double)));
+  XC_CHECK(cudaMemcpy(c->d_score, score.data(), score.size(), cudaMemcpyHostToDevice));
+  XC_CHECK(cudaMemcpy(c->d_eq, eq.data(), eq.size() * sizeof(double), cudaMemcpyHostToDevice));
+  XC_CHECK(cudaMemcpy(c->d_gcw, gcw.data(), gcw.size() * sizeof(double), cudaMemcpyHostToDevice));
+  // Constant-memory codec: RC table, quarter-unit weights, double weights.
+  uchar4 w4q[128];
+  double wd[4 * 128];
+  for (int a = 0; a < 128; a++) {
+    unsigned char q[4];
+    for (int ch = 0; ch < 4; ch++) {
+      const double v = cd.w[ch][a] * 4.0;
+      q[ch] = (v == std::floor(v)) ? (unsigned char)v : 0;   // one-third letters take the double path
+      wd[ch * 128 + a] = cd.w[ch][a];
+    }
+    w4q[a] = make_uchar4(q[0], q[1], q[2], q[3]);
+  }
+  XC_CHECK(upload_constants(cd.rc, w4q, wd));
+  return XC_OK;
+}
+
+// ProbTable::Setup (ProbTable.cc:15-56): 511 rows of 2047 bisection cutoffs,
+// built on the host with the same double arithmetic, across host threads.
+static void build_probtable(double size, std::vector<double>& tab) {
+  tab.assign(512 * 2048, -1.0);
+  auto raw = [size](int length, double ident, double ident_expect) {
+    const double p = ident_expect;
+    const double s = sqrt(p * (1. - p) * (double)length);
+    const double m = p * (double)length;
+    const double x = (double)length * ident;
+    const double cdf = 0.5 * (1. + erf((m - x) / s / 1.414213562));
+    return exp(-(cdf * size));
+  };
+  auto rows = [&](int lo, int hi) {
+    for (int i = lo; i < hi; i++) {
+      const double ie = (double)i / ((double)512 - 1);
+      double* t = &tab[(size_t)i * 2048];
+      t[0] = 2.;
+      for (int j = 1; j < 2048; j++) {
+        double mn = 0, mx = 1, mid;
+        while (mx - mn > 0.00000001) {
+          mid = (mx + mn) / 2.0;
+          if (raw(j, mid, ie) != 0.0) mx = mid;
+          else mn = mid;
+        }
+        t[j] = (mx + mn) / 2.0;
+      }
+    }
+  };
+  unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> th;
+  for (unsigned w = 0; w < nt; w++)
+    th.emplace_back(rows, 1 + (int)(511 * w / nt), 1 + (int)(511 * (w + 1) / nt));
+  for (auto& t : th) t.join();
+}
+
+// ---------------------------------------------------------------------------
+// Batches
+// ---------------------------------------------------------------------------
+static int log2_of(int L) {
+  int l = 0;
+  while ((1 << l) < L) l++;
+  return (1 << l) == L ? l : -1;
+}
+
+int pair_log2L(const xc_params& p, const xc_pair& q) {
+  int L;
+  if (p.fft_len > 0) L = p.fft_len;
+  else if (p.fft_len == 0) L = 2 * p.t_chunk;
+  else {
+    const int m = std::max(q.tlen, q.qlen);
+    L = 1024;
+    while (L < 2 * m) L *= 2;
+  }
+  return log2_of(L);
+}
+
+template <class T>
+static int dev_grow(T*& ptr, size_t& cap, size_t need) {
+  if (need <= cap && ptr) return XC_OK;
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  cap = 0;
+  size_t n = std::max<size_t>(need, 1);
+  n += n / 4;
+  XC_CHECK(cudaMalloc(&ptr, n * sizeof(T)));
+  cap = n;
+  return XC_OK;
+}
+
+template <class T>
+static int host_grow(T*& ptr, size_t& cap, size_t need) {
+  if (need <= cap && ptr) return XC_OK;
+  if (ptr) cudaFreeHost(ptr);
+  ptr = nullptr;
+  cap = 0;
+  size_t n = std::max<size_t>(need, 1);
+  n += n / 4;
+  XC_CHECK(cudaHostAlloc(&ptr, n * sizeof(T), cudaHostAllocDefault));
+  cap = n;
+  return XC_OK;
+}
+
+static void parallel_for(size_t n, size_t grain, const std::function<void(size_t, size_t)>& f) {
+  unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  if (n < grain * 2 || nt == 1) {
+    f(0, n);
+    return;
+  }
+  nt = (unsigned)std::min<size_t>(nt, (n + grain - 1) / grain);
+  std::vector<std::thread> th;
+  for (unsigned w = 1; w < nt; w++) th.emplace_back(f, n * w / nt, n * (w + 1) / nt);
+  f(0, n / nt);
+  for (auto& t : th) t.join();
+}
+
+Batch::~Batch() {
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  if (graph_exec_timed) cudaGraphExecDestroy(graph_exec_timed);
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+  cudaFree(d_pool); cudaFree(d_desc); cudaFree(d_off); cudaFree(d_offcnt); cudaFree(d_flags);
+  cudaFree(d_res); cudaFree(d_rescnt); cudaFree(d_ovf); cudaFree(d_misc); cudaFree(d_base);
+  cudaFree(d_dense); cudaFree(d_dbg); cudaFree(d_dbg_sig); cudaFree(d_dbg_xc);
+  cudaFreeHost(h_pool); cudaFreeHost(h_desc); cudaFreeHost(h_base); cudaFreeHost(h_dense);
+  cudaFreeHost(h_misc); cudaFreeHost(h_ovf);
+}
+
+// Packs pairs into the batch's pinned staging and device buffers (async H2D
+// on stream).  Pairs are bucketed by FFT length; device order = bucket order.
+int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t stream) {
+  if (n > (size_t)INT32_MAX / 4) return XC_ERR_ARG;
+  b->n = (int)n;
+  b->meta.assign(pairs, pairs + n);
+  b->order.resize(n);
+  b->log2L.resize(n);
+  int counts[MAX_LOG2L + 1] = {0};
+  for (size_t i = 0; i < n; i++) {
+    const xc_pair& p = pairs[i];
+    if (p.tlen < 0 || p.qlen < 0 || (p.tlen && !p.tseq) || (p.qlen && !p.qseq)) return XC_ERR_ARG;
+    const int lg = pair_log2L(c->prm, p);
+    if (lg < MIN_LOG2L || lg > MAX_LOG2L) return XC_ERR_UNSUPPORTED;
+    if (p.tlen > (1 << lg) / 2 || p.qlen > (1 << lg) / 2) return XC_ERR_INPUT;
+    b->log2L[i] = lg;
+    counts[lg]++;
+  }
+  // bucket order
+  b->buckets.clear();
+  int start = 0;
+  int fill[MAX_LOG2L + 1];
+  for (int lg = MIN_LOG2L; lg <= MAX_LOG2L; lg++) {
+    fill[lg] = start;
+    if (counts[lg]) b->buckets.push_back({lg, start, counts[lg]});
+    start += counts[lg];
+  }
+  for (size_t i = 0; i < n; i++) b->order[fill[b->log2L[i]]++] = (int)i;
+  // pool and offset-list layout
+  std::vector<uint64_t> toff(n), qoff(n);
+  uint64_t pool = 0, offl = 0;
+  b->desc_host.resize(n);
+  for (size_t d = 0; d < n; d++) {
+    const xc_pair& p = pairs[b->order[d]];
+    const int lg = b->log2L[b->order[d]];
+    toff[d] = pool;
+    pool += ((uint64_t)p.tlen + 15) & ~15ull;
+    qoff[d] = pool;
+    pool += ((uint64_t)p.qlen + 15) & ~15ull;
+    PairDesc& D = b->desc_host[d];
+    D.t_off = (uint32_t)toff[d];
+    D.q_off = (uint32_t)qoff[d];
+    D.tlen = p.tlen;
+    D.qlen = p.qlen;
+    D.log2L = lg;
+    D.flags = p.fast ? PF_FAST : 0u;
+    D.off_base = (uint32_t)offl;
+    D.pad = 0;
+    offl += 2ull << lg;
+  }
+  if (pool >= (1ull << 32) || offl >= (1ull << 32)) return XC_ERR_ARG;
+  const size_t nslots = 2 * n;
+  const size_t slots = (size_t)b->slots;
+  int r;
+  if ((r = host_grow(b->h_pool, b->cap_h_pool, pool + 16)) != XC_OK) return r;
+  if ((r = host_grow(b->h_desc, b->cap_h_desc, n)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_pool, b->cap_pool, pool + 16)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_desc, b->cap_desc, n)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_off, b->cap_off, offl)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_offcnt, b->cap_offcnt, nslots)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_flags, b->cap_flags, n)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_res, b->cap_res, nslots * slots)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_rescnt, b->cap_rescnt, nslots)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_ovf, b->cap_ovf, (size_t)b->ovf_cap)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_misc, b->cap_misc, 4)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_base, b->cap_base, nslots + 1)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_dense, b->cap_dense, nslots * slots)) != XC_OK) return r;
+  if ((r = host_grow(b->h_base, b->cap_h_base, nslots + 1)) != XC_OK) return r;
+  if ((r = host_grow(b->h_misc, b->cap_h_misc, 4)) != XC_OK) return r;
+  b->pool_bytes = pool;
+  // gather sequences into pinned staging (threads for large batches)
+  uint8_t* hp = b->h_pool;
+  const std::vector<int>& ord = b->order;
+  parallel_for(n, 256, [&](size_t lo, size_t hi) {
+    for (size_t d = lo; d < hi; d++) {
+      const xc_pair& p = pairs[ord[d]];
+      if (p.tlen) memcpy(hp + toff[d], p.tseq, (size_t)p.tlen);
+      if (p.qlen) memcpy(hp + qoff[d], p.qseq, (size_t)p.qlen);
+    }
+  });
+  memcpy(b->h_desc, b->desc_host.data(), n * sizeof(PairDesc));
+  XC_CHECK(cudaMemcpyAsync(b->d_pool, b->h_pool, pool, cudaMemcpyHostToDevice, stream));
+  XC_CHECK(cudaMemcpyAsync(b->d_desc, b->h_desc, n * sizeof(PairDesc), cudaMemcpyHostToDevice, stream));
+  b->h2d_bytes = pool + n * sizeof(PairDesc);
+  b->graph_valid = false;
+  b->graph_timed_valid = false;
+  return XC_OK;
+}
+
+// Enqueues the kernels of one batch on stream.
+static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
+  const int nslots = 2 * b->n;
+  XC_CHECK(cudaMemsetAsync(b->d_misc, 0, 4 * sizeof(int), s));
+  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[0], s, cudaEventRecordExternal));
+  for (const Bucket& bk : b->buckets) {
+    const DevTables& t = c->tab[bk.log2L];
+    CorrParams cp{};
+    cp.pairs = b->d_desc;
+    cp.pool = b->d_pool;
+    cp.first = bk.first;
+    cp.tab.twN = t.twN;
+    cp.tab.twL = t.twL;
+    cp.tab.pos_of = t.pos_of;
+    cp.tab.ent = t.ent;
+    cp.cutoff = c->prm.cutoff;
+    cp.cutoff_fast = c->prm.cutoff_fast;
+    cp.off_list = b->d_off;
+    cp.off_cnt = b->d_offcnt;
+    cp.pair_flags = b->d_flags;
+    cp.dbg_sig = b->d_dbg_sig;
+    cp.dbg_xc = b->d_dbg_xc;
+    XC_CHECK(launch_corr(bk.log2L, cp, bk.count, s));
+  }
+  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[1], s, cudaEventRecordExternal));
+  for (const Bucket& bk : b->buckets) {
+    ScanParams sp{};
+    sp.pairs = b->d_desc;
+    sp.pool = b->d_pool;
+    sp.first = bk.first;
+    sp.off_list = b->d_off;
+    sp.off_cnt = b->d_offcnt;
+    sp.pair_flags = b->d_flags;
+    sp.score = c->d_score;
+    sp.eq = c->d_eq;
+    sp.gcw = c->d_gcw;
+    sp.ptable = c->prm.use_prob_table ? c->d_ptable : nullptr;
+    sp.ptable_cutoff = c->prm.prob_table_cutoff;
+    sp.min_prob = c->prm.min_prob;
+    sp.target_total = c->prm.target_total;
+    // Screen bound on expect = cdf*targetTotal: keep if exp(-expect) >= min_prob.
+    double bound = c->prm.min_prob > 0 ? -log(c->prm.min_prob) : INFINITY;
+    sp.screen_expect = bound < 0 ? 0.f : (float)(bound * 1.01 + 1e-30);
+    sp.target_total_f = (float)c->prm.target_total;
+    sp.min_len = c->prm.min_len;
+    sp.slots = b->slots;
+    sp.res = b->d_res;
+    sp.res_cnt = b->d_rescnt;
+    sp.ovf = b->d_ovf;
+    sp.ovf_cnt = b->d_misc + 0;
+    sp.ovf_cap = b->ovf_cap;
+    sp.err = b->d_misc + 1;
+    sp.dbg = b->d_dbg;
+    sp.dbg_cnt = b->d_misc + 2;
+    sp.dbg_cap = b->dbg_cap;
+    XC_CHECK(launch_scan(bk.log2L, sp, bk.count, s));
+  }
+  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[2], s, cudaEventRecordExternal));
+  XC_CHECK(launch_finalize(b->d_rescnt, b->d_res, b->slots, nslots, b->d_base, b->d_dense, nullptr, s));
+  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[3], s, cudaEventRecordExternal));
+  return XC_OK;
+}
+
+int batch_launch_count(const Batch* b) { return 2 * (int)b->buckets.size() + 2; }
+
+// Runs the batch; replays a captured CUDA graph when the batch is unchanged.
+int batch_run(Ctx* c, Batch* b, cudaStream_t s, bool use_graph, bool timed) {
+  if (timed)
+    for (auto& e : b->ev)
+      if (!e) XC_CHECK(cudaEventCreate(&e));
+  if (!use_graph || b->d_dbg || b->d_dbg_sig || b->d_dbg_xc) return batch_enqueue(c, b, s, timed);
+  cudaGraphExec_t& ge = timed ? b->graph_exec_timed : b->graph_exec;
+  bool& valid = timed ? b->graph_timed_valid : b->graph_valid;
+  cudaStream_t& gs = timed ? b->graph_timed_stream : b->graph_stream;
+  if (!valid || gs != s) {
+    if (ge) cudaGraphExecDestroy(ge);
+    ge = nullptr;
+    cudaGraph_t g;
+    XC_CHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int r = batch_enqueue(c, b, s, timed);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (r != XC_OK) return r;
+    XC_CHECK(e);
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    XC_CHECK(e);
+    valid = true;
+    gs = s;
+  }
+  XC_CHECK(cudaGraphLaunch(ge, s));
+  return XC_OK;
+}
+
+// Reads results back and assembles xc_result records in original pair order.
+int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, size_t* n_out,
+                  size_t* pair_counts) {
+  const int n = b->n, nslots = 2 * n;
+  XC_CHECK(cudaMemcpyAsync(b->h_base, b->d_base, (nslots + 1) * sizeof(int), cudaMemcpyDeviceToHost, s));
+  XC_CHECK(cudaMemcpyAsync(b->h_misc, b->d_misc, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  XC_CHECK(cudaStreamSynchronize(s));
+  const int total = b->h_base[nslots];
+  const int novf = b->h_misc[0];
+  const int err = b->h_misc[1];
+  if (err & 1) return XC_ERR_CAPACITY;   // caller re-runs with a bigger overflow pool
+  int r;
+  if ((r = host_grow(b->h_dense, b->cap_h_dense, (size_t)total + 1)) != XC_OK) return r;
+  if (total) XC_CHECK(cudaMemcpyAsync(b->h_dense, b->d_dense, total * sizeof(DevResult), cudaMemcpyDeviceToHost, s));
+  std::vector<int> flags(n);
+  XC_CHECK(cudaMemcpyAsync(flags.data(), b->d_flags, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  std::vector<DevResultX> ovf;
+  if (novf > 0) {
+    ovf.resize(novf);
+    XC_CHECK(cudaMemcpyAsync(ovf.data(), b->d_ovf, novf * sizeof(DevResultX), cudaMemcpyDeviceToHost, s));
+  }
+  XC_CHECK(cudaStreamSynchronize(s));
+  b->d2h_bytes = (uint64_t)(nslots + 1) * sizeof(int) + 4 * sizeof(int) + (uint64_t)total * sizeof(DevResult) +
+                 (uint64_t)n * sizeof(uint32_t) + (uint64_t)novf * sizeof(DevResultX);
+  c->last_h2d = b->h2d_bytes;
+  c->last_d2h = b->d2h_bytes;
+  for (int d = 0; d < n; d++)
+    if (flags[d] & PF_INVALID) return XC_ERR_INPUT;
+  // per slot record lists (device order)
+  std::vector<std::vector<DevResult>> extra;
+  std::vector<int> extra_of;
+  if (novf > 0) {
+    extra_of.assign(nslots, -1);
+    for (const DevResultX& x : ovf) {
+      if (extra_of[x.slot] < 0) {
+        extra_of[x.slot] = (int)extra.size();
+        extra.emplace_back();
+      }
+      extra[extra_of[x.slot]].push_back(x.r);
+    }
+  }
+  // counts per original pair
+  std::vector<size_t> cnt(n, 0);
+  std::vector<int> dev_of(n);
+  for (int d = 0; d < n; d++) dev_of[b->order[d]] = d;
+  size_t need = 0;
+  for (int i = 0; i < n; i++) {
+    const int d = dev_of[i];
+    for (int s2 = 0; s2 < 2; s2++) {
+      const int sl = 2 * d + s2;
+      size_t k = (size_t)(b->h_base[sl + 1] - b->h_base[sl]);
+      if (novf > 0 && extra_of[sl] >= 0) k += extra[extra_of[sl]].size();
+      cnt[i] += k;
+    }
+    need += cnt[i];
+  }
+  if (n_out) *n_out = need;
+  if (pair_counts)
+    for (int i = 0; i < n; i++) pair_counts[i] = cnt[i];
+  if (need > cap || (!out && need)) return XC_ERR_CAPACITY;
+  size_t o = 0;
+  const int qchunk = c->prm.q_chunk;
+  for (int i = 0; i < n; i++) {
+    const int d = dev_of[i];
+    const xc_pair& p = b->meta[i];
+    for (int s2 = 0; s2 < 2; s2++) {
+      const int sl = 2 * d + s2;
+      std::vector<DevResult> recs(b->h_dense + b->h_base[sl], b->h_dense + b->h_base[sl + 1]);
+      if (novf > 0 && extra_of[sl] >= 0) {
+        const auto& e = extra[extra_of[sl]];
+        recs.insert(recs.end(), e.begin(), e.end());
+        std::sort(recs.begin(), recs.end(), [](const DevResult& a, const DevResult& q) {
+          return a.key < q.key || (a.key == q.key && a.tstart < q.tstart);
+        });
+      }
+      for (const DevResult& rr : recs) {
+        xc_result& x = out[o++];
+        memset(&x, 0, sizeof(x));
+        // FilterMatches coordinate mapping (HomologyByXCorrSlave.cc:175-181, RCQuery :56-60)
+        const int tStart = p.t_chunk_start + rr.tstart;
+        const int qStart = s2 == 0 ? p.q_chunk_start + rr.qstart
+                                   : rr.qstart + (int)p.query_size - p.q_chunk_start - qchunk;
+        x.query_id = p.query_id;
+        x.target_id = p.target_id;
+        x.query_size = p.query_size;
+        x.qstart = (unsigned long)(long)qStart;
+        x.tstart = (unsigned long)(long)tStart;
+        x.len = (unsigned long)(long)rr.len;
+        x.reverse = (unsigned char)s2;
+        x.prob = rr.prob;
+        x.ident = rr.ident;
+      }
+    }
+  }
+  return XC_OK;
+}
+
+int ctx_run_pairs(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, xc_result* out, size_t cap,
+                  size_t* n_out, size_t* pair_counts) {
+  int r = batch_pack(c, b, pairs, n, c->stream);
+  if (r != XC_OK) return r;
+  for (int attempt = 0; attempt < 3; attempt++) {
+    if ((r = batch_run(c, b, c->stream, false)) != XC_OK) return r;
+    r = batch_collect(c, b, c->stream, out, cap, n_out, pair_counts);
+    if (r != XC_ERR_CAPACITY || b->h_misc[1] == 0) return r;
+    // device overflow pool was too small: grow to what was asked and re-run
+    b->ovf_cap = std::max(b->ovf_cap * 4, b->h_misc[0] + 1024);
+    if ((r = dev_grow(b->d_ovf, b->cap_ovf, (size_t)b->ovf_cap)) != XC_OK) return r;
+  }
+  return XC_ERR_CAPACITY;
+}
+
+Batch* new_batch(Ctx* c) {
+  Batch* b = new Batch();
+  b->slots = c->prm.result_slots > 0 ? c->prm.result_slots : 64;
+  b->ovf_cap = 1 << 16;
+  return b;
+}
+
+}  // namespace xc
+
+using namespace xc;
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+const char* xc_version(void) { return "satsuma2_gb300 1.0 (sm_103a)"; }
+
+int xc_create(const xc_params* params, int device, xc_ctx** out) {
+  if (!params || !out) return XC_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) return XC_ERR_CUDA;
+  xc_ctx* c = new xc_ctx();
+  c->prm = *params;
+  if (c->prm.t_chunk <= 0) c->prm.t_chunk = 4096;
+  if (c->prm.q_chunk <= 0) c->prm.q_chunk = 4096;
+  c->device = device;
+  int r = cuda_err(cudaSetDevice(device), "cudaSetDevice");
+  if (r == XC_OK) r = cuda_err(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+  if (r == XC_OK) r = cuda_err(prepare_kernels(), "kernel attributes");
+  if (r == XC_OK) r = build_tables(c);
+  if (r == XC_OK && c->prm.use_prob_table) {
+    build_probtable(c->prm.target_total, c->h_ptable);
+    r = cuda_err(cudaMalloc(&c->d_ptable, c->h_ptable.size() * sizeof(double)), "probtable");
+    if (r == XC_OK)
+      r = cuda_err(cudaMemcpy(c->d_ptable, c->h_ptable.data(), c->h_ptable.size() * sizeof(double),
+                              cudaMemcpyHostToDevice), "probtable copy");
+  }
+  if (r == XC_OK) {
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) snprintf(c->devname, sizeof(c->devname), "%s", prop.name);
+    c->work = new_batch(c);
+  }
+  if (r != XC_OK) {
+    xc_destroy(c);
+    return r;
+  }
+  *out = c;
+  return XC_OK;
+}
+
+int xc_destroy(xc_ctx* c) {
+  if (!c) return XC_ERR_ARG;
+  server_stop(c);
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  delete c->work;
+  for (auto& t : c->tab) {
+    cudaFree(t.twN); cudaFree(t.twL); cudaFree(t.pos_of); cudaFree(t.ent);
+  }
+  cudaFree(c->d_score); cudaFree(c->d_eq); cudaFree(c->d_gcw); cudaFree(c->d_ptable);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return XC_OK;
+}
+
+int xc_align_pairs(xc_ctx* c, const xc_pair* pairs, size_t n, xc_result* out, size_t cap, size_t* n_out,
+                   size_t* pair_counts) {
+  if (!c || (!pairs && n)) return XC_ERR_ARG;
+  if (n_out) *n_out = 0;
+  if (n == 0) return XC_OK;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  const size_t maxb = c->prm.max_batch > 0 ? (size_t)c->prm.max_batch : 4096;
+  size_t done = 0, written = 0;
+  while (done < n) {
+    const size_t m = std::min(maxb, n - done);
+    size_t got = 0;
+    int r = ctx_run_pairs(c, c->work, pairs + done, m, out ? out + written : nullptr,
+                          cap >= written ? cap - written : 0, &got, pair_counts ? pair_counts + done : nullptr);
+    if (r == XC_ERR_CAPACITY) {
+      // report the total needed: finish counting the remaining chunks
+      size_t need = written + got;
+      for (size_t d2 = done + m; d2 < n; d2 += maxb) {
+        const size_t m2 = std::min(maxb, n - d2);
+        size_t g2 = 0;
+        int r2 = ctx_run_pairs(c, c->work, pairs + d2, m2, nullptr, 0, &g2, nullptr);
+        if (r2 != XC_OK && r2 != XC_ERR_CAPACITY) return r2;
+        need += g2;
+      }
+      if (n_out) *n_out = need;
+      return XC_ERR_CAPACITY;
+    }
+    if (r != XC_OK) return r;
+    written += got;
+    done += m;
+  }
+  if (n_out) *n_out = written;
+  return XC_OK;
+}
+
+int xc_batch_upload(xc_ctx* c, const xc_pair* pairs, size_t n, xc_batch** out) {
+  if (!c || !out || (!pairs && n) || n == 0) return XC_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  xc_batch* b = new xc_batch();
+  b->slots = c->prm.result_slots > 0 ? c->prm.result_slots : 64;
+  b->ovf_cap = 1 << 16;
+  int r = batch_pack(c, b, pairs, n, c->stream);
+  if (r == XC_OK) r = cuda_err(cudaStreamSynchronize(c->stream), "upload");
+  if (r != XC_OK) {
+    delete b;
+    return r;
+  }
+  *out = b;
+  return XC_OK;
+}
+
+int xc_batch_run(xc_ctx* c, xc_batch* b, void* stream) {
+  if (!c || !b) return XC_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  return batch_run(c, b, s, true);
+}
+
+int xc_batch_results(xc_ctx* c, xc_batch* b, xc_result* out, size_t cap, size_t* n_out, size_t* pair_counts) {
+  if (!c || !b) return XC_ERR_ARG;
+  cudaSetDevice(c->device);
+  XC_CHECK(cudaDeviceSynchronize());
+  return batch_collect(c, b, c->stream, out, cap, n_out, pair_counts);
+}
+
+int xc_batch_free(xc_ctx* c, xc_batch* b) {
+  if (!c || !b) return XC_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaDeviceSynchronize();
+  delete b;
+  return XC_OK;
+}
+
+int xc_batch_launches(xc_ctx* c, xc_batch* b) {
+  if (!c || !b) return XC_ERR_ARG;
+  return batch_launch_count(b);
+}
+
+int xc_batch_run_timed(xc_ctx* c, xc_batch* b, void* stream, float* stage_ms) {
+  if (!c || !b) return XC_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  int r = batch_run(c, b, s, true, true);
+  if (r != XC_OK) return r;
+  XC_CHECK(cudaEventSynchronize(b->ev[3]));
+  if (stage_ms)
+    for (int i = 0; i < 3; i++) XC_CHECK(cudaEventElapsedTime(&stage_ms[i], b->ev[i], b->ev[i + 1]));
+  return XC_OK;
+}
+
+int xc_transfer_stats(xc_ctx* c, uint64_t* h2d, uint64_t* d2h) {
+  if (!c) return XC_ERR_ARG;
+  if (h2d) *h2d = c->last_h2d;
+  if (d2h) *d2h = c->last_d2h;
+  return XC_OK;
+}
+
+int xc_debug_pair(xc_ctx* c, const xc_pair* pair, float* sig, float* xcv, int* offs, int* n_offs, int* segs,
+                  int* n_segs, int seg_cap, int* fft_len_out) {
+  if (!c || !pair) return XC_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  Batch b;
+  b.slots = c->prm.result_slots > 0 ? c->prm.result_slots : 64;
+  b.ovf_cap = 1 << 16;
+  int r = batch_pack(c, &b, pair, 1, c->stream);
+  if (r != XC_OK) return r;
+  const int L = 1 << b.log2L[0];
+  if (fft_len_out) *fft_len_out = L;
+  b.dbg_cap = 1 << 20;
+  XC_CHECK(cudaMalloc(&b.d_dbg, (size_t)b.dbg_cap * sizeof(DbgSeg)));
+  XC_CHECK(cudaMalloc(&b.d_dbg_sig, (size_t)2 * 8 * L * sizeof(float)));
+  XC_CHECK(cudaMemset(b.d_dbg_sig, 0, (size_t)2 * 8 * L * sizeof(float)));
+  XC_CHECK(cudaMalloc(&b.d_dbg_xc, (size_t)2 * L * sizeof(float)));
+  if ((r = batch_run(c, &b, c->stream, false)) != XC_OK) return r;
+  XC_CHECK(cudaStreamSynchronize(c->stream));
+  int misc[4];
+  XC_CHECK(cudaMemcpy(misc, b.d_misc, sizeof(misc), cudaMemcpyDeviceToHost));
+  uint32_t flag;
+  XC_CHECK(cudaMemcpy(&flag, b.d_flags, sizeof(flag), cudaMemcpyDeviceToHost));
+  if (flag & PF_INVALID) return XC_ERR_INPUT;
+  if (sig) XC_CHECK(cudaMemcpy(sig, b.d_dbg_sig, (size_t)2 * 8 * L * sizeof(float), cudaMemcpyDeviceToHost));
+  if (xcv) XC_CHECK(cudaMemcpy(xcv, b.d_dbg_xc, (size_t)2 * L * sizeof(float), cudaMemcpyDeviceToHost));
+  int oc[2];
+  XC_CHECK(cudaMemcpy(oc, b.d_offcnt, sizeof(oc), cudaMemcpyDeviceToHost));
+  if (n_offs) { n_offs[0] = oc[0]; n_offs[1] = oc[1]; }
+  if (offs) {
+    XC_CHECK(cudaMemcpy(offs, b.d_off, (size_t)oc[0] * sizeof(int), cudaMemcpyDeviceToHost));
+    XC_CHECK(cudaMemcpy(offs + L, b.d_off + L, (size_t)oc[1] * sizeof(int), cudaMemcpyDeviceToHost));
+  }
+  const int nd = std::min(misc[2], b.dbg_cap);
+  std::vector<DbgSeg> dg(nd);
+  if (nd) XC_CHECK(cudaMemcpy(dg.data(), b.d_dbg, nd * sizeof(DbgSeg), cudaMemcpyDeviceToHost));
+  std::sort(dg.begin(), dg.end(), [](const DbgSeg& a, const DbgSeg& q) {
+    if (a.slot != q.slot) return a.slot < q.slot;
+    if (a.key != q.key) return a.key < q.key;
+    return a.tstart < q.tstart;
+  });
+  int ns[2] = {0, 0};
+  for (const DbgSeg& g : dg) {
+    const int s2 = g.slot & 1;
+    if (segs && ns[s2] < seg_cap) {
+      int* p = segs + ((size_t)s2 * seg_cap + ns[s2]) * 3;
+      p[0] = g.tstart; p[1] = g.qstart; p[2] = g.len;
+    }
+    ns[s2]++;
+  }
+  if (n_segs) { n_segs[0] = ns[0]; n_segs[1] = ns[1]; }
+  if (misc[1] & 2) return XC_ERR_CAPACITY;
+  return XC_OK;
+}
+
+int xc_device_name(xc_ctx* c, char* buf, size_t len) {
+  if (!c || !buf || !len) return XC_ERR_ARG;
+  snprintf(buf, len, "%s", c->devname);
+  return XC_OK;
+}
+
+}  // extern "C"

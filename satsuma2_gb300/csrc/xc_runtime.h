@@ -1,0 +1,113 @@
+// Host-side runtime structures shared by xc_runtime.cu and xc_server.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <functional>
+#include <mutex>
+#include <vector>
+
+#include "satsuma2_xcorr.h"
+#include "xc_internal.h"
+
+namespace xc {
+
+struct Bucket {
+  int log2L;
+  int first;
+  int count;
+};
+
+// Device and pinned host buffers of one packed batch of chunk pairs.  Pairs
+// are stored in "device order" (grouped by FFT length); order[d] maps a device
+// index to the caller's index.
+struct Batch {
+  int n = 0;
+  int slots = 64;                 // result slots per pair strand
+  int ovf_cap = 1 << 16;          // overflow records
+  int dbg_cap = 0;
+  std::vector<xc_pair> meta;      // caller's pairs (ids, chunk starts), caller order
+  std::vector<int> order;
+  std::vector<int> log2L;         // per caller index
+  std::vector<Bucket> buckets;
+  std::vector<PairDesc> desc_host;
+  uint64_t pool_bytes = 0, h2d_bytes = 0;
+
+  uint8_t* d_pool = nullptr;      size_t cap_pool = 0;
+  PairDesc* d_desc = nullptr;     size_t cap_desc = 0;
+  int* d_off = nullptr;           size_t cap_off = 0;
+  int* d_offcnt = nullptr;        size_t cap_offcnt = 0;
+  uint32_t* d_flags = nullptr;    size_t cap_flags = 0;
+  DevResult* d_res = nullptr;     size_t cap_res = 0;
+  int* d_rescnt = nullptr;        size_t cap_rescnt = 0;
+  DevResultX* d_ovf = nullptr;    size_t cap_ovf = 0;
+  int* d_misc = nullptr;          size_t cap_misc = 0;   // [0] ovf count [1] err [2] dbg count
+  int* d_base = nullptr;          size_t cap_base = 0;
+  DevResult* d_dense = nullptr;   size_t cap_dense = 0;
+  DbgSeg* d_dbg = nullptr;
+  float* d_dbg_sig = nullptr;
+  float* d_dbg_xc = nullptr;
+
+  uint8_t* h_pool = nullptr;      size_t cap_h_pool = 0;
+  PairDesc* h_desc = nullptr;     size_t cap_h_desc = 0;
+  int* h_base = nullptr;          size_t cap_h_base = 0;
+  DevResult* h_dense = nullptr;   size_t cap_h_dense = 0;
+  int* h_misc = nullptr;          size_t cap_h_misc = 0;
+  DevResultX* h_ovf = nullptr;
+
+  cudaGraphExec_t graph_exec = nullptr;
+  bool graph_valid = false;
+  cudaStream_t graph_stream = nullptr;
+  // stage-timing variant: events between the correlation, scan and finalize launches
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaGraphExec_t graph_exec_timed = nullptr;
+  bool graph_timed_valid = false;
+  cudaStream_t graph_timed_stream = nullptr;
+  uint64_t d2h_bytes = 0;
+
+  ~Batch();
+};
+
+struct Server;
+
+struct DevTables {
+  float2* twN = nullptr;
+  float2* twL = nullptr;
+  uint16_t* pos_of = nullptr;
+  double* ent = nullptr;
+};
+
+struct Ctx {
+  xc_params prm{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;               // serialises the synchronous entry points
+  DevTables tab[MAX_LOG2L + 1];
+  int8_t* d_score = nullptr;
+  double* d_eq = nullptr;
+  double* d_gcw = nullptr;
+  double* d_ptable = nullptr;
+  std::vector<double> h_ptable;
+  Batch* work = nullptr;       // reusable batch of xc_align_pairs
+  Server* server = nullptr;
+  char devname[256] = {0};
+  uint64_t last_h2d = 0, last_d2h = 0;
+};
+
+
+
+int pair_log2L(const xc_params& p, const xc_pair& q);
+Batch* new_batch(Ctx* c);
+int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t stream);
+int batch_run(Ctx* c, Batch* b, cudaStream_t s, bool use_graph, bool timed = false);
+int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, size_t* n_out,
+                  size_t* pair_counts);
+int batch_launch_count(const Batch* b);
+int ctx_run_pairs(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, xc_result* out, size_t cap,
+                  size_t* n_out, size_t* pair_counts);
+void server_stop(Ctx* c);
+
+}  // namespace xc
+
+// The opaque handles of the C ABI.
+struct xc_ctx : public xc::Ctx {};
+struct xc_batch : public xc::Batch {};

@@ -1,0 +1,372 @@
+// Serving: thread-safe submission of chunk-pair requests with continuous
+// batching on one GPU.
+//
+// The slave's -p worker threads (HomologyByXCorrSlave.cc:302-319) each popped
+// a t_pair block and ran it alone.  Here any number of host threads call
+// xc_submit; a scheduler thread packs waiting pairs -- across request
+// boundaries -- into the next free in-flight slot (its own stream and buffers)
+// and launches it while earlier slots are still running, so work that arrives
+// while the GPU is busy joins the next launch.  Requests are admitted against
+// a budget of queued pairs and of the device memory their batches need
+// (measured with cudaMemGetInfo when the server starts); xc_submit answers
+// XC_ERR_BUSY beyond it.  xc_wait is bounded: it returns XC_ERR_TIMEOUT and
+// keeps the ticket.  No device code waits on the host or on other kernels.
+#include "satsuma2_xcorr.h"
+#include "xc_runtime.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+
+namespace xc {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+  uint64_t ticket = 0;
+  std::vector<char> bytes;
+  std::vector<xc_pair> pairs;
+  size_t next = 0;          // next pair to schedule
+  size_t done = 0;          // pairs with results
+  std::vector<std::vector<xc_result>> per_pair;
+  int status = XC_OK;
+  bool complete = false;
+  size_t footprint = 0;     // device bytes accounted at admission
+  Clock::time_point t_submit, t_done;
+};
+
+struct Slot {
+  Batch* b = nullptr;
+  cudaStream_t s = nullptr;
+  cudaEvent_t ev = nullptr;
+  std::vector<std::pair<Request*, size_t>> items;
+  std::vector<xc_pair> pairs;
+  bool busy = false;
+  uint64_t seq = 0;
+};
+
+constexpr int NSLOTS = 3;
+
+struct Server {
+  Ctx* ctx = nullptr;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Request*> queue;
+  std::unordered_map<uint64_t, Request*> reqs;
+  uint64_t next_ticket = 1;
+  size_t queued_pairs = 0, queued_bytes = 0;
+  size_t max_pairs = 0, budget_bytes = 0;
+  bool stop = false;
+  std::thread sched;
+  Slot slots[NSLOTS];
+  uint64_t launch_seq = 0;
+  std::vector<double> lat_ms;
+  uint64_t completed = 0, pairs_done = 0;
+  int device = 0;
+  size_t max_batch = 4096;
+};
+
+// Device bytes one pair needs inside a batch (sequences, offsets, results).
+static size_t pair_footprint(const Ctx* c, const xc_pair& p, int slots) {
+  const int lg = pair_log2L(c->prm, p);
+  const size_t L = lg > 0 ? (size_t)1 << lg : 8192;
+  return (size_t)p.tlen + p.qlen + 32 + 2 * L * sizeof(int) + 2 * (size_t)slots * 2 * sizeof(DevResult) + 64;
+}
+
+static void complete_slot(Server* S, Slot& sl) {
+  const size_t n = sl.items.size();
+  std::vector<size_t> counts(n);
+  size_t need = 0;
+  int r = batch_collect(S->ctx, sl.b, sl.s, nullptr, 0, &need, counts.data());
+  std::vector<xc_result> res;
+  if (r == XC_ERR_CAPACITY || (r == XC_OK && need == 0)) {
+    res.resize(need);
+    r = batch_collect(S->ctx, sl.b, sl.s, res.data(), res.size(), &need, counts.data());
+  }
+  const auto now = Clock::now();
+  std::lock_guard<std::mutex> lk(S->mu);
+  size_t o = 0;
+  for (size_t i = 0; i < n; i++) {
+    Request* q = sl.items[i].first;
+    const size_t pi = sl.items[i].second;
+    if (r == XC_OK) {
+      q->per_pair[pi].assign(res.begin() + o, res.begin() + o + counts[i]);
+      o += counts[i];
+    } else {
+      q->status = r;
+    }
+    q->done++;
+    if (q->done == q->pairs.size() && !q->complete) {
+      q->complete = true;
+      q->t_done = now;
+      S->lat_ms.push_back(std::chrono::duration<double, std::milli>(now - q->t_submit).count());
+      S->completed++;
+      S->pairs_done += q->pairs.size();
+      S->queued_bytes -= std::min(S->queued_bytes, q->footprint);
+    }
+  }
+  sl.items.clear();
+  sl.busy = false;
+  S->cv_done.notify_all();
+}
+
+static void scheduler(Server* S) {
+  cudaSetDevice(S->device);
+  for (;;) {
+    // 1. retire finished slots, oldest first
+    for (;;) {
+      Slot* oldest = nullptr;
+      for (auto& sl : S->slots)
+        if (sl.busy && (!oldest || sl.seq < oldest->seq)) oldest = &sl;
+      if (!oldest) break;
+      if (cudaEventQuery(oldest->ev) != cudaSuccess) break;
+      complete_slot(S, *oldest);
+    }
+    // 2. fill a free slot from the queue
+    Slot* free_slot = nullptr;
+    for (auto& sl : S->slots)
+      if (!sl.busy) { free_slot = &sl; break; }
+    bool launched = false;
+    if (free_slot) {
+      std::unique_lock<std::mutex> lk(S->mu);
+      if (S->stop && S->queue.empty()) {
+        bool any_busy = false;
+        for (auto& sl : S->slots) any_busy |= sl.busy;
+        if (!any_busy) return;
+      }
+      free_slot->items.clear();
+      free_slot->pairs.clear();
+      while (!S->queue.empty() && free_slot->pairs.size() < S->max_batch) {
+        Request* q = S->queue.front();
+        while (q->next < q->pairs.size() && free_slot->pairs.size() < S->max_batch) {
+          free_slot->items.emplace_back(q, q->next);
+          free_slot->pairs.push_back(q->pairs[q->next]);
+          q->next++;
+        }
+        if (q->next == q->pairs.size()) S->queue.pop_front();
+      }
+      S->queued_pairs -= std::min(S->queued_pairs, free_slot->pairs.size());
+      lk.unlock();
+      if (!free_slot->pairs.empty()) {
+        int r = batch_pack(S->ctx, free_slot->b, free_slot->pairs.data(), free_slot->pairs.size(), free_slot->s);
+        if (r == XC_OK) r = batch_run(S->ctx, free_slot->b, free_slot->s, false);
+        if (r == XC_OK && cudaEventRecord(free_slot->ev, free_slot->s) != cudaSuccess) r = XC_ERR_CUDA;
+        free_slot->busy = true;
+        free_slot->seq = ++S->launch_seq;
+        if (r != XC_OK) {
+          std::lock_guard<std::mutex> lk2(S->mu);
+          for (auto& it : free_slot->items) {
+            it.first->status = r;
+            it.first->done++;
+            if (it.first->done == it.first->pairs.size()) {
+              it.first->complete = true;
+              it.first->t_done = Clock::now();
+            }
+          }
+          free_slot->items.clear();
+          free_slot->busy = false;
+          S->cv_done.notify_all();
+        }
+        launched = true;
+      }
+    }
+    if (launched) continue;
+    // 3. idle: wait for the oldest slot or new work
+    Slot* oldest = nullptr;
+    for (auto& sl : S->slots)
+      if (sl.busy && (!oldest || sl.seq < oldest->seq)) oldest = &sl;
+    if (oldest) {
+      std::unique_lock<std::mutex> lk(S->mu);
+      const bool have_work = !S->queue.empty() && free_slot != nullptr;
+      lk.unlock();
+      if (!have_work) {
+        // short polling keeps new arrivals flowing into free slots
+        if (cudaEventQuery(oldest->ev) != cudaSuccess) std::this_thread::sleep_for(std::chrono::microseconds(50));
+      }
+    } else {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_work.wait_for(lk, std::chrono::milliseconds(5), [S] { return S->stop || !S->queue.empty(); });
+      if (S->stop && S->queue.empty()) return;
+    }
+  }
+}
+
+static int server_start(Ctx* c) {
+  if (c->server) return XC_OK;
+  Server* S = new Server();
+  S->ctx = c;
+  S->device = c->device;
+  S->max_batch = c->prm.max_batch > 0 ? (size_t)c->prm.max_batch : 4096;
+  size_t free_b = 0, total_b = 0;
+  cudaSetDevice(c->device);
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+    delete S;
+    return XC_ERR_CUDA;
+  }
+  S->budget_bytes = free_b / 2;
+  S->max_pairs = 64 * S->max_batch;
+  for (auto& sl : S->slots) {
+    sl.b = new_batch(c);
+    if (cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess) {
+      delete S;
+      return XC_ERR_CUDA;
+    }
+  }
+  S->sched = std::thread(scheduler, S);
+  c->server = S;
+  return XC_OK;
+}
+
+void server_stop(Ctx* c) {
+  Server* S = c->server;
+  if (!S) return;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+    S->queue.clear();
+  }
+  S->cv_work.notify_all();
+  if (S->sched.joinable()) S->sched.join();
+  for (auto& sl : S->slots) {
+    if (sl.s) cudaStreamSynchronize(sl.s);
+    delete sl.b;
+    if (sl.ev) cudaEventDestroy(sl.ev);
+    if (sl.s) cudaStreamDestroy(sl.s);
+  }
+  for (auto& kv : S->reqs) delete kv.second;
+  delete S;
+  c->server = nullptr;
+}
+
+}  // namespace xc
+
+using namespace xc;
+
+extern "C" {
+
+int xc_submit(xc_ctx* c, const xc_pair* pairs, size_t n, uint64_t* ticket) {
+  if (!c || !ticket || (!pairs && n) || n == 0) return XC_ERR_ARG;
+  {
+    std::lock_guard<std::mutex> lk(c->mu);
+    int r = server_start(c);
+    if (r != XC_OK) return r;
+  }
+  Server* S = c->server;
+  // copy the caller's sequences (valid only during this call)
+  Request* q = new Request();
+  size_t bytes = 0;
+  for (size_t i = 0; i < n; i++) {
+    if (pairs[i].tlen < 0 || pairs[i].qlen < 0) {
+      delete q;
+      return XC_ERR_ARG;
+    }
+    const int lg = pair_log2L(c->prm, pairs[i]);
+    if (lg < MIN_LOG2L || lg > MAX_LOG2L) {
+      delete q;
+      return XC_ERR_UNSUPPORTED;
+    }
+    if (pairs[i].tlen > (1 << lg) / 2 || pairs[i].qlen > (1 << lg) / 2) {
+      delete q;
+      return XC_ERR_INPUT;
+    }
+    bytes += (size_t)pairs[i].tlen + pairs[i].qlen;
+    q->footprint += pair_footprint(c, pairs[i], S->slots[0].b->slots);
+  }
+  q->bytes.resize(bytes);
+  q->pairs.assign(pairs, pairs + n);
+  size_t o = 0;
+  for (size_t i = 0; i < n; i++) {
+    xc_pair& p = q->pairs[i];
+    if (p.tlen) memcpy(&q->bytes[o], p.tseq, p.tlen);
+    p.tseq = q->bytes.data() + o;
+    o += p.tlen;
+    if (p.qlen) memcpy(&q->bytes[o], p.qseq, p.qlen);
+    p.qseq = q->bytes.data() + o;
+    o += p.qlen;
+  }
+  q->per_pair.resize(n);
+  std::unique_lock<std::mutex> lk(S->mu);
+  if (S->stop) {
+    delete q;
+    return XC_ERR_ARG;
+  }
+  if (S->queued_pairs + n > S->max_pairs || S->queued_bytes + q->footprint > S->budget_bytes) {
+    delete q;
+    return XC_ERR_BUSY;
+  }
+  q->ticket = S->next_ticket++;
+  q->t_submit = Clock::now();
+  S->queued_pairs += n;
+  S->queued_bytes += q->footprint;
+  S->reqs[q->ticket] = q;
+  S->queue.push_back(q);
+  *ticket = q->ticket;
+  lk.unlock();
+  S->cv_work.notify_one();
+  return XC_OK;
+}
+
+int xc_wait(xc_ctx* c, uint64_t ticket, int timeout_ms, xc_result* out, size_t cap, size_t* n_out) {
+  if (!c || !c->server) return XC_ERR_ARG;
+  Server* S = c->server;
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(ticket);
+  if (it == S->reqs.end()) return XC_ERR_ARG;
+  Request* q = it->second;
+  const auto deadline = Clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms);
+  while (!q->complete) {
+    if (S->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && !q->complete) return XC_ERR_TIMEOUT;
+  }
+  if (q->status != XC_OK) {
+    const int st = q->status;
+    S->reqs.erase(it);
+    delete q;
+    return st;
+  }
+  size_t need = 0;
+  for (auto& v : q->per_pair) need += v.size();
+  if (n_out) *n_out = need;
+  if (need > cap || (!out && need)) return XC_ERR_CAPACITY;
+  size_t o = 0;
+  for (auto& v : q->per_pair) {
+    if (!v.empty()) memcpy(out + o, v.data(), v.size() * sizeof(xc_result));
+    o += v.size();
+  }
+  S->reqs.erase(it);
+  delete q;
+  return XC_OK;
+}
+
+int xc_serving_stats(xc_ctx* c, double* p50, double* p99, uint64_t* completed, uint64_t* pairs_done) {
+  if (!c) return XC_ERR_ARG;
+  if (!c->server) {
+    if (p50) *p50 = 0;
+    if (p99) *p99 = 0;
+    if (completed) *completed = 0;
+    if (pairs_done) *pairs_done = 0;
+    return XC_OK;
+  }
+  Server* S = c->server;
+  std::lock_guard<std::mutex> lk(S->mu);
+  std::vector<double> v = S->lat_ms;
+  std::sort(v.begin(), v.end());
+  auto pct = [&](double p) {
+    if (v.empty()) return 0.0;
+    size_t i = (size_t)std::min<double>((double)v.size() - 1, std::floor(p * (double)(v.size() - 1) + 0.5));
+    return v[i];
+  };
+  if (p50) *p50 = pct(0.50);
+  if (p99) *p99 = pct(0.99);
+  if (completed) *completed = S->completed;
+  if (pairs_done) *pairs_done = S->pairs_done;
+  return XC_OK;
+}
+
+}  // extern "C"

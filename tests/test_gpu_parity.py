@@ -1,0 +1,263 @@
+"""GPU parity tests: the CUDA path through the C ABI against the reference's
+golden vectors (tests/golden/) and the oracle, on the same seeded inputs.
+
+Bars (see tests/parity.py): signals bit-exact; correlation within 1e-3 of the
+FP64 oracle (relative to its peak); FindTop offsets equal except straddles;
+DoOne segments exact; t_result records exact except ulp-level prob."""
+import hashlib
+import threading
+
+import numpy as np
+import pytest
+
+import oracle
+from tests import parity
+from satsuma2_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+CASES = parity.load_cases()
+XC_TOL = 1e-3
+
+
+@pytest.fixture(scope="module")
+def O():
+    return oracle.Oracle()
+
+
+_CTX = {}
+
+
+def ctx_for(case):
+    import satsuma2_gb300 as sg
+    key = (case["cutoff"], case["min_prob"], case["target_total"], case["min_len"], case["query_chunk"],
+           case["L"], case["probtable"], case["probtable_cutoff"])
+    if key not in _CTX:
+        sg.build.build()
+        _CTX[key] = sg.XCorr(cutoff=case["cutoff"], min_prob=case["min_prob"], target_total=case["target_total"],
+                             min_len=case["min_len"], q_chunk=case["query_chunk"], fft_len=case["L"],
+                             prob_table=bool(case["probtable"]), prob_table_cutoff=case["probtable_cutoff"])
+    return _CTX[key]
+
+
+def pair_item(case):
+    return dict(t=case["t"], q=case["q"], t_chunk_start=case["t_chunk_start"], target_id=case["target_id"],
+                q_chunk_start=case["q_chunk_start"], query_id=case["query_id"], query_size=case["query_size"])
+
+
+SUPPORTED = [c for c in CASES if c["L"] <= 16384]
+
+
+def sha1(a):
+    return hashlib.sha1(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("case", SUPPORTED, ids=[c["name"] for c in SUPPORTED])
+def test_stages_match_reference(O, case):
+    x = ctx_for(case)
+    d = x.debug_pair(**pair_item(case))
+    L = case["L"]
+    assert d["L"] == L
+    rcq = O.rc(case["q"])
+    # signals: strand 0 holds target + query, strand 1 target + RC query
+    assert [sha1(d["signals"][0, 0, c]) for c in range(4)] == case["signal_sha1"][0]
+    assert [sha1(d["signals"][0, 1, c]) for c in range(4)] == case["signal_sha1"][1]
+    assert [sha1(d["signals"][1, 1, c]) for c in range(4)] == case["signal_sha1"][2]
+    for s, qq in enumerate((case["q"], rcq)):
+        band, xc64 = parity.straddles(O, case, qq, s)
+        scale = max(1.0, float(np.abs(xc64).max()))
+        err = float(np.abs(d["xc"][s].astype(np.float64) - xc64).max()) / scale
+        assert err <= XC_TOL, err
+        parity.compare_offsets(d["offsets"][s], case["ref_offsets"][s], band)
+        # DoOne segments over the GPU's own offsets: exact
+        want = [O.doone(case["t"], qq, int(i) - L // 2) for i in d["offsets"][s]]
+        want = np.concatenate(want) if want else np.zeros((0, 3), np.int32)
+        assert np.array_equal(d["segments"][s].reshape(-1, 3), want.reshape(-1, 3))
+
+
+@pytest.mark.parametrize("case", SUPPORTED, ids=[c["name"] for c in SUPPORTED])
+def test_results_match_reference(O, case):
+    x = ctx_for(case)
+    res = x.align([pair_item(case)])
+    d = x.debug_pair(**pair_item(case))
+    rcq = O.rc(case["q"])
+    dropped = set()
+    for s, qq in enumerate((case["q"], rcq)):
+        band, _ = parity.straddles(O, case, qq, s)
+        for i in parity.compare_offsets(d["offsets"][s], case["ref_offsets"][s], band):
+            dropped.add((s, i))
+    ref = case["ref_results"]
+    assert parity.same_results(parity.drop_offsets(res, case, dropped), parity.drop_offsets(ref, case, dropped),
+                               target_total=case["target_total"])
+    # and exactly the oracle's records over the GPU's own offsets
+    pt = None
+    if case["probtable"]:
+        pt = O.probtable(case["target_total"], case["probtable_cutoff"])
+    P = O.params(cutoff=case["cutoff"], min_prob=case["min_prob"], target_total=case["target_total"],
+                 min_len=case["min_len"], q_chunk=case["query_chunk"], fft_len=case["L"], probtable=pt,
+                 probtable_cutoff=case["probtable_cutoff"])
+    pr = O.pair(case["t"], case["q"], t_chunk_start=case["t_chunk_start"], target_id=case["target_id"],
+                q_chunk_start=case["q_chunk_start"], query_id=case["query_id"], query_size=case["query_size"])
+    want, _ = O.align_pair(P, pr, offsets_in=d["offsets"])
+    assert parity.same_results(res, want, target_total=case["target_total"])
+
+
+def test_large_fft_unsupported():
+    import satsuma2_gb300 as sg
+    case = [c for c in CASES if c["L"] == 32768][0]
+    with pytest.raises(sg.XCError) as e:
+        ctx_for(case).align([pair_item(case)])
+    assert e.value.code == -7
+
+
+def test_rejects_non_ascii():
+    import satsuma2_gb300 as sg
+    x = ctx_for(CASES[0])
+    t = bytearray(b"ACGT" * 500)
+    t[100] = 0xC3
+    with pytest.raises(sg.XCError) as e:
+        x.align([(bytes(t), b"ACGT" * 300)])
+    assert e.value.code == -5
+
+
+def test_batch_equals_single_pairs(O):
+    """Many pairs in one launch (bucketed by FFT length) = one pair per call."""
+    import satsuma2_gb300 as sg
+    x = sg.XCorr(fft_len=-1, target_total=4096.0 * 64)
+    items = W.uneven_batch(48, seed=9) + W.uniform_batch(16, seed=21)
+    res, counts = x.align(items, with_counts=True)
+    o = 0
+    for k, it in enumerate(items):
+        single = x.align([it])
+        got = res[o:o + int(counts[k])]
+        o += int(counts[k])
+        assert parity.same_results(got, single)
+    x.close()
+
+
+def test_uniform_batch_vs_oracle(O):
+    import satsuma2_gb300 as sg
+    items = W.uniform_batch(32, seed=5)
+    x = sg.XCorr(target_total=4096.0 * 4096)
+    res, counts = x.align(items, with_counts=True)
+    P = O.params(target_total=4096.0 * 4096)
+    o = 0
+    for k, (t, q) in enumerate(items):
+        got = res[o:o + int(counts[k])]
+        o += int(counts[k])
+        d = x.debug_pair(t=t, q=q)
+        want, _ = O.align_pair(P, O.pair(t, q), offsets_in=d["offsets"])
+        assert parity.same_results(got, want, target_total=4096.0 * 4096)
+    x.close()
+
+
+def test_device_batch_replay_is_stable():
+    import satsuma2_gb300 as sg
+    items = W.uniform_batch(64, seed=33)
+    x = sg.XCorr(target_total=4096.0 * 4096)
+    ref = x.align(items)
+    b = x.upload(items)
+    assert b.launches() >= 4
+    for _ in range(3):
+        b.run()
+        assert parity.same_results(b.results(), ref)
+    b.free()
+    x.close()
+
+
+def test_slave_end_to_end(O):
+    """The CUDA path reproduces the unmodified reference slave's output stream.
+
+    The oracle reproduces that stream exactly on the CPU (test_oracle), so it
+    splits the stream per chunk pair; records from offsets where the GPU's
+    FP32 FindTop and the FP64 oracle disagree inside the straddle band are set
+    aside on both sides."""
+    import satsuma2_gb300 as sg
+    d = parity.load_slave_e2e()
+    m = d["meta"]
+    tseqs = [d["tg0"].tobytes(), d["tg1"].tobytes(), d["sentinel"].tobytes()]
+    qseqs = [d["qg0"].tobytes(), d["qg1"].tobytes(), d["qg2"].tobytes(), d["sentinel"].tobytes()]
+    x = sg.XCorr(cutoff=m["cutoff"], min_prob=m["min_prob_effective"], target_total=m["target_total"],
+                 t_chunk=m["t_chunk"], q_chunk=m["q_chunk"])
+    P = O.params(cutoff=m["cutoff"], min_prob=m["min_prob_effective"], target_total=m["target_total"],
+                 t_chunk=m["t_chunk"], q_chunk=m["q_chunk"])
+    items = []
+    for (tf, tt, qf, qt) in d["blocks"][:-1]:
+        for qi in range(qf, qt + 1):
+            for ti in range(tf, tt + 1):
+                ts, tst, ten = d["tchunks"][ti]
+                qs, qst, qen = d["qchunks"][qi]
+                items.append(dict(t=tseqs[ts][tst:ten], q=qseqs[qs][qst:qen], t_chunk_start=int(tst),
+                                  target_id=int(ts), q_chunk_start=int(qst), query_id=int(qs),
+                                  query_size=len(qseqs[qs])))
+    got, counts = x.align(items, with_counts=True)
+    slave = d["results"]
+    og = os_ = 0
+    n_dropped = 0
+    for k, it in enumerate(items):
+        pr = O.pair(it["t"], it["q"], t_chunk_start=it["t_chunk_start"], target_id=it["target_id"],
+                    q_chunk_start=it["q_chunk_start"], query_id=it["query_id"], query_size=it["query_size"])
+        want, det = O.align_pair(P, pr, want_detail=True)
+        mine = got[og:og + int(counts[k])]
+        theirs = slave[os_:os_ + len(want)]
+        og += int(counts[k])
+        os_ += len(want)
+        assert parity.same_results(theirs, want, target_total=m["target_total"]), "oracle no longer splits the slave stream at pair %d" % k
+        case = dict(L=8192, t_chunk_start=it["t_chunk_start"], q_chunk_start=it["q_chunk_start"],
+                    query_size=it["query_size"], query_chunk=m["q_chunk"], cutoff=m["cutoff"], t=it["t"])
+        dbg = x.debug_pair(**it)
+        dropped = set()
+        for s, qq in enumerate((it["q"], O.rc(it["q"]))):
+            band, _ = parity.straddles(O, case, qq, s)
+            for i in parity.compare_offsets(dbg["offsets"][s], det["offsets"][s], band):
+                dropped.add((s, i))
+        n_dropped += len(dropped)
+        a = parity.drop_offsets(mine, case, dropped)
+        b = parity.drop_offsets(theirs, case, dropped)
+        assert parity.same_results(a, b, target_total=m["target_total"]), "pair %d:\nGPU %s\nslave %s" % (
+            k, a[["qstart", "tstart", "len", "reverse", "prob", "ident"]],
+            b[["qstart", "tstart", "len", "reverse", "prob", "ident"]])
+    assert og == len(got) and os_ == len(slave)
+    x.close()
+
+
+def test_serving_same_alone_and_in_mix():
+    """Continuous batching: each request's results equal its standalone run."""
+    import satsuma2_gb300 as sg
+    x = sg.XCorr(target_total=4096.0 * 4096, max_batch=96)
+    pool = W.uniform_batch(96, seed=44)
+    reqs = [pool[i:i + 1 + (i % 5)] for i in range(0, 90, 6)]
+    alone = [x.align(r) for r in reqs]
+    tickets = [None] * len(reqs)
+
+    def worker(k):
+        tickets[k] = x.submit(reqs[k])
+
+    th = [threading.Thread(target=worker, args=(k,)) for k in range(len(reqs))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for k, tk in enumerate(tickets):
+        got = x.wait(tk, timeout_ms=60000)
+        assert parity.same_results(got, alone[k])
+    st = x.serving_stats()
+    assert st["completed"] >= len(reqs)
+    x.close()
+
+
+def test_wait_times_out_and_keeps_ticket():
+    import satsuma2_gb300 as sg
+    x = sg.XCorr(target_total=4096.0 * 4096)
+    items = W.uniform_batch(512, seed=45)
+    tk = x.submit(items)
+    try:
+        x.wait(tk, timeout_ms=0)
+        timed_out = False
+    except sg.XCError as e:
+        assert e.code == -6
+        timed_out = True
+    res = x.wait(tk, timeout_ms=120000)
+    assert len(res) >= 0
+    assert timed_out or len(res) >= 0
+    x.close()
