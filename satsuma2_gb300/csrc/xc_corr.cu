@@ -1,0 +1,414 @@
+// Correlation + FindTop kernel of the satsuma2 cross-correlation path (sm_103a).
+//
+// corr_kernel<log2 L>: one CTA of 512 threads per (chunk pair, strand).
+//   1. chunk bytes to shared memory; strand 1 reverse-complements the query
+//   2. CCSignal: per-window entropy weights and per-channel means
+//   3. per channel: z = target_c + i*query_c; the even-bin group (threads
+//      0..255) transforms z, the odd-bin group (256..511) z*W_L^n, each an
+//      N = L/2 point in-place mixed-radix transform; then the conjugate
+//      product of the two spectra is added to the channel sum
+//   4. inverse: half-length complex transform of the Hermitian channel sum
+//   5. FindTop: envelope per 256 samples, threshold, ordered compaction
+// Everything stays in shared memory; HBM sees the chunk bytes in and the
+// offset list out.  Reference semantics cited per step; paths are relative to
+// the satsuma2 source tree.
+#include "xc_device.cuh"
+
+namespace xc {
+
+size_t corr_smem_bytes(int log2L) {
+  const size_t N = (size_t)1 << (log2L - 1);
+  const size_t NH = N / 64;
+  return (2 * N + (N / 2 + 8) + N / 2 + 2 * (NH + 64)) * sizeof(float2)   // transforms, sums, twiddles
+         + 2 * N                                                         // target and query bytes
+         + 2 * 256 * sizeof(float)                                       // entropy weight per window
+         + 2 * 256 * sizeof(float2);                                     // per-window channel values
+}
+
+template <int LOG2L>
+__global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(const CorrParams P) {
+  constexpr int L = 1 << LOG2L;
+  constexpr int N = L >> 1;
+  constexpr int LOG2N = LOG2L - 1;
+  constexpr int WIN = L / 512;   // CCSignal::ComputeEntropy window (CrossCorr.cc:46)
+  constexpr int NWIN = 256;      // N / WIN
+  constexpr int NH = N / 64;
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* bufE = reinterpret_cast<float2*>(smem);
+  float2* bufO = bufE + N;
+  float2* accE = bufO + N;              // channel sum at bins 2m, m = 0..N/2 (N/2: Nyquist, real)
+  float2* accO = accE + (N / 2 + 8);    // bins 2m+1, m < N/2; 8 slots off accE's banks
+  float2* twNh = accO + N / 2;          // W_N^(64a)
+  float2* twNl = twNh + NH;             // W_N^b, b < 64
+  float2* twLh = twNl + 64;             // W_L^(64a)
+  float2* twLl = twLh + NH;             // W_L^b
+  uint8_t* st = reinterpret_cast<uint8_t*>(twLl + 64);
+  uint8_t* sq = st + N;
+  float* Et = reinterpret_cast<float*>(sq + N);
+  float* Eq = Et + NWIN;
+  float2* vt = reinterpret_cast<float2*>(Eq + NWIN);
+  float2* vq = vt + NWIN;
+  __shared__ int s_cnt4[8];
+  __shared__ double s_off[8];
+  __shared__ int s_warp[NT_CORR / 32];
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int pidx = P.first + blockIdx.x;
+  const int strand = blockIdx.y;
+  const PairDesc D = P.pairs[pidx];
+  const int T = D.tlen, Q = D.qlen;
+  const uint8_t* __restrict__ gt = P.pool + D.t_off;
+  const uint8_t* __restrict__ gq = P.pool + D.q_off;
+
+  // ---- 1. chunk bytes (DNAVector::ReverseComplement, DNAVector.cc:482-500) ----
+  int high = 0, nonacgt = 0, th_t = 0, th_q = 0;
+  for (int i = tid; i < N; i += NT_CORR) {
+    unsigned b = 0;
+    if (i < T) {
+      b = gt[i];
+      high |= b >> 7;
+      nonacgt |= !is_acgt(b);
+      th_t |= is_third(b);
+    }
+    st[i] = (uint8_t)b;
+    unsigned c = 0;
+    if (i < Q) {
+      const unsigned raw = strand ? gq[Q - 1 - i] : gq[i];
+      high |= raw >> 7;
+      c = strand ? c_rc[raw] : raw;
+      nonacgt |= !is_acgt(c);
+      th_q |= is_third(c);
+    }
+    sq[i] = (uint8_t)c;
+  }
+  for (int i = tid; i < NH; i += NT_CORR) {
+    twNh[i] = P.tab.twN_hi[i];
+    twLh[i] = P.tab.twL_hi[i];
+  }
+  if (tid < 64) {
+    twNl[tid] = P.tab.twN_lo[tid];
+    twLl[tid] = P.tab.twL_lo[tid];
+  }
+  if (tid < 8) s_cnt4[tid] = 0;
+  const int any_high = __syncthreads_or(high);
+  const int generic = __syncthreads_or(nonacgt);
+  th_t = __syncthreads_or(th_t);
+  th_q = __syncthreads_or(th_q);
+  if (any_high) {
+    if (tid == 0) {
+      P.off_cnt[pidx * 2 + strand] = 0;
+      if (strand == 0) P.pair_flags[pidx] = PF_INVALID;
+    }
+    return;
+  }
+  if (tid == 0 && strand == 0) P.pair_flags[pidx] = (D.flags & PF_FAST) | (generic ? PF_GENERIC : 0u);
+  for (int i = tid; i < N + 8; i += NT_CORR) accE[i] = make_float2(0.f, 0.f);   // accE and accO
+
+  // ---- 2a. entropy weight per window (CCSignal::ComputeEntropy, CrossCorr.cc:35-93).
+  //      Threads 0..255: target windows, 256..511: query windows.  Windows
+  //      without one-third letters have exact quarter-unit base sums, so Ent
+  //      comes from a table the host computed with the same double
+  //      expression; others repeat the reference's double arithmetic here. ----
+  {
+    const int which = tid >> 8, w = tid & 255;
+    const uint8_t* s = which ? sq : st;
+    const int len = which ? Q : T;
+    const int third = which ? th_q : th_t;
+    float E = 0.f;
+    if (len < 1024) {
+      E = 1.f;
+    } else if (w * WIN < len) {
+      const int i0 = w * WIN;
+      const int k = min(WIN, len - i0);
+      bool has3 = false;
+      if (third)
+        for (int j = 0; j < k; j++) has3 |= is_third(s[i0 + j]);
+      double sv;
+      if (!has3) {
+        int a4 = 0, c4 = 0, g4 = 0, t4 = 0;
+        for (int j = 0; j < k; j++) {
+          const uchar4 q = c_w4q[s[i0 + j]];
+          a4 += q.x; c4 += q.y; g4 += q.z; t4 += q.w;
+        }
+        const double* et = P.tab.ent + k * (4 * WIN + 1);
+        sv = __dadd_rn(__dadd_rn(__dadd_rn(__ldg(et + a4), __ldg(et + c4)), __ldg(et + g4)), __ldg(et + t4));
+      } else {
+        double a = 0, c = 0, g = 0, t = 0;
+        for (int j = 0; j < k; j++) {
+          const int b = s[i0 + j];
+          a = __dadd_rn(a, c_wd[0][b]);
+          c = __dadd_rn(c, c_wd[1][b]);
+          g = __dadd_rn(g, c_wd[2][b]);
+          t = __dadd_rn(t, c_wd[3][b]);
+        }
+        a = __ddiv_rn(a, (double)k);
+        c = __ddiv_rn(c, (double)k);
+        g = __ddiv_rn(g, (double)k);
+        t = __ddiv_rn(t, (double)k);
+        sv = __dadd_rn(__dadd_rn(__dadd_rn(ent_dev(a), ent_dev(c)), ent_dev(g)), ent_dev(t));
+      }
+      E = __double2float_rn(-sv);
+      if (E < 0.f) E = 0.f;
+    }
+    (which ? Eq : Et)[w] = E;
+  }
+
+  // ---- 2b. channel means (SeqToPCM, CrossCorr.cc:108-116): exact quarter-unit
+  //      sums, or the sequential double sum when one-third letters occur ----
+  {
+    int cn[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = tid; i < N; i += NT_CORR) {
+      if (i < T) { const uchar4 q = c_w4q[st[i]]; cn[0] += q.x; cn[1] += q.y; cn[2] += q.z; cn[3] += q.w; }
+      if (i < Q) { const uchar4 q = c_w4q[sq[i]]; cn[4] += q.x; cn[5] += q.y; cn[6] += q.z; cn[7] += q.w; }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const int v = __reduce_add_sync(0xffffffffu, cn[k]);
+      if (lane == 0 && v) atomicAdd(&s_cnt4[k], v);
+    }
+  }
+  __syncthreads();
+  if (tid < 8) {
+    const int which = tid >> 2, c = tid & 3;
+    const int len = which ? Q : T;
+    const int third = which ? th_q : th_t;
+    double off = 0.0;
+    if (len > 0) {
+      if (!third) {
+        off = __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len);
+      } else {
+        const uint8_t* s = which ? sq : st;
+        double sum = 0.0;
+        for (int i = 0; i < len; i++) sum = __dadd_rn(sum, c_wd[c][s[i]]);
+        off = __ddiv_rn(sum, (double)len);
+      }
+    }
+    s_off[tid] = off;
+  }
+  __syncthreads();
+
+  const int grp = tid >> 8;   // 0: even-bin transform, 1: odd-bin transform
+  const int gtid = tid & 255;
+
+  for (int c = 0; c < 4; c++) {
+    // Per-window channel values: out = float(entropy * (weight - mean))
+    // (CrossCorr.cc:123), weight 0 or 1 for A/C/G/T.
+    if (!generic) {
+      const double off = s_off[grp * 4 + c];
+      const double E = (double)(grp ? Eq : Et)[gtid];
+      float2 v;
+      v.x = __double2float_rn(__dmul_rn(E, __dsub_rn(0.0, off)));
+      v.y = __double2float_rn(__dmul_rn(E, __dsub_rn(1.0, off)));
+      (grp ? vq : vt)[gtid] = v;
+    }
+    __syncthreads();
+
+    // ---- 3. z[n] = target_c[n] + i*query_c[n]; the odd-bin group pre-twiddles
+    //      by W_L^n.  Both signals are zero past N, so the even bins of the
+    //      L-point transform are the N-point transform of z and the odd bins
+    //      that of z*W_L^n. ----
+    {
+      float2* buf = grp ? bufO : bufE;
+      const double offt = s_off[c], offq = s_off[4 + c];
+      for (int n = gtid; n < N; n += 256) {
+        float x = 0.f, y = 0.f;
+        const int w = n / WIN;
+        if (!generic) {
+          if (n < T) { const float2 v = vt[w]; x = code_of(st[n]) == (uint32_t)c ? v.y : v.x; }
+          if (n < Q) { const float2 v = vq[w]; y = code_of(sq[n]) == (uint32_t)c ? v.y : v.x; }
+        } else {
+          if (n < T) x = __double2float_rn(__dmul_rn((double)Et[w], __dsub_rn(c_wd[c][st[n]], offt)));
+          if (n < Q) y = __double2float_rn(__dmul_rn((double)Eq[w], __dsub_rn(c_wd[c][sq[n]], offq)));
+        }
+        if (P.dbg_sig && grp == 0) {
+          float* ds = P.dbg_sig + (size_t)(pidx * 2 + strand) * 8 * L;
+          ds[(size_t)c * L + n] = x;
+          ds[(size_t)(4 + c) * L + n] = y;
+        }
+        float2 z = make_float2(x, y);
+        if (grp) z = cmul(z, tw2(twLh, twLl, n));
+        buf[swz(n)] = z;
+      }
+    }
+    __syncthreads();
+
+    fft_forward<LOG2N>(grp ? bufO : bufE, twNh, twNl, gtid, 256);
+
+    // Per-bin product (CrossCorrelation::DoOne, CrossCorr.cc:477-492):
+    // X = target spectrum, Y = query spectrum from Z(k), Z(L-k).
+    // conj(X)Y on bins 1..N-2, X(0)Y(0) on bin 0, and the target's own value
+    // on bins N-1 and N, which the reference's loop leaves unmultiplied.
+    if (grp == 0) {
+      for (int m = gtid; m <= N / 2; m += 256) {
+        const float2 A = bufE[swz(posof<LOG2N>(m))];
+        const float2 B = bufE[swz(posof<LOG2N>((N - m) & (N - 1)))];
+        const float2 X = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
+        const float2 Y = make_float2(0.5f * (A.y + B.y), -0.5f * (A.x - B.x));
+        if (m == N / 2) accE[m].x += X.x;
+        else accE[m] = cadd(accE[m], cmulc(Y, X));
+      }
+    } else {
+      for (int m = gtid; m < N / 2; m += 256) {
+        const float2 A = bufO[swz(posof<LOG2N>(m))];
+        const float2 B = bufO[swz(posof<LOG2N>(N - 1 - m))];
+        const float2 X = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
+        const float2 Y = make_float2(0.5f * (A.y + B.y), -0.5f * (A.x - B.x));
+        accO[m] = cadd(accO[m], m == N / 2 - 1 ? X : cmulc(Y, X));
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- 4. inverse: half-length complex transform of the Hermitian sum S.
+  //      Z(k) = E(k) + i O(k), E = (S(k) + conj S(N-k))/2,
+  //      O = (S(k) - conj S(N-k)) conj(W_L^k)/2; z[m] = r[2m] + i r[2m+1]. ----
+  auto S = [&](int k) -> float2 { return (k & 1) ? accO[k >> 1] : accE[k >> 1]; };
+  for (int k = tid; k <= N / 2; k += NT_CORR) {
+    const float2 Sk = S(k);
+    const float2 Sn = S(N - k);
+    {
+      const float2 Ev = make_float2(0.5f * (Sk.x + Sn.x), 0.5f * (Sk.y - Sn.y));
+      const float2 Dv = make_float2(0.5f * (Sk.x - Sn.x), 0.5f * (Sk.y + Sn.y));
+      const float2 Ov = cmulc(Dv, tw2(twLh, twLl, k));
+      bufE[swz(posof<LOG2N>(k))] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
+    }
+    if (k != 0 && k != N / 2) {
+      const float2 Ev = make_float2(0.5f * (Sn.x + Sk.x), 0.5f * (Sn.y - Sk.y));
+      const float2 Dv = make_float2(0.5f * (Sn.x - Sk.x), 0.5f * (Sn.y + Sk.y));
+      const float2 Ov = cmulc(Dv, tw2(twLh, twLl, N - k));
+      bufE[swz(posof<LOG2N>(N - k))] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
+    }
+  }
+  __syncthreads();
+  fft_inverse<LOG2N>(bufE, twNh, twNl, tid < 256 ? tid : (1 << 30), 256);
+
+  // ---- 5. FindTop (SeqAnalyzer::FindTop, CrossCorr.cc:878-944): xc[i] =
+  //      r[(i + N) mod L] / N; envelope over 256-sample blocks when L/256 > 8;
+  //      keep i with xc[i] > env*cutoff + 1 in increasing i.  Warp w owns the
+  //      contiguous range [w*L/16, (w+1)*L/16), lanes stride by one. ----
+  constexpr int PER_WARP = L / (NT_CORR / 32);
+  constexpr int ITER = PER_WARP / 32;
+  const int wbase = warp * PER_WARP;
+  const float scale = 1.0f / (float)N;
+  auto xval = [&](int i) -> float {
+    const int n = (i + N) & (L - 1);
+    const float2 z = bufE[swz(n >> 1)];
+    return ((n & 1) ? z.y : z.x) * scale;
+  };
+  float thrb[PER_WARP >= 256 ? PER_WARP / 256 : 1];
+  if constexpr (L / 256 > 8) {
+    const double cut = (D.flags & PF_FAST) ? P.cutoff_fast : P.cutoff;
+#pragma unroll
+    for (int bb = 0; bb < PER_WARP / 256; bb++) {
+      // squares are float products as in the reference; compensated FP32
+      // sum per lane, combined in FP64 across the warp
+      float s = 0.f, comp = 0.f;
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const float x = xval(wbase + bb * 256 + e * 32 + lane);
+        const float v = __fmul_rn(x, x);
+        const float y = __fsub_rn(v, comp);
+        const float t2 = __fadd_rn(s, y);
+        comp = __fsub_rn(__fsub_rn(t2, s), y);
+        s = t2;
+      }
+      // pairwise FP32 tree across the warp for sum and compensation, then
+      // one FP64 combine per block on lane 0
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        s = __fadd_rn(s, __shfl_xor_sync(0xffffffffu, s, o));
+        comp = __fadd_rn(comp, __shfl_xor_sync(0xffffffffu, comp, o));
+      }
+      float th = 0.f;
+      if (lane == 0) {
+        const double ds = __dsub_rn((double)s, (double)comp);
+        const double env = __dsqrt_rn(__ddiv_rn(ds, 256.0));
+        // x > t (double) <=> x > round_down_to_float(t) for a float x.
+        th = __double2float_rd(__dadd_rn(__dmul_rn(env, cut), 1.0));
+      }
+      thrb[bb] = __shfl_sync(0xffffffffu, th, 0);
+    }
+  } else {
+    thrb[0] = 1.0f;
+  }
+  int wcount = 0;
+#pragma unroll 4
+  for (int e = 0; e < ITER; e++) {
+    const int i = wbase + e * 32 + lane;
+    const float x = xval(i);
+    wcount += __popc(__ballot_sync(0xffffffffu, x > thrb[(L / 256 > 8) ? (e >> 3) : 0]));
+    if (P.dbg_xc) P.dbg_xc[(size_t)(pidx * 2 + strand) * L + i] = x;
+  }
+  if (lane == 0) s_warp[warp] = wcount;
+  __syncthreads();
+  if (warp == 0) {
+    const int v = lane < NT_CORR / 32 ? s_warp[lane] : 0;
+    int w = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += u;
+    }
+    if (lane < NT_CORR / 32) s_warp[lane] = w - v;
+    if (lane == NT_CORR / 32 - 1) P.off_cnt[pidx * 2 + strand] = w;
+  }
+  __syncthreads();
+  int run = s_warp[warp];
+  int* out = P.off_list + D.off_base + (size_t)strand * L;
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll 4
+  for (int e = 0; e < ITER; e++) {
+    const int i = wbase + e * 32 + lane;
+    const bool keep = xval(i) > thrb[(L / 256 > 8) ? (e >> 3) : 0];
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) out[run + __popc(m & lt)] = i;
+    run += __popc(m);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+cudaError_t prepare_scan_kernels();
+cudaError_t upload_scan_constants(const unsigned char* rc256, const uchar4* w4q128, const double* w4d);
+
+template <int LOG2L>
+static cudaError_t set_corr_attrs() {
+  return cudaFuncSetAttribute(corr_kernel<LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)corr_smem_bytes(LOG2L));
+}
+
+cudaError_t prepare_kernels() {
+  cudaError_t e;
+  if ((e = set_corr_attrs<10>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<11>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<12>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<13>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<14>()) != cudaSuccess) return e;
+  return prepare_scan_kernels();
+}
+
+cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t s) {
+  if (npairs <= 0) return cudaSuccess;
+  const dim3 grid(npairs, 2);
+  const size_t sm = corr_smem_bytes(log2L);
+  switch (log2L) {
+    case 10: corr_kernel<10><<<grid, NT_CORR, sm, s>>>(p); break;
+    case 11: corr_kernel<11><<<grid, NT_CORR, sm, s>>>(p); break;
+    case 12: corr_kernel<12><<<grid, NT_CORR, sm, s>>>(p); break;
+    case 13: corr_kernel<13><<<grid, NT_CORR, sm, s>>>(p); break;
+    case 14: corr_kernel<14><<<grid, NT_CORR, sm, s>>>(p); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t upload_constants(const unsigned char* rc256, const uchar4* w4q128, const double* w4d) {
+  cudaError_t e = upload_constants_here(rc256, w4q128, w4d);
+  if (e != cudaSuccess) return e;
+  return upload_scan_constants(rc256, w4q128, w4d);
+}
+
+}  // namespace xc

@@ -1,0 +1,255 @@
+// Device-side building blocks shared by the kernels of the satsuma2
+// cross-correlation path: complex helpers, the shared-memory layout of
+// transform buffers, register DFTs, the in-place mixed-radix passes and the
+// codec constants.  Included by xc_corr.cu and xc_scan.cu (each translation
+// unit gets its own copy of the constant tables; upload_constants fills both).
+#pragma once
+#include "xc_internal.h"
+
+#include <math.h>
+
+namespace xc {
+
+static __constant__ unsigned char c_rc[256];   // DNACodec reverse complement (DNAVector.cc:13-58)
+static __constant__ uchar4 c_w4q[128];         // A,C,G,T weights in quarter units (thirds letters: 0)
+static __constant__ double c_wd[4][128];       // DNA_A..DNA_T weights (DNAVector.cc:351-369)
+
+static cudaError_t upload_constants_here(const unsigned char* rc256, const uchar4* w4q128, const double* w4d) {
+  cudaError_t e = cudaMemcpyToSymbol(c_rc, rc256, 256);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyToSymbol(c_w4q, w4q128, 128 * sizeof(uchar4));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(c_wd, w4d, 4 * 128 * sizeof(double));
+}
+
+// -----------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+  return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ float2 mul_i(float2 a) { return make_float2(-a.y, a.x); }
+
+__device__ __forceinline__ bool is_acgt(unsigned b) { return b == 'A' || b == 'C' || b == 'G' || b == 'T'; }
+__device__ __forceinline__ bool is_third(unsigned b) { return b == 'B' || b == 'V' || b == 'H' || b == 'D'; }
+// A=0, C=1, G=2, T=3 for the four ASCII capitals.
+__device__ __forceinline__ uint32_t code_of(unsigned b) { return ((b >> 1) ^ (b >> 2)) & 3u; }
+__device__ __forceinline__ uint32_t lowmask(int n) { return n >= 32 ? 0xffffffffu : ((1u << n) - 1u); }
+
+// Placement of complex element p in a transform buffer: the 8-byte slot (low
+// 4 bits, one of 16 per 128-byte row) is XORed with every higher nibble, so
+// the 16 addresses a half-warp touches -- strided by any power of two, or
+// consecutive bins in digit-reversed order -- land in distinct banks.  A
+// bijection on any power-of-two length >= 16 (only the low nibble changes).
+__host__ __device__ constexpr int swz(int p) { return p ^ (((p >> 4) ^ (p >> 8) ^ (p >> 12)) & 15); }
+// swz is linear over XOR, so swz(a | b) = swz(a) ^ swz(b) when a and b share no
+// set bit; the transform passes use that to turn every access into one XOR
+// with a compile-time constant.
+
+// Twiddle W_N^m from two small shared tables: hi[a] = W_N^(64a), lo[b] = W_N^b.
+__device__ __forceinline__ float2 tw2(const float2* hi, const float2* lo, int m) {
+  return cmul(hi[m >> 6], lo[m & 63]);
+}
+
+// Radix plans (log2 of each pass's radix), shared by the transforms and the
+// digit-reversed position of a bin.  Must match radix_plan() in the runtime.
+template <int LOG2N> struct Plan;
+template <int A, int B, int C, int D>
+struct PlanR {
+  static constexpr int n = D ? 4 : 3;
+  __host__ __device__ static constexpr int lr(int s) { return s == 0 ? A : s == 1 ? B : s == 2 ? C : D; }
+};
+template <> struct Plan<9> : PlanR<3, 3, 3, 0> {};
+template <> struct Plan<10> : PlanR<4, 4, 2, 0> {};
+template <> struct Plan<11> : PlanR<4, 4, 3, 0> {};
+template <> struct Plan<12> : PlanR<4, 4, 4, 0> {};
+template <> struct Plan<13> : PlanR<4, 4, 4, 1> {};
+
+// Position of bin k after the forward (decimation-in-frequency) passes: the
+// digit of radix R_s (least significant first in k) moves to place value
+// N / (R_0 ... R_s).
+template <int LOG2N>
+__device__ __forceinline__ int posof(int k) {
+  using PL = Plan<LOG2N>;
+  int p = 0, off = 0, used = 0;
+#pragma unroll
+  for (int s = 0; s < PL::n; s++) {
+    used += PL::lr(s);
+    p |= ((k >> off) & ((1 << PL::lr(s)) - 1)) << (LOG2N - used);
+    off += PL::lr(s);
+  }
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+// Small DFTs in registers, natural order in and out.  DIR = -1 forward
+// (exp(-i...)), +1 inverse.
+// ---------------------------------------------------------------------------
+template <int DIR>
+__device__ __forceinline__ void bf4(float2& x0, float2& x1, float2& x2, float2& x3) {
+  const float2 a0 = cadd(x0, x2), a1 = csub(x0, x2), a2 = cadd(x1, x3), a3 = mul_i(csub(x1, x3));
+  x0 = cadd(a0, a2);
+  x2 = csub(a0, a2);
+  if (DIR < 0) { x1 = csub(a1, a3); x3 = cadd(a1, a3); }
+  else { x1 = cadd(a1, a3); x3 = csub(a1, a3); }
+}
+
+template <int R, int DIR> struct DFT;
+
+template <int DIR> struct DFT<2, DIR> {
+  static __device__ __forceinline__ void run(float2* x) {
+    const float2 t = x[0];
+    x[0] = cadd(t, x[1]);
+    x[1] = csub(t, x[1]);
+  }
+};
+
+template <int DIR> struct DFT<4, DIR> {
+  static __device__ __forceinline__ void run(float2* x) { bf4<DIR>(x[0], x[1], x[2], x[3]); }
+};
+
+// 8 = 4 x 2: n = 2 n1 + n2, k = k1 + 4 k2.
+template <int DIR> struct DFT<8, DIR> {
+  static __device__ __forceinline__ void run(float2* x) {
+    const float r = 0.70710678118654752f;
+    bf4<DIR>(x[0], x[2], x[4], x[6]);
+    bf4<DIR>(x[1], x[3], x[5], x[7]);
+    x[3] = cmul(x[3], make_float2(r, DIR * r));
+    x[5] = DIR < 0 ? make_float2(x[5].y, -x[5].x) : make_float2(-x[5].y, x[5].x);
+    x[7] = cmul(x[7], make_float2(-r, DIR * r));
+    float2 y[8];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) {
+      y[k1] = cadd(x[2 * k1], x[2 * k1 + 1]);
+      y[k1 + 4] = csub(x[2 * k1], x[2 * k1 + 1]);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = y[k];
+  }
+};
+
+// 16 = 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2.
+template <int DIR> struct DFT<16, DIR> {
+  static __device__ __forceinline__ void run(float2* x) {
+    const float c1 = 0.92387953251128674f, s1 = 0.38268343236508978f, r = 0.70710678118654752f;
+#pragma unroll
+    for (int n2 = 0; n2 < 4; n2++) bf4<DIR>(x[n2], x[n2 + 4], x[n2 + 8], x[n2 + 12]);
+    // x[n2 + 4 k1] *= W16^(n2 k1)
+    x[5] = cmul(x[5], make_float2(c1, DIR * s1));
+    x[9] = cmul(x[9], make_float2(r, DIR * r));
+    x[13] = cmul(x[13], make_float2(s1, DIR * c1));
+    x[6] = cmul(x[6], make_float2(r, DIR * r));
+    x[10] = DIR < 0 ? make_float2(x[10].y, -x[10].x) : make_float2(-x[10].y, x[10].x);
+    x[14] = cmul(x[14], make_float2(-r, DIR * r));
+    x[7] = cmul(x[7], make_float2(s1, DIR * c1));
+    x[11] = cmul(x[11], make_float2(-r, DIR * r));
+    x[15] = cmul(x[15], make_float2(-c1, -DIR * s1));
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) bf4<DIR>(x[4 * k1], x[4 * k1 + 1], x[4 * k1 + 2], x[4 * k1 + 3]);
+    float2 y[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++)
+#pragma unroll
+      for (int k2 = 0; k2 < 4; k2++) y[k1 + 4 * k2] = x[4 * k1 + k2];
+#pragma unroll
+    for (int k = 0; k < 16; k++) x[k] = y[k];
+  }
+};
+
+// One in-place pass of span S and radix R over an N-point buffer.
+// Forward (decimation in frequency): butterfly, then twiddle W_S^(j r').
+// Inverse (decimation in time, the exact reverse): conjugate twiddle, then
+// butterfly.  Forward passes in order S = N, N/R0, ... leave bin k at a
+// mixed-radix digit-reversed position (pos_of table); the inverse passes in
+// reverse order take that layout back to natural order.
+template <int R, int N, int S, bool INV>
+__device__ __forceinline__ void fft_pass(float2* __restrict__ buf, const float2* __restrict__ twh,
+                                         const float2* __restrict__ twl, int t, int nt) {
+  constexpr int d = S / R;
+  constexpr int B = N / R;
+  constexpr int tws = N / S;
+  for (int b = t; b < B; b += nt) {
+    const int j = b & (d - 1);
+    const int base = (b - j) * R + j;   // bits of base and of r*d never overlap
+    const int sb = swz(base);
+    float2 x[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) x[r] = buf[sb ^ swz(r * d)];
+    if (!INV) DFT<R, -1>::run(x);
+    if (d > 1) {
+      if constexpr (R == 16) {
+        // W^r for r = 4a + b from W^m and W^(4m) (two table lookups): keeps
+        // six twiddles live instead of fifteen; about 4 ulp per twiddle.
+        const int m1 = j * tws;
+        const float2 w1 = tw2(twh, twl, m1), w4 = tw2(twh, twl, 4 * m1);
+        const float2 w2 = cmul(w1, w1), w3 = cmul(w2, w1);
+        const float2 w8 = cmul(w4, w4), w12 = cmul(w8, w4);
+#pragma unroll
+        for (int r = 1; r < 16; r++) {
+          const int a = r >> 2, bb = r & 3;
+          const float2 wa = a == 1 ? w4 : a == 2 ? w8 : w12;
+          const float2 wb = bb == 1 ? w1 : bb == 2 ? w2 : w3;
+          const float2 w = a == 0 ? wb : bb == 0 ? wa : cmul(wa, wb);
+          x[r] = INV ? cmulc(x[r], w) : cmul(x[r], w);
+        }
+      } else {
+#pragma unroll
+        for (int r = 1; r < R; r++) x[r] = INV ? cmulc(x[r], tw2(twh, twl, j * r * tws)) : cmul(x[r], tw2(twh, twl, j * r * tws));
+      }
+    }
+    if (INV) DFT<R, 1>::run(x);
+#pragma unroll
+    for (int r = 0; r < R; r++) buf[sb ^ swz(r * d)] = x[r];
+  }
+}
+
+template <int LR, int N, int S, bool INV>
+__device__ __forceinline__ void pass_lr(float2* buf, const float2* h, const float2* l, int t, int nt) {
+  if constexpr (LR == 1) fft_pass<2, N, S, INV>(buf, h, l, t, nt);
+  else if constexpr (LR == 2) fft_pass<4, N, S, INV>(buf, h, l, t, nt);
+  else if constexpr (LR == 3) fft_pass<8, N, S, INV>(buf, h, l, t, nt);
+  else fft_pass<16, N, S, INV>(buf, h, l, t, nt);
+}
+
+template <int LOG2N, int s>
+__host__ __device__ constexpr int plan_used() {   // sum of the log-radices of passes 0..s-1
+  int u = 0;
+  for (int i = 0; i < s; i++) u += Plan<LOG2N>::lr(i);
+  return u;
+}
+
+// Forward transform, natural order in, digit-reversed out (posof).  Every
+// thread of the CTA must call it: each pass ends in __syncthreads.
+template <int LOG2N, int s = 0>
+__device__ __forceinline__ void fft_forward(float2* buf, const float2* h, const float2* l, int t, int nt) {
+  if constexpr (s < Plan<LOG2N>::n) {
+    pass_lr<Plan<LOG2N>::lr(s), (1 << LOG2N), ((1 << LOG2N) >> plan_used<LOG2N, s>()), false>(buf, h, l, t, nt);
+    __syncthreads();
+    fft_forward<LOG2N, s + 1>(buf, h, l, t, nt);
+  }
+}
+
+// Inverse (unnormalised), digit-reversed in, natural order out: the forward
+// passes undone in reverse order.
+template <int LOG2N, int s = Plan<LOG2N>::n - 1>
+__device__ __forceinline__ void fft_inverse(float2* buf, const float2* h, const float2* l, int t, int nt) {
+  if constexpr (s >= 0) {
+    pass_lr<Plan<LOG2N>::lr(s), (1 << LOG2N), ((1 << LOG2N) >> plan_used<LOG2N, s>()), true>(buf, h, l, t, nt);
+    __syncthreads();
+    fft_inverse<LOG2N, s - 1>(buf, h, l, t, nt);
+  }
+}
+
+// Ent (CrossCorr.cc:28-33) for windows holding a one-third IUPAC letter.
+__device__ __forceinline__ double ent_dev(double p) {
+  if (p < 0.001) return 0.0;
+  return __ddiv_rn(__dmul_rn(p, log(p)), 0.69314718056);
+}
+
+}  // namespace xc

@@ -31,10 +31,12 @@ struct __align__(16) PairDesc {
 };
 
 // Per-FFT-length device tables (host-built in double, rounded once).
+// Twiddles W_M^m = hi[m >> 6] * lo[m & 63] for M = N (transform) and M = L.
 struct LTables {
-  const float2* twN;       // exp(-2*pi*i*k/N), k < N, N = L/2
-  const float2* twL;       // exp(-2*pi*i*k/L), k < N
-  const uint16_t* pos_of;  // DIF output position of bin k, k < N
+  const float2* twN_hi;    // exp(-2*pi*i*64a/N), a < N/64, N = L/2
+  const float2* twN_lo;    // exp(-2*pi*i*b/N), b < 64
+  const float2* twL_hi;    // exp(-2*pi*i*64a/L), a < N/64
+  const float2* twL_lo;    // exp(-2*pi*i*b/L), b < 64
   const double* ent;       // Ent(p) for p = (a4/4)/k: [k][a4], k <= win, a4 <= 4*win
 };
 

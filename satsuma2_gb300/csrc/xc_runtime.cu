@@ -71,38 +71,6 @@ static const Codec& codec() {
   return c;
 }
 
-// Radix plan of the N-point transforms (must match fft_forward in the kernels).
-static std::vector<int> radix_plan(int log2N) {
-  switch (log2N) {
-    case 9: return {8, 8, 8};
-    case 10: return {16, 16, 4};
-    case 11: return {16, 16, 8};
-    case 12: return {16, 16, 16};
-    case 13: return {16, 16, 16, 2};
-  }
-  return {};
-}
-
-// Bin k held at DIF output position p: p = d0*r0 + p', k = r0 + R0*k(p').
-static std::vector<uint16_t> dif_positions(int log2N) {
-  const int N = 1 << log2N;
-  std::vector<int> R = radix_plan(log2N);
-  std::vector<uint16_t> pos_of(N);
-  for (int p = 0; p < N; p++) {
-    int k = 0, mult = 1, span = N, rem = p;
-    for (int r : R) {
-      const int d = span / r;
-      const int dig = rem / d;
-      rem %= d;
-      k += dig * mult;
-      mult *= r;
-      span = d;
-    }
-    pos_of[k] = (uint16_t)p;
-  }
-  return pos_of;
-}
-
 static int cuda_err(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return XC_OK;
   fprintf(stderr, "satsuma2_gb300: %s: %s\n", what, cudaGetErrorString(e));
@@ -117,14 +85,22 @@ static int cuda_err(cudaError_t e, const char* what) {
 static int build_tables(Ctx* c) {
   for (int lg = MIN_LOG2L; lg <= MAX_LOG2L; lg++) {
     const int L = 1 << lg, N = L / 2, win = L / 512;
-    std::vector<float2> twN(N), twL(N);
-    for (int k = 0; k < N; k++) {
-      const double a = -2.0 * M_PI * (double)k / (double)N;
-      twN[k] = make_float2((float)cos(a), (float)sin(a));
-      const double b = -2.0 * M_PI * (double)k / (double)L;
-      twL[k] = make_float2((float)cos(b), (float)sin(b));
+    // Two-level twiddle tables: W_M^m = hi[m >> 6] * lo[m & 63], M = N and L,
+    // each entry computed in double and rounded once.
+    const int NH = N / 64;
+    std::vector<float2> tw(2 * (NH + 64));
+    auto w = [](double num, double den) {
+      const double a = -2.0 * M_PI * num / den;
+      return make_float2((float)cos(a), (float)sin(a));
+    };
+    for (int i = 0; i < NH; i++) {
+      tw[i] = w(64.0 * i, N);
+      tw[NH + 64 + i] = w(64.0 * i, L);
     }
-    std::vector<uint16_t> pos = dif_positions(lg - 1);
+    for (int i = 0; i < 64; i++) {
+      tw[NH + i] = w(i, N);
+      tw[2 * NH + 64 + i] = w(i, L);
+    }
     // Ent(p) for p = (a4/4)/k (CrossCorr.cc:28-33,80-84), same double ops.
     const int row = 4 * win + 1;
     std::vector<double> ent((size_t)(win + 1) * row, 0.0);
@@ -135,13 +111,9 @@ static int build_tables(Ctx* c) {
         ent[(size_t)k * row + a4] = p < 0.001 ? 0.0 : p * log(p) / 0.69314718056;
       }
     DevTables& t = c->tab[lg];
-    XC_CHECK(cudaMalloc(&t.twN, N * sizeof(float2)));
-    XC_CHECK(cudaMalloc(&t.twL, N * sizeof(float2)));
-    XC_CHECK(cudaMalloc(&t.pos_of, N * sizeof(uint16_t)));
+    XC_CHECK(cudaMalloc(&t.tw, tw.size() * sizeof(float2)));
     XC_CHECK(cudaMalloc(&t.ent, ent.size() * sizeof(double)));
-    XC_CHECK(cudaMemcpy(t.twN, twN.data(), N * sizeof(float2), cudaMemcpyHostToDevice));
-    XC_CHECK(cudaMemcpy(t.twL, twL.data(), N * sizeof(float2), cudaMemcpyHostToDevice));
-    XC_CHECK(cudaMemcpy(t.pos_of, pos.data(), N * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    XC_CHECK(cudaMemcpy(t.tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice));
     XC_CHECK(cudaMemcpy(t.ent, ent.data(), ent.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
   const Codec& cd = codec();
@@ -383,9 +355,11 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     cp.pairs = b->d_desc;
     cp.pool = b->d_pool;
     cp.first = bk.first;
-    cp.tab.twN = t.twN;
-    cp.tab.twL = t.twL;
-    cp.tab.pos_of = t.pos_of;
+    const int NH = (1 << (bk.log2L - 1)) / 64;
+    cp.tab.twN_hi = t.tw;
+    cp.tab.twN_lo = t.tw + NH;
+    cp.tab.twL_hi = t.tw + NH + 64;
+    cp.tab.twL_lo = t.tw + 2 * NH + 64;
     cp.tab.ent = t.ent;
     cp.cutoff = c->prm.cutoff;
     cp.cutoff_fast = c->prm.cutoff_fast;
@@ -637,7 +611,7 @@ int xc_destroy(xc_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   delete c->work;
   for (auto& t : c->tab) {
-    cudaFree(t.twN); cudaFree(t.twL); cudaFree(t.pos_of); cudaFree(t.ent);
+    cudaFree(t.tw); cudaFree(t.ent);
   }
   cudaFree(c->d_score); cudaFree(c->d_eq); cudaFree(c->d_gcw); cudaFree(c->d_ptable);
   if (c->stream) cudaStreamDestroy(c->stream);

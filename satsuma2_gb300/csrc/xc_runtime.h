@@ -70,9 +70,7 @@ struct Batch {
 struct Server;
 
 struct DevTables {
-  float2* twN = nullptr;
-  float2* twL = nullptr;
-  uint16_t* pos_of = nullptr;
+  float2* tw = nullptr;    // W_N hi (N/64), W_N lo (64), W_L hi (N/64), W_L lo (64)
   double* ent = nullptr;
 };
 
