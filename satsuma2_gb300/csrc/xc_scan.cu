@@ -26,8 +26,9 @@ template <int LOG2L> struct ScanGeom {
   // the byte arrays, which that path no longer reads once the planes exist.
   static constexpr int QCAP = 2048;
   static constexpr size_t region = (size_t)QCAP * 8 > 2 * (size_t)N ? (size_t)QCAP * 8 : 2 * (size_t)N;
+  static constexpr int FW = (TW + 7) / 8;   // 32-bit flag entries per thread (4 bits per word)
   static constexpr size_t bytes =
-      (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK) * 4 + OFF_CHUNK * 2 + region;
+      (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK + FW * NT_SCAN) * 4 + OFF_CHUNK * 2 + region;
 };
 
 size_t scan_smem_bytes(int log2L) {
@@ -86,7 +87,8 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
   uint32_t* qb1 = qb0 + QWP;
   int* qgp = reinterpret_cast<int*>(qb1 + QWP);
   int* offs = qgp + (TW + 1);
-  uint16_t* order = reinterpret_cast<uint16_t*>(offs + OFF_CHUNK);
+  uint32_t* bflags = reinterpret_cast<uint32_t*>(offs + OFF_CHUNK);   // [FW][NT_SCAN] block masks of pass 1
+  uint16_t* order = reinterpret_cast<uint16_t*>(bflags + Gm::FW * NT_SCAN);
   uint8_t* st = reinterpret_cast<uint8_t*>(order + OFF_CHUNK);
   uint8_t* sq = st + N;
   uint2* queue = reinterpret_cast<uint2*>(st);   // bitplane path only, after the planes are built
@@ -343,49 +345,117 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
         const uint32_t q1 = __funnelshift_r(qb1[qw], qb1[qw + 1], sh);
         return ~((tb0[w] ^ q0) | (tb1[w] ^ q1));
       };
-      uint32_t e2 = eword(wfirst - 2), e1 = eword(wfirst - 1);
-      int pref = __popc(e2) + __popc(e1);
-      bool open = false;
-      int start = 0, base = 0;
-      for (int w = wfirst; w <= wlast; w++) {
-        const uint32_t e0 = eword(w);
-        const uint64_t U = ((uint64_t)e1 << 32) | e2;
+      // Valid check positions of word w as a bit mask.
+      auto validmask = [&](int w) -> uint32_t {
         const int lo = max(cfirst - 32 * w, 0), hi = min(clast - 32 * w, 31);
-        const uint32_t vm = (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
-        uint32_t g = 0;
+        return (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
+      };
+      // Pass 1, branch-free: per word a 4-bit mask of the 8-position blocks
+      // whose 53-position span [c0-45, c0+8) holds >= 19 equal bases; no
+      // window inside any other block can pass.  Masks go to shared memory,
+      // eight words per 32-bit entry, entries interleaved across threads.
+      {
+        uint32_t e2 = eword(wfirst - 2), e1 = eword(wfirst - 1);
+        uint32_t acc = 0;
+        for (int w = wfirst; w <= wlast; w++) {
+          const uint32_t e0 = eword(w);
+          const uint64_t U = ((uint64_t)e1 << 32) | e2;
+          const uint32_t vm = validmask(w);
+          uint32_t f = 0;
 #pragma unroll
-        for (int sb = 0; sb < 4; sb++) {
-          if (!((vm >> (8 * sb)) & 0xffu)) continue;
-          const int a = 8 * sb + 19;
-          const int c53 = __popcll(U >> a) + __popc(e0 & lowmask(a - 11));
-          if (c53 < MIN_HITS) continue;
-#pragma unroll
-          for (int u = 8 * sb; u < 8 * sb + 8; u++) {
-            const int wc = __popcll(U >> (u + 19)) + __popc(e0 & lowmask(u + 1));
-            if (wc >= MIN_HITS) g |= 1u << u;
+          for (int sb = 0; sb < 4; sb++) {
+            const int a = 8 * sb + 19;
+            const int c53 = __popcll(U >> a) + __popc(e0 & lowmask(a - 11));
+            f |= (uint32_t)((c53 >= MIN_HITS) && ((vm >> (8 * sb)) & 0xffu)) << sb;
           }
-        }
-        g &= vm;
-        const uint32_t prev = (g << 1) | (open ? 1u : 0u);
-        const uint32_t rise = g & ~prev;
-        const uint32_t fall = ~g & prev & vm;
-        uint32_t ev = rise | fall;
-        while (ev) {
-          const int u = __ffs(ev) - 1;
-          ev &= ev - 1;
-          if ((rise >> u) & 1u) {
-            start = 32 * w + u - 45;
-            base = pref - __popcll(U >> (u + 19));
-          } else {
-            push(key, pos, start, 32 * w + u, pref + __popc(e0 & lowmask(u)) - base);
+          const int q = w - wfirst;
+          acc |= f << (4 * (q & 7));
+          if ((q & 7) == 7 || w == wlast) {
+            bflags[(q >> 3) * NT_SCAN + tid] = acc;
+            acc = 0;
           }
+          e2 = e1;
+          e1 = e0;
         }
-        open = (g >> hi) & 1u;
-        if (w == wlast && open) push(key, pos, start, iend, pref + __popc(e0 & lowmask(iend - 32 * w)) - base);
-        pref += __popc(e0);
-        e2 = e1;
-        e1 = e0;
       }
+      // Pass 2, sparse: exact windows only in flagged blocks, then runs of
+      // passing checks.  A run is contiguous, so every word it covers is
+      // flagged and visited in order; its equal-base count is the rising
+      // window's count plus the bits after it.
+      const int nq = wlast - wfirst + 1;
+      bool open = false;
+      int start = 0, runcnt = 0, accpos = 0, lastw = -4;
+      uint32_t e2 = 0, e1 = 0, e0 = 0;
+      for (int q8 = 0; q8 * 8 < nq; q8++) {
+        uint32_t fw = bflags[q8 * NT_SCAN + tid];
+        while (fw) {
+          const int nib = (__ffs(fw) - 1) >> 2;
+          const uint32_t f = (fw >> (4 * nib)) & 15u;
+          fw &= ~(15u << (4 * nib));
+          const int w = wfirst + q8 * 8 + nib;
+          if (open && w != lastw + 1) {
+            // the run ended at the first check of the unflagged word lastw+1
+            push(key, pos, start, 32 * (lastw + 1), runcnt);
+            open = false;
+          }
+          if (w == lastw + 1) {
+            e2 = e1;
+            e1 = e0;
+            e0 = eword(w);
+          } else if (w == lastw + 2) {
+            e2 = e0;
+            e1 = eword(w - 1);
+            e0 = eword(w);
+          } else {
+            e2 = eword(w - 2);
+            e1 = eword(w - 1);
+            e0 = eword(w);
+          }
+          lastw = w;
+          const uint64_t U = ((uint64_t)e1 << 32) | e2;
+          const uint32_t vm = validmask(w);
+          uint32_t g = 0;
+#pragma unroll
+          for (int sb = 0; sb < 4; sb++) {
+            if (!((f >> sb) & 1u)) continue;
+#pragma unroll
+            for (int u = 8 * sb; u < 8 * sb + 8; u++) {
+              const int wc = __popcll(U >> (u + 19)) + __popc(e0 & lowmask(u + 1));
+              g |= (uint32_t)(wc >= MIN_HITS) << u;
+            }
+          }
+          g &= vm;
+          const uint32_t prev = (g << 1) | (open ? 1u : 0u);
+          const uint32_t rise = g & ~prev;
+          const uint32_t fall = ~g & prev & vm;
+          uint32_t ev = rise | fall;
+          while (ev) {
+            const int u = __ffs(ev) - 1;
+            ev &= ev - 1;
+            if ((rise >> u) & 1u) {
+              start = 32 * w + u - 45;
+              runcnt = __popcll(U >> (u + 19)) + __popc(e0 & lowmask(u + 1));   // window count at the rise
+              accpos = u + 1;
+              open = true;
+            } else {
+              runcnt += __popc(e0 & lowmask(u) & ~lowmask(accpos));
+              push(key, pos, start, 32 * w + u, runcnt);
+              open = false;
+            }
+          }
+          if (open) {
+            if (w == wlast) {
+              const int ue = iend - 32 * w;   // 1..32
+              push(key, pos, start, iend, runcnt + __popc(e0 & lowmask(ue) & ~lowmask(accpos)));
+              open = false;
+            } else {
+              runcnt += __popc(e0 & ~lowmask(accpos));
+              accpos = 0;
+            }
+          }
+        }
+      }
+      if (open) push(key, pos, start, 32 * (lastw + 1), runcnt);
     };
     for (;;) {
       int k0 = 0;

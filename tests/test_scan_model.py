@@ -1,0 +1,157 @@
+"""CPU model of the scan kernel's bitplane DoOne (xc_scan.cu): 2-bit planes,
+32-position equality words, the branch-free block screen (pass 1) and the
+sparse exact pass with run tracking (pass 2), restated with Python integers
+and checked against the oracle's DoOne on the same diagonals -- segments and
+their equal-base counts exactly."""
+import numpy as np
+import pytest
+
+import oracle
+from satsuma2_gb300 import workloads as W
+
+MIN_HITS = 19
+M32 = 0xFFFFFFFF
+
+
+def popc(x):
+    return bin(x).count("1")
+
+
+def lowmask(n):
+    return M32 if n >= 32 else (1 << n) - 1
+
+
+def planes(seq, nwords, pad=0):
+    codes = [((b >> 1) ^ (b >> 2)) & 3 for b in seq]
+    b0 = [0] * (nwords + pad)
+    b1 = [0] * (nwords + pad)
+    for i, c in enumerate(codes):
+        w = i // 32 + pad
+        b0[w] |= (c & 1) << (i & 31)
+        b1[w] |= (c >> 1) << (i & 31)
+    return b0, b1
+
+
+def model_doone(t, q, pos):
+    """Returns [(tstart, qstart, len, equal_bases)] as the kernel emits them."""
+    T, Q = len(t), len(q)
+    TW = max(T, Q) // 32 + 2
+    tb0, tb1 = planes(t, TW + 2)
+    qb0, qb1 = planes(q, TW + 8, pad=2)
+    i0 = max(0, -pos)
+    iend = min(T - 1, Q - pos)
+    cfirst, clast = i0 + 46, iend - 1
+    if clast < cfirst:
+        return []
+
+    def fs(lo, hi, sh):
+        return ((hi << 32 | lo) >> sh) & M32
+
+    def eword(w):
+        if w < 0:
+            return 0
+        qo = 32 * w + pos + 64
+        qw, sh = qo >> 5, qo & 31
+        q0 = fs(qb0[qw], qb0[qw + 1], sh)
+        q1 = fs(qb1[qw], qb1[qw + 1], sh)
+        return ~((tb0[w] ^ q0) | (tb1[w] ^ q1)) & M32
+
+    def validmask(w):
+        lo, hi = max(cfirst - 32 * w, 0), min(clast - 32 * w, 31)
+        return (M32 >> (31 - hi)) & (M32 << lo) & M32
+
+    wfirst, wlast = cfirst >> 5, clast >> 5
+    # pass 1
+    flags = {}
+    e2, e1 = eword(wfirst - 2), eword(wfirst - 1)
+    for w in range(wfirst, wlast + 1):
+        e0 = eword(w)
+        U = (e1 << 32) | e2
+        vm = validmask(w)
+        f = 0
+        for sb in range(4):
+            a = 8 * sb + 19
+            c53 = popc(U >> a) + popc(e0 & lowmask(a - 11))
+            if c53 >= MIN_HITS and (vm >> (8 * sb)) & 0xFF:
+                f |= 1 << sb
+        if f:
+            flags[w] = f
+        e2, e1 = e1, e0
+    # pass 2
+    out = []
+    opened, start, runcnt, accpos, lastw = False, 0, 0, 0, -4
+    e2 = e1 = e0 = 0
+    for w in sorted(flags):
+        f = flags[w]
+        if opened and w != lastw + 1:
+            out.append((start, 32 * (lastw + 1), runcnt))
+            opened = False
+        if w == lastw + 1:
+            e2, e1, e0 = e1, e0, eword(w)
+        elif w == lastw + 2:
+            e2, e1, e0 = e0, eword(w - 1), eword(w)
+        else:
+            e2, e1, e0 = eword(w - 2), eword(w - 1), eword(w)
+        lastw = w
+        U = (e1 << 32) | e2
+        vm = validmask(w)
+        g = 0
+        for sb in range(4):
+            if not (f >> sb) & 1:
+                continue
+            for u in range(8 * sb, 8 * sb + 8):
+                wc = popc(U >> (u + 19)) + popc(e0 & lowmask(u + 1))
+                if wc >= MIN_HITS:
+                    g |= 1 << u
+        g &= vm
+        prev = ((g << 1) | (1 if opened else 0)) & M32
+        rise = g & ~prev & M32
+        fall = ~g & prev & vm & M32
+        for u in range(32):
+            if (rise >> u) & 1:
+                start = 32 * w + u - 45
+                runcnt = popc(U >> (u + 19)) + popc(e0 & lowmask(u + 1))
+                accpos = u + 1
+                opened = True
+            elif (fall >> u) & 1:
+                runcnt += popc(e0 & lowmask(u) & ~lowmask(accpos) & M32)
+                out.append((start, 32 * w + u, runcnt))
+                opened = False
+        if opened:
+            if w == wlast:
+                ue = iend - 32 * w
+                out.append((start, iend, runcnt + popc(e0 & lowmask(ue) & ~lowmask(accpos) & M32)))
+                opened = False
+            else:
+                runcnt += popc(e0 & ~lowmask(accpos) & M32)
+                accpos = 0
+    if opened:
+        out.append((start, 32 * (lastw + 1), runcnt))
+    return [(s, s + pos, e - s, m) for s, e, m in out]
+
+
+def equal_bases(t, q, s, pos, ln):
+    return sum(1 for i in range(ln) if t[s + i] == q[s + pos + i])
+
+
+@pytest.fixture(scope="module")
+def O():
+    return oracle.Oracle()
+
+
+def test_model_matches_oracle_doone(O):
+    rng = np.random.default_rng(77)
+    cases = W.uniform_batch(6, seed=8) + [W.plain_pair(3)]
+    t = W.random_bases(rng, 4096)
+    cases.append((t.tobytes(), t.tobytes()))                      # identical: one long run
+    cases.append((t.tobytes(), W.tandem_repeat(rng, 4096, 2, 3).tobytes()))
+    for t, q in cases:
+        offs = O.findtop(O.xcorr64(t, q, 8192), 1.8)
+        extra = rng.integers(-4095, 4096, size=20)
+        for i in list(offs[:40]) + [int(x) + 4096 for x in extra]:
+            pos = int(i) - 4096
+            got = model_doone(t, q, pos)
+            want = O.doone(t, q, pos)
+            assert [g[:3] for g in got] == [tuple(x) for x in want.tolist()], pos
+            for s, qs, ln, m in got:
+                assert m == equal_bases(t, q, s, pos, ln)
