@@ -205,14 +205,18 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
     }
     __syncthreads();
 
-    // ---- 3. z[n] = target_c[n] + i*query_c[n]; the odd-bin group pre-twiddles
-    //      by W_L^n.  Both signals are zero past N, so the even bins of the
-    //      L-point transform are the N-point transform of z and the odd bins
-    //      that of z*W_L^n. ----
+    // ---- 3. z[n] = target_c[n] + i*query_c[n] to the even buffer and
+    //      z[n]*W_L^n to the odd buffer.  Both signals are zero past N, so the
+    //      even bins of the L-point transform are the N-point transform of z
+    //      and the odd bins that of z*W_L^n.  W_L^n = W_L^tid * W_L^(512 it):
+    //      one per-thread twiddle times a compile-time constant. ----
     {
-      float2* buf = grp ? bufO : bufE;
       const double offt = s_off[c], offq = s_off[4 + c];
-      for (int n = gtid; n < N; n += 256) {
+      const int stid = swz(tid);
+      const float2 wt = tw2(twLh, twLl, tid);
+#pragma unroll 4
+      for (int it = 0; it < N / NT_CORR; it++) {
+        const int n = tid + NT_CORR * it;
         float x = 0.f, y = 0.f;
         const int w = n / WIN;
         if (!generic) {
@@ -222,14 +226,16 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
           if (n < T) x = __double2float_rn(__dmul_rn((double)Et[w], __dsub_rn(c_wd[c][st[n]], offt)));
           if (n < Q) y = __double2float_rn(__dmul_rn((double)Eq[w], __dsub_rn(c_wd[c][sq[n]], offq)));
         }
-        if (P.dbg_sig && grp == 0) {
+        if (P.dbg_sig) {
           float* ds = P.dbg_sig + (size_t)(pidx * 2 + strand) * 8 * L;
           ds[(size_t)c * L + n] = x;
           ds[(size_t)(4 + c) * L + n] = y;
         }
-        float2 z = make_float2(x, y);
-        if (grp) z = cmul(z, tw2(twLh, twLl, n));
-        buf[swz(n)] = z;
+        const int sn = stid ^ swz(NT_CORR * it);   // tid and NT_CORR*it share no bit
+        // W_L^(512 it) = exp(-i pi (16384 it / L) / 16)
+        const float2 wc = make_float2(cos_pi16((16384 / L) * it), -sin_pi16((16384 / L) * it));
+        bufE[sn] = make_float2(x, y);
+        bufO[sn] = cmul(make_float2(x, y), cmul(wt, wc));
       }
     }
     __syncthreads();
@@ -240,19 +246,32 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
     // X = target spectrum, Y = query spectrum from Z(k), Z(L-k).
     // conj(X)Y on bins 1..N-2, X(0)Y(0) on bin 0, and the target's own value
     // on bins N-1 and N, which the reference's loop leaves unmultiplied.
+    // Addresses: swz(posof(.)) is XOR-linear, so for m = gtid + 256*it it is
+    // lp(gtid) ^ lp(256*it) with the second term a compile-time constant.
     if (grp == 0) {
-      for (int m = gtid; m <= N / 2; m += 256) {
-        const float2 A = bufE[swz(posof<LOG2N>(m))];
-        const float2 B = bufE[swz(posof<LOG2N>((N - m) & (N - 1)))];
+      const int la = lp<LOG2N>(gtid);
+      const int lb = lp<LOG2N>((256 - gtid) & 255);
+#pragma unroll
+      for (int it = 0; it <= N / 512; it++) {
+        const int m = gtid + 256 * it;
+        if (m > N / 2) break;
+        // partner N-m = (N - 256(it+1)) | (256 - gtid) for gtid >= 1
+        const int pb = gtid ? (lb ^ lp<LOG2N>(N - 256 * (it + 1))) : lp<LOG2N>((N - 256 * it) & (N - 1));
+        const float2 A = bufE[la ^ lp<LOG2N>(256 * it)];
+        const float2 B = bufE[pb];
         const float2 X = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
         const float2 Y = make_float2(0.5f * (A.y + B.y), -0.5f * (A.x - B.x));
         if (m == N / 2) accE[m].x += X.x;
         else accE[m] = cadd(accE[m], cmulc(Y, X));
       }
     } else {
-      for (int m = gtid; m < N / 2; m += 256) {
-        const float2 A = bufO[swz(posof<LOG2N>(m))];
-        const float2 B = bufO[swz(posof<LOG2N>(N - 1 - m))];
+      const int la = lp<LOG2N>(gtid);
+#pragma unroll
+      for (int it = 0; it < N / 512; it++) {
+        const int m = gtid + 256 * it;
+        const int pa = la ^ lp<LOG2N>(256 * it);
+        const float2 A = bufO[pa];
+        const float2 B = bufO[pa ^ lp<LOG2N>(N - 1)];   // N-1-m = m ^ (N-1)
         const float2 X = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
         const float2 Y = make_float2(0.5f * (A.y + B.y), -0.5f * (A.x - B.x));
         accO[m] = cadd(accO[m], m == N / 2 - 1 ? X : cmulc(Y, X));
@@ -265,20 +284,29 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
   //      Z(k) = E(k) + i O(k), E = (S(k) + conj S(N-k))/2,
   //      O = (S(k) - conj S(N-k)) conj(W_L^k)/2; z[m] = r[2m] + i r[2m+1]. ----
   auto S = [&](int k) -> float2 { return (k & 1) ? accO[k >> 1] : accE[k >> 1]; };
-  for (int k = tid; k <= N / 2; k += NT_CORR) {
-    const float2 Sk = S(k);
-    const float2 Sn = S(N - k);
-    {
-      const float2 Ev = make_float2(0.5f * (Sk.x + Sn.x), 0.5f * (Sk.y - Sn.y));
-      const float2 Dv = make_float2(0.5f * (Sk.x - Sn.x), 0.5f * (Sk.y + Sn.y));
-      const float2 Ov = cmulc(Dv, tw2(twLh, twLl, k));
-      bufE[swz(posof<LOG2N>(k))] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
-    }
-    if (k != 0 && k != N / 2) {
-      const float2 Ev = make_float2(0.5f * (Sn.x + Sk.x), 0.5f * (Sn.y - Sk.y));
-      const float2 Dv = make_float2(0.5f * (Sn.x - Sk.x), 0.5f * (Sn.y + Sk.y));
-      const float2 Ov = cmulc(Dv, tw2(twLh, twLl, N - k));
-      bufE[swz(posof<LOG2N>(N - k))] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
+  {
+    const int la = lp<LOG2N>(tid);
+    const int lb = lp<LOG2N>((NT_CORR - tid) & (NT_CORR - 1));
+#pragma unroll
+    for (int it = 0; it <= N / (2 * NT_CORR); it++) {
+      const int k = tid + NT_CORR * it;
+      if (k > N / 2) break;
+      const float2 Sk = S(k);
+      const float2 Sn = S(N - k);
+      {
+        const float2 Ev = make_float2(0.5f * (Sk.x + Sn.x), 0.5f * (Sk.y - Sn.y));
+        const float2 Dv = make_float2(0.5f * (Sk.x - Sn.x), 0.5f * (Sk.y + Sn.y));
+        const float2 Ov = cmulc(Dv, tw2(twLh, twLl, k));
+        bufE[la ^ lp<LOG2N>(NT_CORR * it)] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
+      }
+      if (k != 0 && k != N / 2) {
+        // N-k = (N - NT_CORR(it+1)) | (NT_CORR - tid) for tid >= 1
+        const int pb = tid ? (lb ^ lp<LOG2N>(N - NT_CORR * (it + 1))) : lp<LOG2N>(N - NT_CORR * it);
+        const float2 Ev = make_float2(0.5f * (Sn.x + Sk.x), 0.5f * (Sn.y - Sk.y));
+        const float2 Dv = make_float2(0.5f * (Sn.x - Sk.x), 0.5f * (Sn.y + Sk.y));
+        const float2 Ov = cmulc(Dv, tw2(twLh, twLl, N - k));
+        bufE[pb] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
+      }
     }
   }
   __syncthreads();

@@ -52,6 +52,17 @@ __host__ __device__ constexpr int swz(int p) { return p ^ (((p >> 4) ^ (p >> 8) 
 // set bit; the transform passes use that to turn every access into one XOR
 // with a compile-time constant.
 
+// cos(pi m / 16) and sin(pi m / 16) for any integer m, for compile-time twiddles.
+__host__ __device__ constexpr float cos_pi16(int m) {
+  constexpr float c[9] = {1.0f, 0.98078528040323043f, 0.92387953251128674f, 0.83146961230254524f,
+                          0.70710678118654752f, 0.55557023301960218f, 0.38268343236508978f,
+                          0.19509032201612826f, 0.0f};
+  m &= 31;                       // period 2*pi
+  if (m > 16) m = 32 - m;        // cos is even
+  return m <= 8 ? c[m] : -c[16 - m];
+}
+__host__ __device__ constexpr float sin_pi16(int m) { return cos_pi16(8 - m); }
+
 // Twiddle W_N^m from two small shared tables: hi[a] = W_N^(64a), lo[b] = W_N^b.
 __device__ __forceinline__ float2 tw2(const float2* hi, const float2* lo, int m) {
   return cmul(hi[m >> 6], lo[m & 63]);
@@ -75,7 +86,7 @@ template <> struct Plan<13> : PlanR<4, 4, 4, 1> {};
 // digit of radix R_s (least significant first in k) moves to place value
 // N / (R_0 ... R_s).
 template <int LOG2N>
-__device__ __forceinline__ int posof(int k) {
+__host__ __device__ constexpr int posof(int k) {
   using PL = Plan<LOG2N>;
   int p = 0, off = 0, used = 0;
 #pragma unroll
@@ -86,6 +97,11 @@ __device__ __forceinline__ int posof(int k) {
   }
   return p;
 }
+
+// Shared-memory index of bin k: swz(posof(k)).  Both maps are XOR-linear, so
+// lp(a | b) = lp(a) ^ lp(b) for bit-disjoint a and b.
+template <int LOG2N>
+__host__ __device__ constexpr int lp(int k) { return swz(posof<LOG2N>(k)); }
 
 // ---------------------------------------------------------------------------
 // Small DFTs in registers, natural order in and out.  DIR = -1 forward

@@ -386,9 +386,16 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
       bool open = false;
       int start = 0, runcnt = 0, accpos = 0, lastw = -4;
       uint32_t e2 = 0, e1 = 0, e0 = 0;
-      for (int q8 = 0; q8 * 8 < nq; q8++) {
-        uint32_t fw = bflags[q8 * NT_SCAN + tid];
-        while (fw) {
+      // One flat loop over this lane's flagged words (a cursor skips empty
+      // entries), so a warp runs max-over-lanes of the flagged-word count
+      // rather than that maximum per 8-word entry.
+      const int nq8 = (nq + 7) >> 3;
+      int q8 = 0;
+      uint32_t fw = bflags[tid];
+      for (;;) {
+        while (fw == 0 && ++q8 < nq8) fw = bflags[q8 * NT_SCAN + tid];
+        if (fw == 0) break;
+        {
           const int nib = (__ffs(fw) - 1) >> 2;
           const uint32_t f = (fw >> (4 * nib)) & 15u;
           fw &= ~(15u << (4 * nib));
