@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
       const double offt = s_off[c], offq = s_off[4 + c];
       const int stid = swz(tid);
       const float2 wt = tw2(twLh, twLl, tid);
-#pragma unroll 4
+#pragma unroll
       for (int it = 0; it < N / NT_CORR; it++) {
         const int n = tid + NT_CORR * it;
         float x = 0.f, y = 0.f;
