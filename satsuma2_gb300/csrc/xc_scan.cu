@@ -1,26 +1,20 @@
 // Scan and finalize kernels of the satsuma2 cross-correlation path (sm_103a).
 //
-//   scan_kernel<log2 L>  one CTA of 128 threads per (chunk pair, strand):
-//                        SeqAnalyzer::DoOne over every FindTop offset, then
-//                        FilterMatches on the raw segments.
-//     A/C/G/T pairs: 2-bit bitplanes give 32 equality bits per word op.
-//       pass 1 (one diagonal per lane): a branch-free screen marks the
-//         8-position blocks whose 53-position span holds >= 19 equal bases;
-//       pass 2 (one diagonal per warp, lanes = its marked words): exact
-//         windows, run boundaries from neighbour-lane shuffles, run starts
-//         from a warp max-scan, segments queued with one atomic per warp;
-//       drain (all threads): equal-base counts, FP32 probability screen,
-//         exact FP64 GetMatchProbability / PrintMatch for the survivors.
-//     Other pairs (N, IUPAC, unknown letters): the reference's byte-table
-//       DoOne per lane and the exact double sums.
+//   scan_kernel<log2 L>  one CTA per (chunk pair, strand): DoOne's ungapped
+//                        46-wide window scan of every FindTop offset on 2-bit
+//                        bitplanes (32 positions per word op, 8-position window
+//                        screening), then FilterMatches on the raw segments: an
+//                        FP32 screen of the match probability and the exact FP64
+//                        GetMatchProbability / PrintMatch tail for survivors.
 //   finalize kernels     order each strand's results as the reference appends
 //                        them and pack them densely.
 #include "xc_device.cuh"
 
-#include <limits.h>
-
 namespace xc {
 
+// ---------------------------------------------------------------------------
+// Scan kernel: DoOne + FilterMatches
+// ---------------------------------------------------------------------------
 template <int LOG2L> struct ScanGeom {
   static constexpr int L = 1 << LOG2L;
   static constexpr int N = L >> 1;
@@ -28,14 +22,13 @@ template <int LOG2L> struct ScanGeom {
   static constexpr int TWP = TW + 2;       // target plane words (zero padded)
   static constexpr int QPAD = 2;           // leading zero words of the query planes
   static constexpr int QWP = TW + 6;       // query plane words
-  static constexpr int FW = (TW + 7) / 8;  // pass-1 flag entries per thread (4 bits per word)
-  static constexpr int NWARP = NT_SCAN / 32;
   // Raw-segment queue of the bitplane path (8 bytes per segment).  It reuses
   // the byte arrays, which that path no longer reads once the planes exist.
   static constexpr int QCAP = 2048;
   static constexpr size_t region = (size_t)QCAP * 8 > 2 * (size_t)N ? (size_t)QCAP * 8 : 2 * (size_t)N;
-  static constexpr size_t bytes = (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK + FW * NT_SCAN) * 4 +
-                                  (size_t)OFF_CHUNK * 2 + (size_t)NWARP * TW * 2 + region;
+  static constexpr int FW = (TW + 7) / 8;   // 32-bit flag entries per thread (4 bits per word)
+  static constexpr size_t bytes =
+      (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK + FW * NT_SCAN) * 4 + OFF_CHUNK * 2 + region;
 };
 
 size_t scan_smem_bytes(int log2L) {
@@ -64,7 +57,7 @@ __device__ __forceinline__ int gc_count(const uint32_t* b0, const uint32_t* b1, 
   return ge - ga;
 }
 
-// Warp-cooperative prefix of per-word G/C counts -> pref[0..nw].
+// Warp-cooperative inclusive prefix of per-word G/C counts -> pref[0..nw].
 __device__ __forceinline__ void gc_prefix(const uint32_t* b0, const uint32_t* b1, int* pref, int nw, int lane) {
   int run = 0;
   for (int w0 = 0; w0 < nw; w0 += 32) {
@@ -82,30 +75,10 @@ __device__ __forceinline__ void gc_prefix(const uint32_t* b0, const uint32_t* b1
   if (lane == 0) pref[nw] = run;
 }
 
-__device__ __forceinline__ int warp_incl_sum(int v, int lane) {
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int u = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o) v += u;
-  }
-  return v;
-}
-
-__device__ __forceinline__ int warp_incl_max(int v, int lane) {
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int u = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o) v = max(v, u);
-  }
-  return v;
-}
-
 template <int LOG2L>
 __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
   using Gm = ScanGeom<LOG2L>;
   constexpr int L = Gm::L, N = Gm::N, TW = Gm::TW, TWP = Gm::TWP, QPAD = Gm::QPAD, QWP = Gm::QWP;
-  constexpr int QCAP = Gm::QCAP;
-  constexpr unsigned FULL = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
   uint32_t* tb0 = reinterpret_cast<uint32_t*>(smem);
   uint32_t* tb1 = tb0 + TWP;
@@ -114,12 +87,12 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
   uint32_t* qb1 = qb0 + QWP;
   int* qgp = reinterpret_cast<int*>(qb1 + QWP);
   int* offs = qgp + (TW + 1);
-  uint32_t* bflags = reinterpret_cast<uint32_t*>(offs + OFF_CHUNK);      // [FW][NT_SCAN] pass-1 block masks
+  uint32_t* bflags = reinterpret_cast<uint32_t*>(offs + OFF_CHUNK);   // [FW][NT_SCAN] block masks of pass 1
   uint16_t* order = reinterpret_cast<uint16_t*>(bflags + Gm::FW * NT_SCAN);
-  uint16_t* wlist = order + OFF_CHUNK;                                  // [NWARP][TW] marked words of one diagonal
-  uint8_t* st = reinterpret_cast<uint8_t*>(wlist + Gm::NWARP * TW);
+  uint8_t* st = reinterpret_cast<uint8_t*>(order + OFF_CHUNK);
   uint8_t* sq = st + N;
   uint2* queue = reinterpret_cast<uint2*>(st);   // bitplane path only, after the planes are built
+  constexpr int QCAP = Gm::QCAP;
   __shared__ int s_hist[64];
   __shared__ int s_next;
   __shared__ int s_res;
@@ -130,18 +103,17 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
   const int strand = blockIdx.y;
   const int slot = pidx * 2 + strand;
   const PairDesc D = P.pairs[pidx];
-  const uint32_t pflags = P.pair_flags[pidx];
+  const uint32_t flags = P.pair_flags[pidx];
   const int cnt = P.off_cnt[slot];
-  if ((pflags & PF_INVALID) || cnt <= 0) {
+  if ((flags & PF_INVALID) || cnt <= 0) {
     if (tid == 0) P.res_cnt[slot] = 0;
     return;
   }
   const int T = D.tlen, Q = D.qlen;
-  const bool generic = (pflags & PF_GENERIC) != 0;
+  const bool generic = (flags & PF_GENERIC) != 0;
   const uint8_t* __restrict__ gt = P.pool + D.t_off;
   const uint8_t* __restrict__ gq = P.pool + D.q_off;
 
-  // chunk bytes; strand 1 reverse-complements the query (DNAVector.cc:482-500)
   for (int i = tid; i < N; i += NT_SCAN) {
     st[i] = i < T ? gt[i] : 0;
     unsigned c = 0;
@@ -189,31 +161,9 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
 
   const int* __restrict__ olist = P.off_list + D.off_base + (size_t)strand * L;
 
-  // Equality bits of target positions [32w, 32w+32) on diagonal pos.
-  auto eword = [&](int pos, int w) -> uint32_t {
-    if (w < 0) return 0u;
-    const int qo = 32 * w + pos + 32 * QPAD;
-    const int qw = qo >> 5, sh = qo & 31;
-    const uint32_t q0 = __funnelshift_r(qb0[qw], qb0[qw + 1], sh);
-    const uint32_t q1 = __funnelshift_r(qb1[qw], qb1[qw + 1], sh);
-    return ~((tb0[w] ^ q0) | (tb1[w] ^ q1));
-  };
-  // Equal bases of segment [s0, s1) on diagonal pos.
-  auto seg_hits = [&](int pos, int s0, int s1) -> int {
-    int h = 0;
-    const int wa = s0 >> 5, wb = (s1 - 1) >> 5;
-    for (int w = wa; w <= wb; w++) {
-      uint32_t m = 0xffffffffu;
-      if (w == wa) m &= ~lowmask(s0 & 31);
-      if (w == wb) m &= lowmask(((s1 - 1) & 31) + 1);
-      h += __popc(eword(pos, w) & m);
-    }
-    return h;
-  };
-
-  // One DoOne segment [s0, s1) on offset pos (CrossCorr.cc:693,713) through
-  // FilterMatches (HomologyByXCorrSlave.cc:171-212).  hits: exact equal-base
-  // count for A/C/G/T pairs (ignored on the generic path).
+  // Emits one DoOne segment [s0, s1) on offset pos (CrossCorr.cc:693,713) and
+  // applies FilterMatches (HomologyByXCorrSlave.cc:171-212) to it.  hits:
+  // exact equal-base count for A/C/G/T pairs (ignored on the generic path).
   auto emit = [&](int key, int pos, int s0, int s1, int hits) {
     const int len = s1 - s0;
     if (P.dbg) {
@@ -299,13 +249,16 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
 
   for (int c0 = 0; c0 < cnt; c0 += OFF_CHUNK) {
     const int nc = min(OFF_CHUNK, cnt - c0);
-    // Queue slot q gets segment [s0, s1) of chunk-local offset li; a full
-    // queue falls back to handling the segment in place.
-    auto enqueue = [&](int q, int li, int pos, int s0, int s1) {
-      if (q < QCAP)
-        queue[q] = make_uint2((uint32_t)li | ((uint32_t)s0 << 16), (uint32_t)(s1 - s0));
+    // Bitplane path: queue a raw segment (chunk-local offset index, start,
+    // length, equal-base count) for the converged drain below; handle it in
+    // place only when the queue is full.
+    auto push = [&](int key, int pos, int s0, int s1, int hits) {
+      const int qi = atomicAdd(&s_qn, 1);
+      if (qi < QCAP)
+        queue[qi] = make_uint2((uint32_t)(key - c0) | ((uint32_t)s0 << 16),
+                               (uint32_t)(s1 - s0) | ((uint32_t)hits << 16));
       else
-        emit(c0 + li, pos, s0, s1, seg_hits(pos, s0, s1));
+        emit(key, pos, s0, s1, hits);
     };
     if (tid < 64) s_hist[tid] = 0;
     __syncthreads();
@@ -319,9 +272,21 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
     __syncthreads();
     if (warp == 0) {
       const int v0 = s_hist[lane], v1 = s_hist[lane + 32];
-      const int i0 = warp_incl_sum(v0, lane);
-      const int tot0 = __shfl_sync(FULL, i0, 31);
-      const int i1 = warp_incl_sum(v1, lane);
+      int a = v0 + v1;   // lanes own bins lane and lane+32: scan two halves
+      int i0 = v0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, i0, o);
+        if (lane >= o) i0 += u;
+      }
+      const int tot0 = __shfl_sync(0xffffffffu, i0, 31);
+      int i1 = v1;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, i1, o);
+        if (lane >= o) i1 += u;
+      }
+      (void)a;
       s_hist[lane] = i0 - v0;
       s_hist[lane + 32] = tot0 + i1 - v1;
     }
@@ -334,63 +299,68 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
     if (tid == 0) s_next = 0;
     __syncthreads();
 
-    // A warp takes 32 consecutive (similar-length) diagonals at a time.
-    for (;;) {
-      int k0 = 0;
-      if (lane == 0) k0 = atomicAdd(&s_next, 32);
-      k0 = __shfl_sync(FULL, k0, 0);
-      if (k0 >= nc) break;
-      const int k = k0 + lane;
-      const bool have = k < nc;
-      const int li = have ? (int)order[k] : 0;
-      const int pos = have ? offs[li] - N : 0;
+    // A warp takes 32 consecutive (similar-length) diagonals at a time and
+    // finishes them together, so its lanes stay converged.
+    auto process = [&](int k) {
+      const int li = order[k];
+      const int pos = offs[li] - N;
+      const int key = c0 + li;
       const int i0 = max(0, -pos);
       const int iend = min(T - 1, Q - pos);
-
       if (generic) {
         // SeqAnalyzer::DoOne, OPTIM_DOONE (CrossCorr.cc:667-724), byte table.
-        if (have) {
-          int match = 0, last = -1, n = 0;
-          for (int i = i0; i < T; i++) {
-            const int j = i + pos;
-            if (j >= Q || i + 1 >= T) {
-              if (last != -1) emit(c0 + li, pos, last, i, 0);
-              break;
-            }
-            match += __ldg(&P.score[st[i] * 128 + sq[j]]);
-            if (n > 45) {
-              match -= __ldg(&P.score[st[i - 46] * 128 + sq[j - 46]]);
-              if (match > 1889) {
-                if (last == -1) last = i - 45;
-              } else {
-                if (last != -1) emit(c0 + li, pos, last, i, 0);
-                last = -1;
-              }
-            }
-            n++;
+        int match = 0, last = -1, n = 0;
+        for (int i = i0; i < T; i++) {
+          const int j = i + pos;
+          if (j >= Q || i + 1 >= T) {
+            if (last != -1) emit(key, pos, last, i, 0);
+            break;
           }
+          match += __ldg(&P.score[st[i] * 128 + sq[j]]);
+          if (n > 45) {
+            match -= __ldg(&P.score[st[i - 46] * 128 + sq[j - 46]]);
+            if (match > 1889) {
+              if (last == -1) last = i - 45;
+            } else {
+              if (last != -1) emit(key, pos, last, i, 0);
+              last = -1;
+            }
+          }
+          n++;
         }
-        __syncwarp();
-        continue;
+        return;
       }
-
       // A/C/G/T: window sums are 100 x equal-base counts, so a window passes
       // when it holds >= 19 equal bases.  Check positions c run from i0+46 to
       // iend-1; window(c) = [c-45, c]; a segment is a maximal run of passing
       // checks [a..b], emitted as [a-45, b+1) (or [a-45, iend) at the end).
       const int cfirst = i0 + 46, clast = iend - 1;
-      const bool valid = have && clast >= cfirst;
+      if (clast < cfirst) return;
       const int wfirst = cfirst >> 5, wlast = clast >> 5;
-
-      // ---- pass 1 (lane = diagonal): block masks to bflags[q >> 3][tid] ----
-      if (valid) {
-        uint32_t e2 = eword(pos, wfirst - 2), e1 = eword(pos, wfirst - 1);
+      auto eword = [&](int w) -> uint32_t {
+        if (w < 0) return 0u;
+        const int qo = 32 * w + pos + 32 * QPAD;
+        const int qw = qo >> 5, sh = qo & 31;
+        const uint32_t q0 = __funnelshift_r(qb0[qw], qb0[qw + 1], sh);
+        const uint32_t q1 = __funnelshift_r(qb1[qw], qb1[qw + 1], sh);
+        return ~((tb0[w] ^ q0) | (tb1[w] ^ q1));
+      };
+      // Valid check positions of word w as a bit mask.
+      auto validmask = [&](int w) -> uint32_t {
+        const int lo = max(cfirst - 32 * w, 0), hi = min(clast - 32 * w, 31);
+        return (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
+      };
+      // Pass 1, branch-free: per word a 4-bit mask of the 8-position blocks
+      // whose 53-position span [c0-45, c0+8) holds >= 19 equal bases; no
+      // window inside any other block can pass.  Masks go to shared memory,
+      // eight words per 32-bit entry, entries interleaved across threads.
+      {
+        uint32_t e2 = eword(wfirst - 2), e1 = eword(wfirst - 1);
         uint32_t acc = 0;
         for (int w = wfirst; w <= wlast; w++) {
-          const uint32_t e0 = eword(pos, w);
+          const uint32_t e0 = eword(w);
           const uint64_t U = ((uint64_t)e1 << 32) | e2;
-          const int lo = max(cfirst - 32 * w, 0), hi = min(clast - 32 * w, 31);
-          const uint32_t vm = (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
+          const uint32_t vm = validmask(w);
           uint32_t f = 0;
 #pragma unroll
           for (int sb = 0; sb < 4; sb++) {
@@ -408,118 +378,99 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
           e1 = e0;
         }
       }
-      __syncwarp();
-
-      // ---- pass 2 (warp = diagonal j, lanes = its marked words) ----
-      uint16_t* wl = wlist + warp * TW;
-      for (int j = 0; j < 32; j++) {
-        if (!__shfl_sync(FULL, (int)valid, j)) continue;
-        const int jpos = __shfl_sync(FULL, pos, j);
-        const int jli = __shfl_sync(FULL, li, j);
-        const int jcf = __shfl_sync(FULL, cfirst, j);
-        const int jcl = __shfl_sync(FULL, clast, j);
-        const int jend = __shfl_sync(FULL, iend, j);
-        const int jwf = jcf >> 5, jwl = jcl >> 5;
-        const int owner = (warp << 5) + j;
-        const int nq8 = (jwl - jwf + 8) >> 3;
-        // gather the marked words of diagonal j in order
-        const uint32_t ent = lane < nq8 ? bflags[lane * NT_SCAN + owner] : 0u;
-        const uint32_t nz = (ent | (ent >> 1) | (ent >> 2) | (ent >> 3)) & 0x11111111u;
-        const int ncl = __popc(nz);
-        const int iincl = warp_incl_sum(ncl, lane);
-        const int F = __shfl_sync(FULL, iincl, 31);
+      // Pass 2, sparse: exact windows only in flagged blocks, then runs of
+      // passing checks.  A run is contiguous, so every word it covers is
+      // flagged and visited in order; its equal-base count is the rising
+      // window's count plus the bits after it.
+      const int nq = wlast - wfirst + 1;
+      bool open = false;
+      int start = 0, runcnt = 0, accpos = 0, lastw = -4;
+      uint32_t e2 = 0, e1 = 0, e0 = 0;
+      // One flat loop over this lane's flagged words (a cursor skips empty
+      // entries), so a warp runs max-over-lanes of the flagged-word count
+      // rather than that maximum per 8-word entry.
+      const int nq8 = (nq + 7) >> 3;
+      int q8 = 0;
+      uint32_t fw = bflags[tid];
+      for (;;) {
+        while (fw == 0 && ++q8 < nq8) fw = bflags[q8 * NT_SCAN + tid];
+        if (fw == 0) break;
         {
-          int o = iincl - ncl;
-          uint32_t m = nz;
-          while (m) {
-            const int nib = (__ffs(m) - 1) >> 2;
-            m &= m - 1;
-            wl[o++] = (uint16_t)((lane * 8 + nib) | (((ent >> (4 * nib)) & 15u) << 8));
+          const int nib = (__ffs(fw) - 1) >> 2;
+          const uint32_t f = (fw >> (4 * nib)) & 15u;
+          fw &= ~(15u << (4 * nib));
+          const int w = wfirst + q8 * 8 + nib;
+          if (open && w != lastw + 1) {
+            // the run ended at the first check of the unflagged word lastw+1
+            push(key, pos, start, 32 * (lastw + 1), runcnt);
+            open = false;
           }
-        }
-        __syncwarp();
-        int carry_w = INT_MIN / 2, carry_rise = -1;
-        uint32_t carry_b31 = 0;
-        for (int b = 0; b < F; b += 32) {
-          const int idx = b + lane;
-          const bool act = idx < F;
-          int w = INT_MIN / 2;
-          uint32_t g = 0, vm = 0;
-          if (act) {
-            const uint32_t e = wl[idx];
-            w = jwf + (int)(e & 255u);
-            const uint32_t f = e >> 8;
-            const uint32_t e2 = eword(jpos, w - 2), e1 = eword(jpos, w - 1), e0 = eword(jpos, w);
-            const uint64_t U = ((uint64_t)e1 << 32) | e2;
+          if (w == lastw + 1) {
+            e2 = e1;
+            e1 = e0;
+            e0 = eword(w);
+          } else if (w == lastw + 2) {
+            e2 = e0;
+            e1 = eword(w - 1);
+            e0 = eword(w);
+          } else {
+            e2 = eword(w - 2);
+            e1 = eword(w - 1);
+            e0 = eword(w);
+          }
+          lastw = w;
+          const uint64_t U = ((uint64_t)e1 << 32) | e2;
+          const uint32_t vm = validmask(w);
+          uint32_t g = 0;
 #pragma unroll
-            for (int sb = 0; sb < 4; sb++) {
-              if (!((f >> sb) & 1u)) continue;
+          for (int sb = 0; sb < 4; sb++) {
+            if (!((f >> sb) & 1u)) continue;
 #pragma unroll
-              for (int u = 8 * sb; u < 8 * sb + 8; u++) {
-                const int wc = __popcll(U >> (u + 19)) + __popc(e0 & lowmask(u + 1));
-                g |= (uint32_t)(wc >= MIN_HITS) << u;
-              }
+            for (int u = 8 * sb; u < 8 * sb + 8; u++) {
+              const int wc = __popcll(U >> (u + 19)) + __popc(e0 & lowmask(u + 1));
+              g |= (uint32_t)(wc >= MIN_HITS) << u;
             }
-            const int lo = max(jcf - 32 * w, 0), hi = min(jcl - 32 * w, 31);
-            vm = (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
-            g &= vm;
           }
-          // G just before this word: bit 31 of the previous marked word if adjacent
-          int pw = __shfl_up_sync(FULL, w, 1);
-          uint32_t pg = __shfl_up_sync(FULL, g, 1) >> 31;
-          if (lane == 0) { pw = carry_w; pg = carry_b31; }
-          const uint32_t pbit = (act && pw == w - 1) ? pg : 0u;
-          // next marked word
-          int nw = __shfl_down_sync(FULL, w, 1);
-          if (lane == 31) nw = (b + 32 < F) ? jwf + (int)(wl[b + 32] & 255u) : INT_MAX;
-          if (idx + 1 >= F) nw = INT_MAX;
-          const uint32_t prev = (g << 1) | pbit;
+          g &= vm;
+          const uint32_t prev = (g << 1) | (open ? 1u : 0u);
           const uint32_t rise = g & ~prev;
           const uint32_t fall = ~g & prev & vm;
-          // a run still open at the last valid check of this word ends at the
-          // next unmarked word's first check, or at the diagonal's end
-          int extra_end = -1;
-          if (act) {
-            const int hi = min(jcl - 32 * w, 31);
-            if ((g >> hi) & 1u) {
-              if (w == jwl) extra_end = jend;
-              else if (nw != w + 1) extra_end = 32 * (w + 1);
+          uint32_t ev = rise | fall;
+          while (ev) {
+            const int u = __ffs(ev) - 1;
+            ev &= ev - 1;
+            if ((rise >> u) & 1u) {
+              start = 32 * w + u - 45;
+              runcnt = __popcll(U >> (u + 19)) + __popc(e0 & lowmask(u + 1));   // window count at the rise
+              accpos = u + 1;
+              open = true;
+            } else {
+              runcnt += __popc(e0 & lowmask(u) & ~lowmask(accpos));
+              push(key, pos, start, 32 * w + u, runcnt);
+              open = false;
             }
           }
-          // latest rise before this word (warp max-scan, carried across batches)
-          const int lastr = rise ? 32 * w + (31 - __clz((int)rise)) : -1;
-          const int mx = warp_incl_max(lastr, lane);
-          int prior = __shfl_up_sync(FULL, mx, 1);
-          if (lane == 0) prior = -1;
-          prior = max(prior, carry_rise);
-          // segments: every fall and a closing end; one queue atomic per warp
-          const int nf = __popc(fall) + (extra_end >= 0);
-          const int fincl = warp_incl_sum(nf, lane);
-          const int ftot = __shfl_sync(FULL, fincl, 31);
-          int qbase = 0;
-          if (lane == 0 && ftot) qbase = atomicAdd(&s_qn, ftot);
-          qbase = __shfl_sync(FULL, qbase, 0);
-          int q = qbase + fincl - nf;
-          uint32_t fm = fall;
-          while (fm) {
-            const int u = __ffs(fm) - 1;
-            fm &= fm - 1;
-            const uint32_t rb = rise & lowmask(u);
-            const int sc = rb ? 32 * w + (31 - __clz((int)rb)) : prior;
-            if (sc >= 0) enqueue(q, jli, jpos, sc - 45, 32 * w + u);   // a fall always follows a rise
-            q++;
+          if (open) {
+            if (w == wlast) {
+              const int ue = iend - 32 * w;   // 1..32
+              push(key, pos, start, iend, runcnt + __popc(e0 & lowmask(ue) & ~lowmask(accpos)));
+              open = false;
+            } else {
+              runcnt += __popc(e0 & ~lowmask(accpos));
+              accpos = 0;
+            }
           }
-          if (extra_end >= 0) {
-            const int sc = rise ? lastr : prior;
-            if (sc >= 0) enqueue(q, jli, jpos, sc - 45, extra_end);
-          }
-          const int lastl = min(31, F - 1 - b);
-          carry_w = __shfl_sync(FULL, w, lastl);
-          carry_b31 = __shfl_sync(FULL, g, lastl) >> 31;
-          carry_rise = max(carry_rise, __shfl_sync(FULL, mx, 31));
         }
-        __syncwarp();
       }
+      if (open) push(key, pos, start, 32 * (lastw + 1), runcnt);
+    };
+    for (;;) {
+      int k0 = 0;
+      if (lane == 0) k0 = atomicAdd(&s_next, 32);
+      k0 = __shfl_sync(0xffffffffu, k0, 0);
+      if (k0 >= nc) break;
+      if (k0 + lane < nc) process(k0 + lane);
+      __syncwarp();
     }
     __syncthreads();
     // Drain the queued segments with every thread (converged warps).
@@ -527,10 +478,9 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
       const int qn = min(s_qn, QCAP);
       for (int e = tid; e < qn; e += NT_SCAN) {
         const uint2 g = queue[e];
-        const int li = (int)(g.x & 0xffffu), s0 = (int)(g.x >> 16);
-        const int s1 = s0 + (int)g.y;
-        const int pos = offs[li] - N;
-        emit(c0 + li, pos, s0, s1, seg_hits(pos, s0, s1));
+        const int key = (int)(g.x & 0xffffu), s0 = (int)(g.x >> 16);
+        const int len = (int)(g.y & 0xffffu), hits = (int)(g.y >> 16);
+        emit(c0 + key, offs[key] - N, s0, s0 + len, hits);
       }
       __syncthreads();
       if (tid == 0) s_qn = 0;
@@ -554,12 +504,23 @@ __global__ void __launch_bounds__(1024) count_scan_kernel(const int* __restrict_
   for (int c0 = 0; c0 < n; c0 += 1024) {
     const int i = c0 + tid;
     const int v = i < n ? min(cnt[i], slots) : 0;
-    const int incl = warp_incl_sum(v, lane);
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
     if (lane == 31) s_w[warp] = incl;
     __syncthreads();
     if (warp == 0) {
       const int x = s_w[lane];
-      s_w[lane] = warp_incl_sum(x, lane) - x;
+      int y = x;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= o) y += u;
+      }
+      s_w[lane] = y - x;
     }
     __syncthreads();
     const int carry = s_carry;

@@ -155,121 +155,3 @@ def test_model_matches_oracle_doone(O):
             assert [g[:3] for g in got] == [tuple(x) for x in want.tolist()], pos
             for s, qs, ln, m in got:
                 assert m == equal_bases(t, q, s, pos, ln)
-
-
-def model_doone_warp(t, q, pos):
-    """Pass 2 as the warp-cooperative kernel does it: marked words in batches
-    of 32 lanes, the previous lane's last G bit, a max-scan of rise positions
-    and a closing end for runs reaching an unmarked word or the diagonal end.
-    Returns segments sorted by start (the kernel queues them unordered)."""
-    T, Q = len(t), len(q)
-    TW = max(T, Q) // 32 + 2
-    tb0, tb1 = planes(t, TW + 2)
-    qb0, qb1 = planes(q, TW + 8, pad=2)
-    i0 = max(0, -pos)
-    iend = min(T - 1, Q - pos)
-    cfirst, clast = i0 + 46, iend - 1
-    if clast < cfirst:
-        return []
-
-    def fs(lo, hi, sh):
-        return ((hi << 32 | lo) >> sh) & M32
-
-    def eword(w):
-        if w < 0:
-            return 0
-        qo = 32 * w + pos + 64
-        qw, sh = qo >> 5, qo & 31
-        return ~((tb0[w] ^ fs(qb0[qw], qb0[qw + 1], sh)) | (tb1[w] ^ fs(qb1[qw], qb1[qw + 1], sh))) & M32
-
-    def vmask(w):
-        lo, hi = max(cfirst - 32 * w, 0), min(clast - 32 * w, 31)
-        return (M32 >> (31 - hi)) & (M32 << lo) & M32
-
-    wfirst, wlast = cfirst >> 5, clast >> 5
-    marked = []
-    for w in range(wfirst, wlast + 1):
-        e2, e1, e0 = eword(w - 2), eword(w - 1), eword(w)
-        U = (e1 << 32) | e2
-        vm = vmask(w)
-        f = 0
-        for sb in range(4):
-            a = 8 * sb + 19
-            if popc(U >> a) + popc(e0 & lowmask(a - 11)) >= MIN_HITS and (vm >> (8 * sb)) & 0xFF:
-                f |= 1 << sb
-        if f:
-            marked.append((w, f))
-    segs = []
-    carry_w, carry_b31, carry_rise = -10 ** 9, 0, -1
-    F = len(marked)
-    for b in range(0, F, 32):
-        lanes = []
-        for lane in range(32):
-            idx = b + lane
-            if idx >= F:
-                lanes.append(None)
-                continue
-            w, f = marked[idx]
-            e2, e1, e0 = eword(w - 2), eword(w - 1), eword(w)
-            U = (e1 << 32) | e2
-            g = 0
-            for sb in range(4):
-                if (f >> sb) & 1:
-                    for u in range(8 * sb, 8 * sb + 8):
-                        if popc(U >> (u + 19)) + popc(e0 & lowmask(u + 1)) >= MIN_HITS:
-                            g |= 1 << u
-            vm = vmask(w)
-            lanes.append((w, g & vm, vm))
-        mx = -1
-        for lane in range(32):
-            if lanes[lane] is None:
-                continue
-            w, g, vm = lanes[lane]
-            if lane == 0:
-                pw, pg = carry_w, carry_b31
-            else:
-                pw, pg = lanes[lane - 1][0], lanes[lane - 1][1] >> 31
-            pbit = pg if pw == w - 1 else 0
-            idx = b + lane
-            nw = marked[idx + 1][0] if idx + 1 < F else 10 ** 9
-            prev = ((g << 1) | pbit) & M32
-            rise = g & ~prev & M32
-            fall = ~g & prev & vm & M32
-            hi = min(clast - 32 * w, 31)
-            extra = -1
-            if (g >> hi) & 1:
-                if w == wlast:
-                    extra = iend
-                elif nw != w + 1:
-                    extra = 32 * (w + 1)
-            lastr = 32 * w + rise.bit_length() - 1 if rise else -1
-            prior = max(mx, carry_rise)
-            mx = max(mx, lastr)
-            for u in range(32):
-                if (fall >> u) & 1:
-                    rb = rise & lowmask(u)
-                    sc = 32 * w + rb.bit_length() - 1 if rb else prior
-                    segs.append((sc - 45, 32 * w + u))
-            if extra >= 0:
-                segs.append(((lastr if rise else prior) - 45, extra))
-        last = [l for l in lanes if l is not None][-1]
-        carry_w, carry_b31 = last[0], last[1] >> 31
-        carry_rise = max(carry_rise, mx)
-    segs.sort()
-    return [(s, s + pos, e - s, equal_bases(t, q, s, pos, e - s)) for s, e in segs]
-
-
-def test_warp_model_matches_oracle_doone(O):
-    rng = np.random.default_rng(78)
-    cases = W.uniform_batch(5, seed=9) + [W.plain_pair(4)]
-    t = W.random_bases(rng, 4096)
-    cases.append((t.tobytes(), t.tobytes()))
-    cases.append((t.tobytes(), W.tandem_repeat(rng, 4096, 2, 3).tobytes()))
-    for t, q in cases:
-        offs = O.findtop(O.xcorr64(t, q, 8192), 1.8)
-        extra = rng.integers(-4095, 4096, size=15)
-        for i in list(offs[:30]) + [int(x) + 4096 for x in extra]:
-            pos = int(i) - 4096
-            got = model_doone_warp(t, q, pos)
-            want = O.doone(t, q, pos)
-            assert [g[:3] for g in got] == [tuple(x) for x in want.tolist()], pos
