@@ -87,8 +87,7 @@ struct ScanParams {
   double ptable_cutoff;
   double min_prob;
   double target_total;
-  float screen_expect;      // -log(min_prob) * 1.01 (FP32 screen bound), +inf if min_prob <= 0
-  float target_total_f;
+  float screen_z;           // FP32 screen: reject when pm*N - hits > screen_z * sd (+inf keeps all)
   int min_len;
   int slots;                // result slots per pair strand
   DevResult* res;           // [pair*2+strand][slots]

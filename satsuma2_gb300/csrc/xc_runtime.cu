@@ -344,6 +344,30 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   return XC_OK;
 }
 
+// z-score threshold of the scan kernel's FP32 screen.  A segment is kept when
+// exp(-Phi(z) * targetTotal) >= min_prob, z = (pm*N - hits) / sd
+// (AlignProbability.cc:107-125), i.e. when Phi(z) <= -log(min_prob) /
+// targetTotal, i.e. z <= z*.  z* comes from bisection on the normal CDF in
+// double, with the bound raised by 1% and by 4.5e-16 -- the reference forms
+// Phi as 0.5 * (1 + erf(.)), which loses everything below ~1e-16 to
+// cancellation, so its exact test accepts up to that much beyond the true CDF.
+// The kernel rejects only above z* + 0.02, orders of magnitude beyond the
+// FP32 error of its z; survivors take the exact FP64 test.
+static float screen_z(double min_prob, double target_total) {
+  if (!(min_prob > 0) || !(target_total > 0)) return INFINITY;
+  const double bound = -log(min_prob);
+  if (!(bound >= 0)) return -INFINITY;   // min_prob > 1: nothing passes the exact test either
+  const double r = bound / target_total * 1.01 + 4.5e-16;
+  if (r >= 1.0) return INFINITY;
+  double lo = -60.0, hi = 60.0;          // Phi(lo) < r <= Phi(hi) for every r the doubles reach
+  for (int it = 0; it < 200; it++) {
+    const double mid = 0.5 * (lo + hi);
+    if (0.5 * erfc(-mid / sqrt(2.0)) <= r) lo = mid; else hi = mid;
+  }
+  return (float)(hi + 0.02);
+}
+
+
 // Enqueues the kernels of one batch on stream.
 static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
   const int nslots = 2 * b->n;
@@ -386,10 +410,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     sp.ptable_cutoff = c->prm.prob_table_cutoff;
     sp.min_prob = c->prm.min_prob;
     sp.target_total = c->prm.target_total;
-    // Screen bound on expect = cdf*targetTotal: keep if exp(-expect) >= min_prob.
-    double bound = c->prm.min_prob > 0 ? -log(c->prm.min_prob) : INFINITY;
-    sp.screen_expect = bound < 0 ? 0.f : (float)(bound * 1.01 + 1e-30);
-    sp.target_total_f = (float)c->prm.target_total;
+    sp.screen_z = screen_z(c->prm.min_prob, c->prm.target_total);
     sp.min_len = c->prm.min_len;
     sp.slots = b->slots;
     sp.res = b->d_res;
@@ -450,6 +471,10 @@ int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, 
   const int novf = b->h_misc[0];
   const int err = b->h_misc[1];
   if (err & 1) return XC_ERR_CAPACITY;   // caller re-runs with a bigger overflow pool
+  if (err & 4) {
+    fprintf(stderr, "satsuma2_gb300: scan kernel: inconsistent segment bounds\n");
+    return XC_ERR_CUDA;
+  }
   int r;
   if ((r = host_grow(b->h_dense, b->cap_h_dense, (size_t)total + 1)) != XC_OK) return r;
   if (total) XC_CHECK(cudaMemcpyAsync(b->h_dense, b->d_dense, total * sizeof(DevResult), cudaMemcpyDeviceToHost, s));

@@ -1,11 +1,22 @@
 // Scan and finalize kernels of the satsuma2 cross-correlation path (sm_103a).
 //
-//   scan_kernel<log2 L>  one CTA per (chunk pair, strand): DoOne's ungapped
-//                        46-wide window scan of every FindTop offset on 2-bit
-//                        bitplanes (32 positions per word op, 8-position window
-//                        screening), then FilterMatches on the raw segments: an
-//                        FP32 screen of the match probability and the exact FP64
-//                        GetMatchProbability / PrintMatch tail for survivors.
+//   scan_kernel<log2 L>  one CTA of 128 threads per (chunk pair, strand):
+//                        SeqAnalyzer::DoOne over every FindTop offset, then
+//                        FilterMatches on the raw segments.
+//     A/C/G/T pairs, in rounds of 128 diagonals (longest first):
+//       pass 1 (thread = diagonal): on 2-bit bitplanes, 32 equality bits per
+//         word op, a branch-free screen marks the 8-check blocks whose
+//         53-position span holds >= 19 equal bases;
+//       items: the marked blocks of the round laid out contiguously per
+//         diagonal by a prefix sum, processed one per thread --
+//         phase A: the block's 8 exact window bits;
+//         phase B: rises and falls against the previous block's last bit,
+//           run starts from the same block or by looking back, segments
+//           queued with one atomic per warp;
+//       drain (thread = segment): equal-base counts, FP32 probability
+//         screen, exact FP64 GetMatchProbability / PrintMatch for survivors.
+//     Other pairs (N, IUPAC, unknown letters): the reference's byte-table
+//       DoOne per lane and the exact double sums.
 //   finalize kernels     order each strand's results as the reference appends
 //                        them and pack them densely.
 #include "xc_device.cuh"
@@ -22,13 +33,16 @@ template <int LOG2L> struct ScanGeom {
   static constexpr int TWP = TW + 2;       // target plane words (zero padded)
   static constexpr int QPAD = 2;           // leading zero words of the query planes
   static constexpr int QWP = TW + 6;       // query plane words
-  // Raw-segment queue of the bitplane path (8 bytes per segment).  It reuses
-  // the byte arrays, which that path no longer reads once the planes exist.
-  static constexpr int QCAP = 2048;
-  static constexpr size_t region = (size_t)QCAP * 8 > 2 * (size_t)N ? (size_t)QCAP * 8 : 2 * (size_t)N;
-  static constexpr int FW = (TW + 7) / 8;   // 32-bit flag entries per thread (4 bits per word)
-  static constexpr size_t bytes =
-      (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK + FW * NT_SCAN) * 4 + OFF_CHUNK * 2 + region;
+  static constexpr int FW = (TW + 7) / 8;  // flag entries per diagonal (8 words x 4 blocks each)
+  // Marked-block items of one pass-2 sub-range and the segment queue (4 bytes
+  // each; item indices fit 12 bits).  The queue shares its bytes with the
+  // chunk byte arrays, which only the byte-table path fills.
+  static constexpr int ICAP = 3072;
+  static constexpr int QCAP = 3072;
+  static constexpr size_t region = (size_t)QCAP * 4 > 2 * (size_t)N ? (size_t)QCAP * 4 : 2 * (size_t)N;
+  static constexpr size_t bytes = region +
+      (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK + FW * NT_SCAN + ICAP + NT_SCAN) * 4 +
+      (size_t)OFF_CHUNK * 2;
 };
 
 size_t scan_smem_bytes(int log2L) {
@@ -57,18 +71,22 @@ __device__ __forceinline__ int gc_count(const uint32_t* b0, const uint32_t* b1, 
   return ge - ga;
 }
 
-// Warp-cooperative inclusive prefix of per-word G/C counts -> pref[0..nw].
+__device__ __forceinline__ int warp_incl_sum(int v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  return v;
+}
+
+// Warp-cooperative exclusive prefix of per-word G/C counts -> pref[0..nw].
 __device__ __forceinline__ void gc_prefix(const uint32_t* b0, const uint32_t* b1, int* pref, int nw, int lane) {
   int run = 0;
   for (int w0 = 0; w0 < nw; w0 += 32) {
     const int w = w0 + lane;
     const int c = w < nw ? __popc(b0[w] ^ b1[w]) : 0;
-    int incl = c;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += v;
-    }
+    const int incl = warp_incl_sum(c, lane);
     if (w < nw) pref[w] = run + incl - c;
     run += __shfl_sync(0xffffffffu, incl, 31);
   }
@@ -79,79 +97,82 @@ template <int LOG2L>
 __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
   using Gm = ScanGeom<LOG2L>;
   constexpr int L = Gm::L, N = Gm::N, TW = Gm::TW, TWP = Gm::TWP, QPAD = Gm::QPAD, QWP = Gm::QWP;
+  constexpr int ICAP = Gm::ICAP, QCAP = Gm::QCAP, NWARP = NT_SCAN / 32;
+  constexpr unsigned FULL = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
-  uint32_t* tb0 = reinterpret_cast<uint32_t*>(smem);
+  uint8_t* st = smem;
+  uint8_t* sq = st + N;
+  uint32_t* queue = reinterpret_cast<uint32_t*>(smem);   // bitplane path only: item | bit << 12
+  uint32_t* tb0 = reinterpret_cast<uint32_t*>(smem + Gm::region);
   uint32_t* tb1 = tb0 + TWP;
   int* tgp = reinterpret_cast<int*>(tb1 + TWP);
   uint32_t* qb0 = reinterpret_cast<uint32_t*>(tgp + (TW + 1));
   uint32_t* qb1 = qb0 + QWP;
   int* qgp = reinterpret_cast<int*>(qb1 + QWP);
   int* offs = qgp + (TW + 1);
-  uint32_t* bflags = reinterpret_cast<uint32_t*>(offs + OFF_CHUNK);   // [FW][NT_SCAN] block masks of pass 1
-  uint16_t* order = reinterpret_cast<uint16_t*>(bflags + Gm::FW * NT_SCAN);
-  uint8_t* st = reinterpret_cast<uint8_t*>(order + OFF_CHUNK);
-  uint8_t* sq = st + N;
-  uint2* queue = reinterpret_cast<uint2*>(st);   // bitplane path only, after the planes are built
-  constexpr int QCAP = Gm::QCAP;
+  uint32_t* bflags = reinterpret_cast<uint32_t*>(offs + OFF_CHUNK);   // [FW][NT_SCAN] pass-1 block masks
+  uint32_t* items = bflags + Gm::FW * NT_SCAN;                        // [ICAP] diag | block << 7 | G << 24
+  int* dpos = reinterpret_cast<int*>(items + ICAP);                   // [NT_SCAN] offsets of the round
+  uint16_t* order = reinterpret_cast<uint16_t*>(dpos + NT_SCAN);
   __shared__ int s_hist[64];
-  __shared__ int s_next;
-  __shared__ int s_res;
-  __shared__ int s_qn;
+  __shared__ int s_wsum[NWARP];
+  __shared__ int s_next, s_res, s_qn;
+  __shared__ int s_cy_d[2], s_cy_blk[2], s_cy_g[2], s_cy_start[2];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int pidx = P.first + blockIdx.x;
   const int strand = blockIdx.y;
   const int slot = pidx * 2 + strand;
   const PairDesc D = P.pairs[pidx];
-  const uint32_t flags = P.pair_flags[pidx];
+  const uint32_t pflags = P.pair_flags[pidx];
   const int cnt = P.off_cnt[slot];
-  if ((flags & PF_INVALID) || cnt <= 0) {
+  if ((pflags & PF_INVALID) || cnt <= 0) {
     if (tid == 0) P.res_cnt[slot] = 0;
     return;
   }
   const int T = D.tlen, Q = D.qlen;
-  const bool generic = (flags & PF_GENERIC) != 0;
+  const bool generic = (pflags & PF_GENERIC) != 0;
   const uint8_t* __restrict__ gt = P.pool + D.t_off;
   const uint8_t* __restrict__ gq = P.pool + D.q_off;
 
-  for (int i = tid; i < N; i += NT_SCAN) {
-    st[i] = i < T ? gt[i] : 0;
-    unsigned c = 0;
-    if (i < Q) {
-      const unsigned raw = strand ? gq[Q - 1 - i] : gq[i];
-      c = strand ? c_rc[raw] : raw;
-    }
-    sq[i] = (uint8_t)c;
-  }
   if (tid == 0) {
     s_res = 0;
     s_qn = 0;
   }
-  __syncthreads();
-  if (!generic) {
-    // 2-bit codes as two bitplanes, bit u of word w = position 32w+u.
-    for (int w = tid; w < TWP; w += NT_SCAN) {
-      uint32_t b0 = 0, b1 = 0;
-      if (w < TW) {
-        for (int u = 0; u < 32; u++) {
-          const int i = 32 * w + u;
-          if (i < T) { const uint32_t cd = code_of(st[i]); b0 |= (cd & 1u) << u; b1 |= (cd >> 1) << u; }
-        }
+  if (generic) {
+    // chunk bytes; strand 1 reverse-complements the query (DNAVector.cc:482-500)
+    for (int i = tid; i < N; i += NT_SCAN) {
+      st[i] = i < T ? gt[i] : 0;
+      unsigned c = 0;
+      if (i < Q) {
+        const unsigned raw = strand ? gq[Q - 1 - i] : gq[i];
+        c = strand ? c_rc[raw] : raw;
       }
-      tb0[w] = b0;
-      tb1[w] = b1;
+      sq[i] = (uint8_t)c;
     }
-    for (int w = tid; w < QWP; w += NT_SCAN) {
-      uint32_t b0 = 0, b1 = 0;
-      const int ww = w - QPAD;
-      if (ww >= 0 && ww < TW) {
-        for (int u = 0; u < 32; u++) {
-          const int i = 32 * ww + u;
-          if (i < Q) { const uint32_t cd = code_of(sq[i]); b0 |= (cd & 1u) << u; b1 |= (cd >> 1) << u; }
-        }
+  } else {
+    // 2-bit codes as two bitplanes straight from the pool, bit u of word w =
+    // position 32w+u: one warp per word, one ballot per plane.  The pair is
+    // all A/C/G/T, whose complement flips both code bits.
+    for (int w = warp; w < TWP; w += NWARP) {
+      const int i = 32 * w + lane;
+      const bool in = i < T;
+      const uint32_t cd = in ? code_of(gt[i]) : 0u;
+      const uint32_t b0 = __ballot_sync(FULL, cd & 1u), b1 = __ballot_sync(FULL, cd & 2u);
+      if (lane == 0) {
+        tb0[w] = b0;
+        tb1[w] = b1;
       }
-      qb0[w] = b0;
-      qb1[w] = b1;
+    }
+    for (int w = warp; w < QWP; w += NWARP) {
+      const int i = 32 * (w - QPAD) + lane;
+      const bool in = i >= 0 && i < Q;
+      const uint32_t cd = in ? (strand ? code_of(gq[Q - 1 - i]) ^ 3u : code_of(gq[i])) : 0u;
+      const uint32_t b0 = __ballot_sync(FULL, cd & 1u), b1 = __ballot_sync(FULL, cd & 2u);
+      if (lane == 0) {
+        qb0[w] = b0;
+        qb1[w] = b1;
+      }
     }
     __syncthreads();
     if (warp == 0) gc_prefix(tb0, tb1, tgp, TW, lane);
@@ -161,9 +182,31 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
 
   const int* __restrict__ olist = P.off_list + D.off_base + (size_t)strand * L;
 
-  // Emits one DoOne segment [s0, s1) on offset pos (CrossCorr.cc:693,713) and
-  // applies FilterMatches (HomologyByXCorrSlave.cc:171-212) to it.  hits:
-  // exact equal-base count for A/C/G/T pairs (ignored on the generic path).
+  // Equality bits of target positions [32w, 32w+32) on diagonal pos.
+  auto eword = [&](int pos, int w) -> uint32_t {
+    if (w < 0) return 0u;
+    const int qo = 32 * w + pos + 32 * QPAD;
+    const int qw = qo >> 5, sh = qo & 31;
+    const uint32_t q0 = __funnelshift_r(qb0[qw], qb0[qw + 1], sh);
+    const uint32_t q1 = __funnelshift_r(qb1[qw], qb1[qw + 1], sh);
+    return ~((tb0[w] ^ q0) | (tb1[w] ^ q1));
+  };
+  // Equal bases of segment [s0, s1) on diagonal pos.
+  auto seg_hits = [&](int pos, int s0, int s1) -> int {
+    int h = 0;
+    const int wa = s0 >> 5, wb = (s1 - 1) >> 5;
+    for (int w = wa; w <= wb; w++) {
+      uint32_t m = 0xffffffffu;
+      if (w == wa) m &= ~lowmask(s0 & 31);
+      if (w == wb) m &= lowmask(((s1 - 1) & 31) + 1);
+      h += __popc(eword(pos, w) & m);
+    }
+    return h;
+  };
+
+  // One DoOne segment [s0, s1) on offset pos (CrossCorr.cc:693,713) through
+  // FilterMatches (HomologyByXCorrSlave.cc:171-212).  hits: exact equal-base
+  // count for A/C/G/T pairs (ignored on the generic path).
   auto emit = [&](int key, int pos, int s0, int s1, int hits) {
     const int len = s1 - s0;
     if (P.dbg) {
@@ -183,14 +226,13 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
       const int gT = gc_count(tb0, tb1, tgp, s0, s1);
       const int gQ = gc_count(qb0 + QPAD, qb1 + QPAD, qgp, s0 + pos, s1 + pos);
       if (!P.ptable) {
-        // FP32 screen: reject only when the expectation clears the bound by
-        // 1%, far beyond FP32 error; anything else goes to the exact test.
+        // FP32 screen on the z-score (pm*N - hits) / sd: reject only past a
+        // threshold set on the host with a margin far beyond FP32 error;
+        // anything else goes to the exact test.
         const float Nf = (float)len, gq = (float)gQ, gtf = (float)gT / Nf;
         const float pm = (gq * gtf + (Nf - gq) * (1.f - gtf)) / Nf * 0.5f;
         const float sg = sqrtf(pm * (1.f - pm) * Nf);
-        const float arg = (pm * Nf - (float)hits) / sg * 0.70710678118654752f;
-        const float ex = 0.5f * erfcf(-arg) * P.target_total_f;
-        if (ex > P.screen_expect) return;
+        if (pm * Nf - (float)hits > P.screen_z * sg) return;
       }
       matches = (double)hits;
       gcT = (double)gT;
@@ -249,20 +291,10 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
 
   for (int c0 = 0; c0 < cnt; c0 += OFF_CHUNK) {
     const int nc = min(OFF_CHUNK, cnt - c0);
-    // Bitplane path: queue a raw segment (chunk-local offset index, start,
-    // length, equal-base count) for the converged drain below; handle it in
-    // place only when the queue is full.
-    auto push = [&](int key, int pos, int s0, int s1, int hits) {
-      const int qi = atomicAdd(&s_qn, 1);
-      if (qi < QCAP)
-        queue[qi] = make_uint2((uint32_t)(key - c0) | ((uint32_t)s0 << 16),
-                               (uint32_t)(s1 - s0) | ((uint32_t)hits << 16));
-      else
-        emit(key, pos, s0, s1, hits);
-    };
     if (tid < 64) s_hist[tid] = 0;
     __syncthreads();
-    // Longest diagonals first so the warps of the CTA stay balanced.
+    // Longest diagonals first: the threads of a round and the lanes of a warp
+    // get diagonals of similar length.
     for (int k = tid; k < nc; k += NT_SCAN) {
       const int o = olist[c0 + k];
       offs[k] = o;
@@ -272,21 +304,9 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
     __syncthreads();
     if (warp == 0) {
       const int v0 = s_hist[lane], v1 = s_hist[lane + 32];
-      int a = v0 + v1;   // lanes own bins lane and lane+32: scan two halves
-      int i0 = v0;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int u = __shfl_up_sync(0xffffffffu, i0, o);
-        if (lane >= o) i0 += u;
-      }
-      const int tot0 = __shfl_sync(0xffffffffu, i0, 31);
-      int i1 = v1;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int u = __shfl_up_sync(0xffffffffu, i1, o);
-        if (lane >= o) i1 += u;
-      }
-      (void)a;
+      const int i0 = warp_incl_sum(v0, lane);
+      const int tot0 = __shfl_sync(FULL, i0, 31);
+      const int i1 = warp_incl_sum(v1, lane);
       s_hist[lane] = i0 - v0;
       s_hist[lane + 32] = tot0 + i1 - v1;
     }
@@ -299,68 +319,72 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
     if (tid == 0) s_next = 0;
     __syncthreads();
 
-    // A warp takes 32 consecutive (similar-length) diagonals at a time and
-    // finishes them together, so its lanes stay converged.
-    auto process = [&](int k) {
-      const int li = order[k];
-      const int pos = offs[li] - N;
-      const int key = c0 + li;
+    if (generic) {
+      // A warp takes 32 consecutive (similar-length) diagonals at a time.
+      for (;;) {
+        int k0 = 0;
+        if (lane == 0) k0 = atomicAdd(&s_next, 32);
+        k0 = __shfl_sync(FULL, k0, 0);
+        if (k0 >= nc) break;
+        if (k0 + lane < nc) {
+          const int li = order[k0 + lane];
+          const int pos = offs[li] - N;
+          const int key = c0 + li;
+          const int i0 = max(0, -pos);
+          // SeqAnalyzer::DoOne, OPTIM_DOONE (CrossCorr.cc:667-724), byte table.
+          int match = 0, last = -1, n = 0;
+          for (int i = i0; i < T; i++) {
+            const int j = i + pos;
+            if (j >= Q || i + 1 >= T) {
+              if (last != -1) emit(key, pos, last, i, 0);
+              break;
+            }
+            match += __ldg(&P.score[st[i] * 128 + sq[j]]);
+            if (n > 45) {
+              match -= __ldg(&P.score[st[i - 46] * 128 + sq[j - 46]]);
+              if (match > 1889) {
+                if (last == -1) last = i - 45;
+              } else {
+                if (last != -1) emit(key, pos, last, i, 0);
+                last = -1;
+              }
+            }
+            n++;
+          }
+        }
+        __syncwarp();
+      }
+      __syncthreads();
+      continue;
+    }
+
+    // A/C/G/T: window sums are 100 x equal-base counts, so a window passes
+    // when it holds >= 19 equal bases.  Check positions c run from i0+46 to
+    // iend-1; window(c) = [c-45, c]; a segment is a maximal run of passing
+    // checks [a..b], emitted as [a-45, b+1) (or [a-45, iend) at the end).
+    for (int r0 = 0; r0 < nc; r0 += NT_SCAN) {
+      const int k = r0 + tid;
+      const bool have = k < nc;
+      const int pos = have ? offs[order[k]] - N : 0;
+      dpos[tid] = pos;
       const int i0 = max(0, -pos);
       const int iend = min(T - 1, Q - pos);
-      if (generic) {
-        // SeqAnalyzer::DoOne, OPTIM_DOONE (CrossCorr.cc:667-724), byte table.
-        int match = 0, last = -1, n = 0;
-        for (int i = i0; i < T; i++) {
-          const int j = i + pos;
-          if (j >= Q || i + 1 >= T) {
-            if (last != -1) emit(key, pos, last, i, 0);
-            break;
-          }
-          match += __ldg(&P.score[st[i] * 128 + sq[j]]);
-          if (n > 45) {
-            match -= __ldg(&P.score[st[i - 46] * 128 + sq[j - 46]]);
-            if (match > 1889) {
-              if (last == -1) last = i - 45;
-            } else {
-              if (last != -1) emit(key, pos, last, i, 0);
-              last = -1;
-            }
-          }
-          n++;
-        }
-        return;
-      }
-      // A/C/G/T: window sums are 100 x equal-base counts, so a window passes
-      // when it holds >= 19 equal bases.  Check positions c run from i0+46 to
-      // iend-1; window(c) = [c-45, c]; a segment is a maximal run of passing
-      // checks [a..b], emitted as [a-45, b+1) (or [a-45, iend) at the end).
       const int cfirst = i0 + 46, clast = iend - 1;
-      if (clast < cfirst) return;
+      const bool valid = have && clast >= cfirst;
       const int wfirst = cfirst >> 5, wlast = clast >> 5;
-      auto eword = [&](int w) -> uint32_t {
-        if (w < 0) return 0u;
-        const int qo = 32 * w + pos + 32 * QPAD;
-        const int qw = qo >> 5, sh = qo & 31;
-        const uint32_t q0 = __funnelshift_r(qb0[qw], qb0[qw + 1], sh);
-        const uint32_t q1 = __funnelshift_r(qb1[qw], qb1[qw + 1], sh);
-        return ~((tb0[w] ^ q0) | (tb1[w] ^ q1));
-      };
-      // Valid check positions of word w as a bit mask.
-      auto validmask = [&](int w) -> uint32_t {
-        const int lo = max(cfirst - 32 * w, 0), hi = min(clast - 32 * w, 31);
-        return (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
-      };
-      // Pass 1, branch-free: per word a 4-bit mask of the 8-position blocks
-      // whose 53-position span [c0-45, c0+8) holds >= 19 equal bases; no
-      // window inside any other block can pass.  Masks go to shared memory,
-      // eight words per 32-bit entry, entries interleaved across threads.
-      {
-        uint32_t e2 = eword(wfirst - 2), e1 = eword(wfirst - 1);
+
+      // ---- pass 1 (thread = diagonal): a 4-bit block mask per word, eight
+      //      words per entry in bflags[q >> 3][tid]; no window inside an
+      //      unmarked block can pass.
+      int nb = 0;
+      if (valid) {
+        uint32_t e2 = eword(pos, wfirst - 2), e1 = eword(pos, wfirst - 1);
         uint32_t acc = 0;
         for (int w = wfirst; w <= wlast; w++) {
-          const uint32_t e0 = eword(w);
+          const uint32_t e0 = eword(pos, w);
           const uint64_t U = ((uint64_t)e1 << 32) | e2;
-          const uint32_t vm = validmask(w);
+          const int lo = max(cfirst - 32 * w, 0), hi = min(clast - 32 * w, 31);
+          const uint32_t vm = (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
           uint32_t f = 0;
 #pragma unroll
           for (int sb = 0; sb < 4; sb++) {
@@ -372,118 +396,174 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
           acc |= f << (4 * (q & 7));
           if ((q & 7) == 7 || w == wlast) {
             bflags[(q >> 3) * NT_SCAN + tid] = acc;
+            nb += __popc(acc);
             acc = 0;
           }
           e2 = e1;
           e1 = e0;
         }
       }
-      // Pass 2, sparse: exact windows only in flagged blocks, then runs of
-      // passing checks.  A run is contiguous, so every word it covers is
-      // flagged and visited in order; its equal-base count is the rising
-      // window's count plus the bits after it.
-      const int nq = wlast - wfirst + 1;
-      bool open = false;
-      int start = 0, runcnt = 0, accpos = 0, lastw = -4;
-      uint32_t e2 = 0, e1 = 0, e0 = 0;
-      // One flat loop over this lane's flagged words (a cursor skips empty
-      // entries), so a warp runs max-over-lanes of the flagged-word count
-      // rather than that maximum per 8-word entry.
-      const int nq8 = (nq + 7) >> 3;
-      int q8 = 0;
-      uint32_t fw = bflags[tid];
-      for (;;) {
-        while (fw == 0 && ++q8 < nq8) fw = bflags[q8 * NT_SCAN + tid];
-        if (fw == 0) break;
-        {
-          const int nib = (__ffs(fw) - 1) >> 2;
-          const uint32_t f = (fw >> (4 * nib)) & 15u;
-          fw &= ~(15u << (4 * nib));
-          const int w = wfirst + q8 * 8 + nib;
-          if (open && w != lastw + 1) {
-            // the run ended at the first check of the unflagged word lastw+1
-            push(key, pos, start, 32 * (lastw + 1), runcnt);
-            open = false;
-          }
-          if (w == lastw + 1) {
-            e2 = e1;
-            e1 = e0;
-            e0 = eword(w);
-          } else if (w == lastw + 2) {
-            e2 = e0;
-            e1 = eword(w - 1);
-            e0 = eword(w);
-          } else {
-            e2 = eword(w - 2);
-            e1 = eword(w - 1);
-            e0 = eword(w);
-          }
-          lastw = w;
-          const uint64_t U = ((uint64_t)e1 << 32) | e2;
-          const uint32_t vm = validmask(w);
-          uint32_t g = 0;
+      // item index of this diagonal's first marked block: CTA exclusive scan
+      const int nincl = warp_incl_sum(nb, lane);
+      if (lane == 31) s_wsum[warp] = nincl;
+      if (tid == 0) s_cy_d[1] = -1;   // nothing carried into the first sub-range
+      __syncthreads();
+      int ibase = nincl - nb, total = 0;
 #pragma unroll
-          for (int sb = 0; sb < 4; sb++) {
-            if (!((f >> sb) & 1u)) continue;
-#pragma unroll
-            for (int u = 8 * sb; u < 8 * sb + 8; u++) {
-              const int wc = __popcll(U >> (u + 19)) + __popc(e0 & lowmask(u + 1));
-              g |= (uint32_t)(wc >= MIN_HITS) << u;
+      for (int x = 0; x < NWARP; x++) {
+        const int v = s_wsum[x];
+        ibase += x < warp ? v : 0;
+        total += v;
+      }
+
+      // ---- pass 2 over sub-ranges of at most ICAP items.  A sub-range may
+      //      split a diagonal: its last item (block, bits, open-run start)
+      //      is carried into the next one.
+      int par = 0;
+      for (int g0 = 0; g0 < total; g0 += ICAP, par ^= 1) {
+        const int n = min(ICAP, total - g0);
+        const int g1 = g0 + n;
+        if (nb && ibase < g1 && ibase + nb > g0) {
+          int kk = ibase;
+          const int nq8 = (wlast - wfirst + 8) >> 3;
+          for (int q8 = 0; q8 < nq8 && kk < g1; q8++) {
+            uint32_t ent = bflags[q8 * NT_SCAN + tid];
+            const int c = __popc(ent);
+            if (kk + c <= g0) {
+              kk += c;
+              continue;
             }
-          }
-          g &= vm;
-          const uint32_t prev = (g << 1) | (open ? 1u : 0u);
-          const uint32_t rise = g & ~prev;
-          const uint32_t fall = ~g & prev & vm;
-          uint32_t ev = rise | fall;
-          while (ev) {
-            const int u = __ffs(ev) - 1;
-            ev &= ev - 1;
-            if ((rise >> u) & 1u) {
-              start = 32 * w + u - 45;
-              runcnt = __popcll(U >> (u + 19)) + __popc(e0 & lowmask(u + 1));   // window count at the rise
-              accpos = u + 1;
-              open = true;
-            } else {
-              runcnt += __popc(e0 & lowmask(u) & ~lowmask(accpos));
-              push(key, pos, start, 32 * w + u, runcnt);
-              open = false;
-            }
-          }
-          if (open) {
-            if (w == wlast) {
-              const int ue = iend - 32 * w;   // 1..32
-              push(key, pos, start, iend, runcnt + __popc(e0 & lowmask(ue) & ~lowmask(accpos)));
-              open = false;
-            } else {
-              runcnt += __popc(e0 & ~lowmask(accpos));
-              accpos = 0;
+            while (ent) {
+              const int bi = __ffs(ent) - 1;
+              ent &= ent - 1;
+              if (kk >= g0 && kk < g1) items[kk - g0] = (uint32_t)tid | ((uint32_t)(32 * q8 + bi) << 7);
+              kk++;
             }
           }
         }
+        __syncthreads();
+
+        // ---- phase A (thread = item): exact window bits of the block's
+        //      8 checks, window(c) = window(c-1) + e[c] - e[c-46].
+        for (int i = tid; i < n; i += NT_SCAN) {
+          const uint32_t it = items[i];
+          const int d = (int)(it & 127u), blk = (int)((it >> 7) & 2047u);
+          const int p = dpos[d];
+          const int cf = max(0, -p) + 46, cl = min(T - 1, Q - p) - 1;
+          const int sb = blk & 3, w = (cf >> 5) + (blk >> 2);
+          const int cb = 32 * w + 8 * sb;
+          const uint32_t e2 = eword(p, w - 2), e1 = eword(p, w - 1), e0 = eword(p, w);
+          const uint64_t U = ((uint64_t)e1 << 32) | e2;
+          const uint32_t Y = e0 >> (8 * sb);
+          const uint32_t X = (uint32_t)(U >> (8 * sb + 18));
+          int c = __popcll(U >> (8 * sb + 19)) + __popc(e0 & lowmask(8 * sb + 1));
+          uint32_t g = (uint32_t)(c >= MIN_HITS);
+#pragma unroll
+          for (int u = 1; u < 8; u++) {
+            c += (int)((Y >> u) & 1u) - (int)((X >> u) & 1u);
+            g |= (uint32_t)(c >= MIN_HITS) << u;
+          }
+          const int lo = max(cf - cb, 0), hi = min(cl - cb, 7);
+          const uint32_t vm8 = (0xffu >> (7 - hi)) & (0xffu << lo);
+          items[i] = it | ((g & vm8) << 24);
+        }
+        __syncthreads();
+
+        // ---- phase B (thread = item): falls and closing ends of runs of
+        //      passing checks, queued as (item, bit) descriptors.
+        const int cy = par ^ 1;   // carry slot written by the previous sub-range
+        auto prev_bit = [&](int i, int d, int blk) -> uint32_t {
+          if (i > 0) {
+            const uint32_t pv = items[i - 1];
+            return ((int)(pv & 127u) == d && (int)((pv >> 7) & 2047u) == blk - 1) ? (pv >> 31) : 0u;
+          }
+          return (s_cy_d[cy] == d && s_cy_blk[cy] == blk - 1) ? (((uint32_t)s_cy_g[cy] >> 7) & 1u) : 0u;
+        };
+        // check position where the run holding bit u-1 of item i began
+        auto run_start = [&](int i, int d, int blk, uint32_t g, int u) -> int {
+          uint32_t rb = g & ~(((g << 1) | prev_bit(i, d, blk)) & 0xffu) & lowmask(u);
+          while (!rb) {
+            if (--i < 0) return s_cy_start[cy];
+            const uint32_t it = items[i];
+            blk = (int)((it >> 7) & 2047u);
+            g = it >> 24;
+            rb = g & ~(((g << 1) | prev_bit(i, d, blk)) & 0xffu);
+          }
+          return 32 * ((max(0, -dpos[d]) + 46) >> 5) + 8 * blk + (31 - __clz((int)rb));
+        };
+        // segment ending at bit u (0..7: a fall; 8: the closing end) of item i
+        auto segment = [&](int i, int u) {
+          const uint32_t it = items[i];
+          const int d = (int)(it & 127u), blk = (int)((it >> 7) & 2047u);
+          const uint32_t g = it >> 24;
+          const int p = dpos[d];
+          const int cf = max(0, -p) + 46, ie = min(T - 1, Q - p), cl = ie - 1;
+          const int cb = 32 * (cf >> 5) + 8 * blk;
+          int s1 = cb + u, ub = u;
+          if (u == 8) {
+            const int hi = min(cl - cb, 7);
+            s1 = cb + hi == cl ? ie : cb + 8;
+            ub = hi + 1;
+          }
+          const int s0 = run_start(i, d, blk, g, ub) - 45;
+          if (s0 < 1 || s1 <= s0) {   // cannot happen: a run start precedes its end
+            atomicOr(P.err, 4);
+            return;
+          }
+          emit(c0 + order[r0 + d], p, s0, s1, seg_hits(p, s0, s1));
+        };
+        for (int ib = 0; ib < n; ib += NT_SCAN) {
+          const int i = ib + tid;
+          uint32_t ends = 0;   // fall bits, bit 8 = closing end
+          if (i < n) {
+            const uint32_t it = items[i];
+            const int d = (int)(it & 127u), blk = (int)((it >> 7) & 2047u);
+            const uint32_t g = it >> 24;
+            const int p = dpos[d];
+            const int cf = max(0, -p) + 46, cl = min(T - 1, Q - p) - 1;
+            const int cb = 32 * (cf >> 5) + 8 * blk;
+            const int lo = max(cf - cb, 0), hi = min(cl - cb, 7);
+            const uint32_t vm8 = (0xffu >> (7 - hi)) & (0xffu << lo);
+            ends = ~g & (((g << 1) | prev_bit(i, d, blk)) & 0xffu) & vm8;
+            // a run still open at the block's last valid check ends at the
+            // diagonal's end or at the first check of an unmarked next block
+            if (((g >> hi) & 1u) &&
+                (cb + hi == cl || !((bflags[((blk + 1) >> 5) * NT_SCAN + d] >> ((blk + 1) & 31)) & 1u)))
+              ends |= 0x100u;
+            if (i == n - 1) {   // carried into the next sub-range
+              s_cy_d[par] = d;
+              s_cy_blk[par] = blk;
+              s_cy_g[par] = (int)g;
+              s_cy_start[par] = ((g >> 7) & 1u) ? run_start(i, d, blk, g, 8) : -1;
+            }
+          }
+          const int nseg = __popc(ends);
+          const int sincl = warp_incl_sum(nseg, lane);
+          int q = 0;
+          if (lane == 31 && sincl) q = atomicAdd(&s_qn, sincl);
+          q = __shfl_sync(FULL, q, 31) + sincl - nseg;
+          while (ends) {
+            const int u = __ffs(ends) - 1;
+            ends &= ends - 1;
+            if (q < QCAP)
+              queue[q] = (uint32_t)i | ((uint32_t)u << 12);
+            else
+              segment(i, u);   // full queue: in place
+            q++;
+          }
+        }
+        __syncthreads();
+
+        // ---- phase C (thread = segment): run start, equal-base count,
+        //      FilterMatches.
+        const int qn = min(s_qn, QCAP);
+        for (int e = tid; e < qn; e += NT_SCAN) {
+          const uint32_t sg = queue[e];
+          segment((int)(sg & 4095u), (int)(sg >> 12));
+        }
+        __syncthreads();
+        if (tid == 0) s_qn = 0;
       }
-      if (open) push(key, pos, start, 32 * (lastw + 1), runcnt);
-    };
-    for (;;) {
-      int k0 = 0;
-      if (lane == 0) k0 = atomicAdd(&s_next, 32);
-      k0 = __shfl_sync(0xffffffffu, k0, 0);
-      if (k0 >= nc) break;
-      if (k0 + lane < nc) process(k0 + lane);
-      __syncwarp();
-    }
-    __syncthreads();
-    // Drain the queued segments with every thread (converged warps).
-    if (!generic) {
-      const int qn = min(s_qn, QCAP);
-      for (int e = tid; e < qn; e += NT_SCAN) {
-        const uint2 g = queue[e];
-        const int key = (int)(g.x & 0xffffu), s0 = (int)(g.x >> 16);
-        const int len = (int)(g.y & 0xffffu), hits = (int)(g.y >> 16);
-        emit(c0 + key, offs[key] - N, s0, s0 + len, hits);
-      }
-      __syncthreads();
-      if (tid == 0) s_qn = 0;
       __syncthreads();
     }
   }

@@ -155,3 +155,123 @@ def test_model_matches_oracle_doone(O):
             assert [g[:3] for g in got] == [tuple(x) for x in want.tolist()], pos
             for s, qs, ln, m in got:
                 assert m == equal_bases(t, q, s, pos, ln)
+
+
+def model_doone_items(t, q, pos, icap=4096):
+    """Pass 2 as the item kernel does it: every flagged 8-check block is an
+    item (contiguous per diagonal, in block order); phase A gives each item
+    its 8 exact window bits, phase B finds rises and falls from the previous
+    item's last bit and takes a fall's run start from the same item or by
+    looking back over the items before it.  Items are processed in
+    sub-ranges of icap with the last item of one sub-range carried into the
+    next.  Returns segments sorted by start (the kernel queues them unordered)."""
+    T, Q = len(t), len(q)
+    TW = max(T, Q) // 32 + 2
+    tb0, tb1 = planes(t, TW + 2)
+    qb0, qb1 = planes(q, TW + 8, pad=2)
+    i0 = max(0, -pos)
+    iend = min(T - 1, Q - pos)
+    cfirst, clast = i0 + 46, iend - 1
+    if clast < cfirst:
+        return []
+
+    def fs(lo, hi, sh):
+        return ((hi << 32 | lo) >> sh) & M32
+
+    def eword(w):
+        if w < 0:
+            return 0
+        qo = 32 * w + pos + 64
+        qw, sh = qo >> 5, qo & 31
+        return ~((tb0[w] ^ fs(qb0[qw], qb0[qw + 1], sh)) | (tb1[w] ^ fs(qb1[qw], qb1[qw + 1], sh))) & M32
+
+    def vmask(w):
+        lo, hi = max(cfirst - 32 * w, 0), min(clast - 32 * w, 31)
+        return (M32 >> (31 - hi)) & (M32 << lo) & M32
+
+    wfirst, wlast = cfirst >> 5, clast >> 5
+    flagged = set()
+    for w in range(wfirst, wlast + 1):
+        e2, e1, e0 = eword(w - 2), eword(w - 1), eword(w)
+        U = (e1 << 32) | e2
+        vm = vmask(w)
+        for sb in range(4):
+            a = 8 * sb + 19
+            if popc(U >> a) + popc(e0 & lowmask(a - 11)) >= MIN_HITS and (vm >> (8 * sb)) & 0xFF:
+                flagged.add(4 * (w - wfirst) + sb)
+    blks = sorted(flagged)
+    # phase A
+    G = []
+    for blk in blks:
+        w, sb = wfirst + (blk >> 2), blk & 3
+        e2, e1, e0 = eword(w - 2), eword(w - 1), eword(w)
+        U = (e1 << 32) | e2
+        g = 0
+        for u in range(8):
+            c = 8 * sb + u
+            if popc(U >> (c + 19)) + popc(e0 & lowmask(c + 1)) >= MIN_HITS:
+                g |= 1 << u
+        G.append(g & (vmask(w) >> (8 * sb)) & 0xFF)
+
+    def rise_of(i, pbit):
+        return G[i] & ~(((G[i] << 1) | pbit) & 0xFF) & 0xFF
+
+    segs = []
+    carry = None   # (blk, G, open-run start) of the previous sub-range's last item
+    for g0 in range(0, len(blks), icap):
+        g1 = min(len(blks), g0 + icap)
+
+        def pbit_of(i):
+            if i > g0:
+                return (G[i - 1] >> 7) if blks[i - 1] == blks[i] - 1 else 0
+            if carry is not None and carry[0] == blks[i] - 1:
+                return carry[1] >> 7
+            return 0
+
+        def run_start(i, u):
+            """Check position where the run holding bit u-1 of item i began."""
+            rb = rise_of(i, pbit_of(i)) & lowmask(u)
+            while not rb:
+                i -= 1
+                if i < g0:
+                    return carry[2]
+                rb = rise_of(i, pbit_of(i))
+            return 32 * (wfirst + (blks[i] >> 2)) + 8 * (blks[i] & 3) + rb.bit_length() - 1
+
+        for i in range(g0, g1):
+            blk, g = blks[i], G[i]
+            w, sb = wfirst + (blk >> 2), blk & 3
+            c0 = 32 * w + 8 * sb
+            vm8 = (vmask(w) >> (8 * sb)) & 0xFF
+            hi = min(clast - c0, 7)
+            prev = ((g << 1) | pbit_of(i)) & 0xFF
+            fall = ~g & prev & vm8 & 0xFF
+            for u in range(8):
+                if (fall >> u) & 1:
+                    segs.append((run_start(i, u) - 45, c0 + u))
+            if (g >> hi) & 1:
+                if c0 + hi == clast:
+                    segs.append((run_start(i, hi + 1) - 45, iend))
+                elif blk + 1 not in flagged:
+                    segs.append((run_start(i, 8) - 45, c0 + 8))
+        last = g1 - 1
+        carry = (blks[last], G[last], run_start(last, 8) if (G[last] >> 7) & 1 else -1)
+    segs.sort()
+    return [(s, s + pos, e - s, equal_bases(t, q, s, pos, e - s)) for s, e in segs]
+
+
+@pytest.mark.parametrize("icap", [4096, 7, 1])
+def test_item_model_matches_oracle_doone(O, icap):
+    rng = np.random.default_rng(79)
+    cases = W.uniform_batch(4, seed=10) + [W.plain_pair(5)]
+    t = W.random_bases(rng, 4096)
+    cases.append((t.tobytes(), t.tobytes()))
+    cases.append((t.tobytes(), W.tandem_repeat(rng, 4096, 2, 3).tobytes()))
+    for t, q in cases:
+        offs = O.findtop(O.xcorr64(t, q, 8192), 1.8)
+        extra = rng.integers(-4095, 4096, size=10)
+        for i in list(offs[:20]) + [int(x) + 4096 for x in extra]:
+            pos = int(i) - 4096
+            got = model_doone_items(t, q, pos, icap)
+            want = O.doone(t, q, pos)
+            assert [g[:3] for g in got] == [tuple(x) for x in want.tolist()], (pos, icap)
