@@ -10,7 +10,7 @@ constexpr int MIN_LOG2L = 10;    // FFT length 1024
 constexpr int MAX_LOG2L = 14;    // FFT length 16384 (shared-memory resident)
 constexpr int NT_CORR = 512;     // threads of the correlation kernel
 constexpr int NT_SCAN = 128;     // threads of the scan kernel
-constexpr int OFF_CHUNK = 1024;  // offsets staged per scan round
+constexpr int OFF_CHUNK = 512;   // offsets staged per scan chunk
 constexpr int WINDOW = 46;       // DoOne window: m_minLen + 1 positions (CrossCorr.cc:701-705)
 constexpr int MIN_HITS = 19;     // ACGT windows pass when 100*hits > 1889 (CrossCorr.cc:675)
 

@@ -10,11 +10,11 @@
 //       items: the marked blocks of the round laid out contiguously per
 //         diagonal by a prefix sum, processed one per thread --
 //         phase A: the block's 8 exact window bits;
-//         phase B: rises and falls against the previous block's last bit,
-//           run starts from the same block or by looking back, segments
-//           queued with one atomic per warp;
-//       drain (thread = segment): equal-base counts, FP32 probability
-//         screen, exact FP64 GetMatchProbability / PrintMatch for survivors.
+//         phase B: falls and closing ends of runs against the previous
+//           block's last bit, queued as (item, bit) with one atomic per warp;
+//       phase C (thread = segment): run start from the same block or by
+//         looking back, equal-base count, FP32 probability screen, exact FP64
+//         GetMatchProbability / PrintMatch for survivors.
 //     Other pairs (N, IUPAC, unknown letters): the reference's byte-table
 //       DoOne per lane and the exact double sums.
 //   finalize kernels     order each strand's results as the reference appends
@@ -38,7 +38,7 @@ template <int LOG2L> struct ScanGeom {
   // each; item indices fit 12 bits).  The queue shares its bytes with the
   // chunk byte arrays, which only the byte-table path fills.
   static constexpr int ICAP = 3072;
-  static constexpr int QCAP = 3072;
+  static constexpr int QCAP = 2048;
   static constexpr size_t region = (size_t)QCAP * 4 > 2 * (size_t)N ? (size_t)QCAP * 4 : 2 * (size_t)N;
   static constexpr size_t bytes = region +
       (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK + FW * NT_SCAN + ICAP + NT_SCAN) * 4 +
@@ -378,20 +378,32 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
       //      unmarked block can pass.
       int nb = 0;
       if (valid) {
+        // The query word pair of target word w is (w + qd, w + qd + 1) at bit
+        // shift sh: one new query word per step.
+        const int qd = (pos + 32 * QPAD) >> 5, sh = (pos + 32 * QPAD) & 31;
+        // blocks holding valid checks in the first and last words
+        const uint32_t bm_first = (0xfu << ((cfirst & 31) >> 3)) & 0xfu;
+        const uint32_t bm_last = 0xfu >> (3 - ((clast & 31) >> 3));
         uint32_t e2 = eword(pos, wfirst - 2), e1 = eword(pos, wfirst - 1);
+        int qi = wfirst + qd;
+        uint32_t a0 = qb0[qi], a1 = qb1[qi];
         uint32_t acc = 0;
         for (int w = wfirst; w <= wlast; w++) {
-          const uint32_t e0 = eword(pos, w);
+          const uint32_t n0 = qb0[qi + 1], n1 = qb1[qi + 1];
+          const uint32_t e0 = ~((tb0[w] ^ __funnelshift_r(a0, n0, sh)) | (tb1[w] ^ __funnelshift_r(a1, n1, sh)));
+          a0 = n0;
+          a1 = n1;
+          qi++;
           const uint64_t U = ((uint64_t)e1 << 32) | e2;
-          const int lo = max(cfirst - 32 * w, 0), hi = min(clast - 32 * w, 31);
-          const uint32_t vm = (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
           uint32_t f = 0;
 #pragma unroll
           for (int sb = 0; sb < 4; sb++) {
             const int a = 8 * sb + 19;
             const int c53 = __popcll(U >> a) + __popc(e0 & lowmask(a - 11));
-            f |= (uint32_t)((c53 >= MIN_HITS) && ((vm >> (8 * sb)) & 0xffu)) << sb;
+            f |= (uint32_t)(c53 >= MIN_HITS) << sb;
           }
+          if (w == wfirst) f &= bm_first;
+          if (w == wlast) f &= bm_last;
           const int q = w - wfirst;
           acc |= f << (4 * (q & 7));
           if ((q & 7) == 7 || w == wlast) {
@@ -639,8 +651,11 @@ __global__ void __launch_bounds__(256) gather_sort_kernel(const int* __restrict_
 // ---------------------------------------------------------------------------
 template <int LOG2L>
 static cudaError_t set_scan_attrs() {
-  return cudaFuncSetAttribute(scan_kernel<LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)scan_smem_bytes(LOG2L));
+  cudaError_t e = cudaFuncSetAttribute(scan_kernel<LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)scan_smem_bytes(LOG2L));
+  if (e != cudaSuccess) return e;
+  // several CTAs per SM: ask for the largest shared-memory carveout
+  return cudaFuncSetAttribute(scan_kernel<LOG2L>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 
 cudaError_t prepare_scan_kernels() {
