@@ -32,7 +32,7 @@ assert RESULT_DTYPE.itemsize == 72
 EXPORTS = ("xc_create", "xc_destroy", "xc_align_pairs", "xc_batch_upload", "xc_batch_run",
            "xc_batch_results", "xc_batch_free", "xc_batch_launches", "xc_batch_run_timed",
            "xc_transfer_stats", "xc_submit", "xc_wait", "xc_serving_stats", "xc_debug_pair",
-           "xc_version", "xc_device_name")
+           "xc_version", "xc_device_name", "xc_align_pair_noalloc")
 
 
 class XCError(RuntimeError):
@@ -74,6 +74,7 @@ def load(path=LIB_PATH):
     lib.xc_create.argtypes = [ctypes.POINTER(Params), i, ctypes.POINTER(vp)]
     lib.xc_destroy.argtypes = [vp]
     lib.xc_align_pairs.argtypes = [vp, vp, sz, vp, sz, ctypes.POINTER(sz), vp]
+    lib.xc_align_pair_noalloc.argtypes = [vp, vp, vp, sz, ctypes.POINTER(sz)]
     lib.xc_batch_upload.argtypes = [vp, vp, sz, ctypes.POINTER(vp)]
     lib.xc_batch_run.argtypes = [vp, vp, vp]
     lib.xc_batch_results.argtypes = [vp, vp, vp, sz, ctypes.POINTER(sz), vp]

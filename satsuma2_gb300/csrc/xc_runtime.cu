@@ -353,7 +353,7 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
 // cancellation, so its exact test accepts up to that much beyond the true CDF.
 // The kernel rejects only above z* + 0.02, orders of magnitude beyond the
 // FP32 error of its z; survivors take the exact FP64 test.
-static float screen_z(double min_prob, double target_total) {
+float screen_z(double min_prob, double target_total) {
   if (!(min_prob > 0) || !(target_total > 0)) return INFINITY;
   const double bound = -log(min_prob);
   if (!(bound >= 0)) return -INFINITY;   // min_prob > 1: nothing passes the exact test either

@@ -100,6 +100,8 @@ int batch_run(Ctx* c, Batch* b, cudaStream_t s, bool use_graph, bool timed = fal
 int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, size_t* n_out,
                   size_t* pair_counts);
 int batch_launch_count(const Batch* b);
+// z-score threshold of the scan kernel's FP32 probability screen.
+float screen_z(double min_prob, double target_total);
 int ctx_run_pairs(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, xc_result* out, size_t cap,
                   size_t* n_out, size_t* pair_counts);
 void server_stop(Ctx* c);
