@@ -576,6 +576,64 @@ int ctx_run_pairs(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, xc_result* o
   return XC_ERR_CAPACITY;
 }
 
+// xc_align_pairs: the pairs run as sub-batches alternating between two
+// batches and two streams, so the host packing and the host-to-device copy of
+// one sub-batch overlap the kernels of the one before; results are collected
+// in order.  Sub-batches hold at least 1024 pairs (a launch fills the GPU) and
+// a big call is cut in about four.
+int ctx_align_pipelined(Ctx* c, const xc_pair* pairs, size_t n, xc_result* out, size_t cap, size_t* n_out,
+                        size_t* pair_counts) {
+  const size_t maxb = c->prm.max_batch > 0 ? (size_t)c->prm.max_batch : 4096;
+  const size_t sub = n <= 1024 ? n : std::min(maxb, std::max<size_t>(1024, (n + 3) / 4));
+  const size_t nchunks = (n + sub - 1) / sub;
+  size_t written = 0, need = 0;
+  uint64_t h2d = 0, d2h = 0;
+  bool full = false;   // output capacity exceeded: later sub-batches are only counted
+  auto start = [&](size_t k) -> int {
+    const size_t lo = k * sub, m = std::min(sub, n - lo);
+    Batch* b = c->work[k & 1];
+    const cudaStream_t s = c->work_stream[k & 1];
+    int r = batch_pack(c, b, pairs + lo, m, s);
+    if (r == XC_OK) r = batch_run(c, b, s, false);
+    return r;
+  };
+  auto finish = [&](size_t k) -> int {
+    const size_t lo = k * sub, m = std::min(sub, n - lo);
+    Batch* b = c->work[k & 1];
+    xc_result* o = (full || !out) ? nullptr : out + written;
+    const size_t cp = full ? 0 : (cap >= written ? cap - written : 0);
+    size_t got = 0;
+    int r = batch_collect(c, b, c->work_stream[k & 1], o, cp, &got, pair_counts ? pair_counts + lo : nullptr);
+    if (r == XC_ERR_CAPACITY && b->h_misc[1] != 0)   // device overflow pool too small: run it again alone
+      r = ctx_run_pairs(c, b, pairs + lo, m, o, cp, &got, pair_counts ? pair_counts + lo : nullptr);
+    need += got;
+    h2d += c->last_h2d;
+    d2h += c->last_d2h;
+    if (r == XC_ERR_CAPACITY) {
+      full = true;
+      return XC_OK;
+    }
+    if (r != XC_OK) return r;
+    written += got;
+    return XC_OK;
+  };
+  int r = XC_OK;
+  size_t k = 0, done = 0;
+  for (; k < nchunks && r == XC_OK; k++) {
+    if (k >= 2) r = finish(done++);
+    if (r == XC_OK) r = start(k);
+  }
+  while (r == XC_OK && done < k) r = finish(done++);
+  if (r != XC_OK) {
+    for (int i = 0; i < 2; i++) cudaStreamSynchronize(c->work_stream[i]);
+    return r;
+  }
+  c->last_h2d = h2d;
+  c->last_d2h = d2h;
+  if (n_out) *n_out = need;
+  return full ? XC_ERR_CAPACITY : XC_OK;
+}
+
 Batch* new_batch(Ctx* c) {
   Batch* b = new Batch();
   b->slots = c->prm.result_slots > 0 ? c->prm.result_slots : 64;
@@ -619,7 +677,10 @@ int xc_create(const xc_params* params, int device, xc_ctx** out) {
   if (r == XC_OK) {
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) snprintf(c->devname, sizeof(c->devname), "%s", prop.name);
-    c->work = new_batch(c);
+    for (int i = 0; i < 2 && r == XC_OK; i++) {
+      c->work[i] = new_batch(c);
+      r = cuda_err(cudaStreamCreateWithFlags(&c->work_stream[i], cudaStreamNonBlocking), "stream");
+    }
   }
   if (r != XC_OK) {
     xc_destroy(c);
@@ -634,7 +695,11 @@ int xc_destroy(xc_ctx* c) {
   server_stop(c);
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  delete c->work;
+  for (int i = 0; i < 2; i++) {
+    if (c->work_stream[i]) cudaStreamSynchronize(c->work_stream[i]);
+    delete c->work[i];
+    if (c->work_stream[i]) cudaStreamDestroy(c->work_stream[i]);
+  }
   for (auto& t : c->tab) {
     cudaFree(t.tw); cudaFree(t.ent);
   }
@@ -651,32 +716,7 @@ int xc_align_pairs(xc_ctx* c, const xc_pair* pairs, size_t n, xc_result* out, si
   if (n == 0) return XC_OK;
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
-  const size_t maxb = c->prm.max_batch > 0 ? (size_t)c->prm.max_batch : 4096;
-  size_t done = 0, written = 0;
-  while (done < n) {
-    const size_t m = std::min(maxb, n - done);
-    size_t got = 0;
-    int r = ctx_run_pairs(c, c->work, pairs + done, m, out ? out + written : nullptr,
-                          cap >= written ? cap - written : 0, &got, pair_counts ? pair_counts + done : nullptr);
-    if (r == XC_ERR_CAPACITY) {
-      // report the total needed: finish counting the remaining chunks
-      size_t need = written + got;
-      for (size_t d2 = done + m; d2 < n; d2 += maxb) {
-        const size_t m2 = std::min(maxb, n - d2);
-        size_t g2 = 0;
-        int r2 = ctx_run_pairs(c, c->work, pairs + d2, m2, nullptr, 0, &g2, nullptr);
-        if (r2 != XC_OK && r2 != XC_ERR_CAPACITY) return r2;
-        need += g2;
-      }
-      if (n_out) *n_out = need;
-      return XC_ERR_CAPACITY;
-    }
-    if (r != XC_OK) return r;
-    written += got;
-    done += m;
-  }
-  if (n_out) *n_out = written;
-  return XC_OK;
+  return ctx_align_pipelined(c, pairs, n, out, cap, n_out, pair_counts);
 }
 
 int xc_batch_upload(xc_ctx* c, const xc_pair* pairs, size_t n, xc_batch** out) {

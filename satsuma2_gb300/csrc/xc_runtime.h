@@ -85,7 +85,8 @@ struct Ctx {
   double* d_gcw = nullptr;
   double* d_ptable = nullptr;
   std::vector<double> h_ptable;
-  Batch* work = nullptr;       // reusable batch of xc_align_pairs
+  Batch* work[2] = {nullptr, nullptr};       // xc_align_pairs: two sub-batches in flight
+  cudaStream_t work_stream[2] = {nullptr, nullptr};
   Server* server = nullptr;
   char devname[256] = {0};
   uint64_t last_h2d = 0, last_d2h = 0;
@@ -104,6 +105,8 @@ int batch_launch_count(const Batch* b);
 float screen_z(double min_prob, double target_total);
 int ctx_run_pairs(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, xc_result* out, size_t cap,
                   size_t* n_out, size_t* pair_counts);
+int ctx_align_pipelined(Ctx* c, const xc_pair* pairs, size_t n, xc_result* out, size_t cap, size_t* n_out,
+                        size_t* pair_counts);
 void server_stop(Ctx* c);
 
 }  // namespace xc
