@@ -31,7 +31,7 @@ extern "C" {
 #define XC_ERR_CAPACITY (-4)     /* output buffer too small; *n_out holds the size needed */
 #define XC_ERR_INPUT (-5)        /* a byte >= 128, or a chunk longer than half the FFT length */
 #define XC_ERR_TIMEOUT (-6)      /* xc_wait timed out; the ticket stays valid */
-#define XC_ERR_UNSUPPORTED (-7)  /* FFT length outside 1024..16384 */
+#define XC_ERR_UNSUPPORTED (-7)  /* FFT length outside 1024..32768 */
 #define XC_ERR_BUSY (-8)         /* admission refused: request queue or memory budget full */
 
 /* Result record.  Same fields, order and 72-byte LP64 layout as t_result
@@ -145,7 +145,8 @@ int xc_serving_stats(xc_ctx* ctx, double* p50_ms, double* p99_ms, uint64_t* comp
  * sig[((s*2+k)*4+c)*L + i], i < L/2), the correlation xc[s*L + i], FindTop
  * offsets offs[s*L + j] with n_offs[s], and raw DoOne segments (tStart,
  * qStart, len) at segs[(s*seg_cap + j)*3] with n_segs[s].  Any output may be
- * NULL.  *fft_len_out gets the FFT length used. */
+ * NULL.  *fft_len_out gets the FFT length L used; size sig for 16*L floats,
+ * xc for 2*L and offs for 2*L ints (L <= 32768). */
 int xc_debug_pair(xc_ctx* ctx, const xc_pair* pair, float* sig, float* xc, int* offs,
                   int* n_offs, int* segs, int* n_segs, int seg_cap, int* fft_len_out);
 

@@ -566,8 +566,15 @@ int orc_align_pair(const orc_params* P, const orc_pair* pr, const float* xc_in,
     for (int i = 0; i < nt; i++) {
       int pos = top[i] - L / 2;
       int room = scap - ns;
-      int c = orc_doone(pr->tseq, pr->tlen, q, pr->qlen, pos, sg + 3 * ns, room > 0 ? room : 0);
-      ns += c < room ? c : room;
+      int c = orc_doone(pr->tseq, pr->tlen, q, pr->qlen, pos, sg + 3 * ns, room);
+      if (c > room) {   /* low-complexity chunks: grow the segment buffer and redo */
+        while (scap - ns < c) scap *= 2;
+        int* g = (int*)realloc(sg, sizeof(int) * 3 * (size_t)scap);
+        if (!g) break;
+        sg = g;
+        c = orc_doone(pr->tseq, pr->tlen, q, pr->qlen, pos, sg + 3 * ns, scap - ns);
+      }
+      ns += c;
     }
     if (segs && n_segs) {
       n_segs[strand] = ns;

@@ -18,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libsatsuma2_gb300.so")
 
 XC_OK = 0
+MAX_FFT_LEN = 32768   # longest FFT the library runs (XC_ERR_UNSUPPORTED beyond)
 ERRORS = {-1: "XC_ERR_ARG", -2: "XC_ERR_CUDA", -3: "XC_ERR_NOMEM", -4: "XC_ERR_CAPACITY",
           -5: "XC_ERR_INPUT", -6: "XC_ERR_TIMEOUT", -7: "XC_ERR_UNSUPPORTED", -8: "XC_ERR_BUSY"}
 
@@ -175,7 +176,7 @@ class XCorr:
     def debug_pair(self, t, q, seg_cap=1 << 16, **kw):
         """Stage outputs of one pair: signals, xc, offsets, raw segments per strand."""
         arr, keep = make_pairs([dict(t=t, q=q, **kw)])
-        Lmax = 1 << 14
+        Lmax = MAX_FFT_LEN
         sig = np.zeros(2 * 8 * Lmax, np.float32)
         xcv = np.zeros(2 * Lmax, np.float32)
         offs = np.zeros(2 * Lmax, np.int32)

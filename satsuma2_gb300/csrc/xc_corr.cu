@@ -10,8 +10,11 @@
 //   4. inverse: half-length complex transform of the Hermitian channel sum
 //   5. FindTop: envelope per 256 samples, threshold, ordered compaction
 // Everything stays in shared memory; HBM sees the chunk bytes in and the
-// offset list out.  Reference semantics cited per step; paths are relative to
-// the satsuma2 source tree.
+// offset list out.  At L = 32768 the two transforms and the channel sums no
+// longer fit one SM: the even and odd transforms then run in turn on all 512
+// threads in one buffer, and the channel sums go to a per-strand scratch in
+// global memory (128 KB, L2-resident while the CTA runs).  Reference
+// semantics cited per step; paths are relative to the satsuma2 source tree.
 #include "xc_device.cuh"
 
 namespace xc {
@@ -19,7 +22,8 @@ namespace xc {
 size_t corr_smem_bytes(int log2L) {
   const size_t N = (size_t)1 << (log2L - 1);
   const size_t NH = N / 64;
-  return (2 * N + (N / 2 + 8) + N / 2 + 2 * (NH + 64)) * sizeof(float2)   // transforms, sums, twiddles
+  const size_t bufs = log2L > MAX_SMEM_LOG2L ? N : 2 * N + (N / 2 + 8) + N / 2;   // transforms (+ sums)
+  return (bufs + 2 * (NH + 64)) * sizeof(float2)                         // and twiddles
          + 2 * N                                                         // target and query bytes
          + 2 * 256 * sizeof(float)                                       // entropy weight per window
          + 2 * 256 * sizeof(float2);                                     // per-window channel values
@@ -33,13 +37,14 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
   constexpr int WIN = L / 512;   // CCSignal::ComputeEntropy window (CrossCorr.cc:46)
   constexpr int NWIN = 256;      // N / WIN
   constexpr int NH = N / 64;
+  constexpr bool SEQ = LOG2L > MAX_SMEM_LOG2L;   // one transform buffer, channel sums in global memory
 
   extern __shared__ __align__(16) unsigned char smem[];
   float2* bufE = reinterpret_cast<float2*>(smem);
-  float2* bufO = bufE + N;
+  float2* bufO = bufE + N;              // (not SEQ)
   float2* accE = bufO + N;              // channel sum at bins 2m, m = 0..N/2 (N/2: Nyquist, real)
   float2* accO = accE + (N / 2 + 8);    // bins 2m+1, m < N/2; 8 slots off accE's banks
-  float2* twNh = accO + N / 2;          // W_N^(64a)
+  float2* twNh = SEQ ? bufE + N : accO + N / 2;   // W_N^(64a)
   float2* twNl = twNh + NH;             // W_N^b, b < 64
   float2* twLh = twNl + 64;             // W_L^(64a)
   float2* twLl = twLh + NH;             // W_L^b
@@ -104,7 +109,14 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
     return;
   }
   if (tid == 0 && strand == 0) P.pair_flags[pidx] = (D.flags & PF_FAST) | (generic ? PF_GENERIC : 0u);
-  for (int i = tid; i < N + 8; i += NT_CORR) accE[i] = make_float2(0.f, 0.f);   // accE and accO
+  if constexpr (!SEQ)
+    for (int i = tid; i < N + 8; i += NT_CORR) accE[i] = make_float2(0.f, 0.f);   // accE and accO
+  float2* gaccE = nullptr;   // SEQ: this strand's channel sums in global memory
+  float2* gaccO = nullptr;
+  if constexpr (SEQ) {
+    gaccE = P.acc + (size_t)(blockIdx.x * 2 + strand) * acc_stride(LOG2L);
+    gaccO = gaccE + (N / 2 + 8);
+  }
 
   // ---- 2a. entropy weight per window (CCSignal::ComputeEntropy, CrossCorr.cc:35-93).
   //      Threads 0..255: target windows, 256..511: query windows.  Windows
@@ -205,6 +217,60 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
     }
     __syncthreads();
 
+    if constexpr (SEQ) {
+      // ---- 3 (L = 32768): the even-bin transform of z, then the odd-bin
+      //      transform of z*W_L^n, each on all threads in one buffer; the
+      //      per-bin products go to the global channel sums (set on channel
+      //      0, added after). ----
+      const double offt = s_off[c], offq = s_off[4 + c];
+      const int stid = swz(tid);
+      for (int g = 0; g < 2; g++) {
+#pragma unroll 4
+        for (int it = 0; it < N / NT_CORR; it++) {
+          const int n = tid + NT_CORR * it;
+          float x = 0.f, y = 0.f;
+          const int w = n / WIN;
+          if (!generic) {
+            if (n < T) { const float2 v = vt[w]; x = code_of(st[n]) == (uint32_t)c ? v.y : v.x; }
+            if (n < Q) { const float2 v = vq[w]; y = code_of(sq[n]) == (uint32_t)c ? v.y : v.x; }
+          } else {
+            if (n < T) x = __double2float_rn(__dmul_rn((double)Et[w], __dsub_rn(c_wd[c][st[n]], offt)));
+            if (n < Q) y = __double2float_rn(__dmul_rn((double)Eq[w], __dsub_rn(c_wd[c][sq[n]], offq)));
+          }
+          if (P.dbg_sig && g == 0) {
+            float* ds = P.dbg_sig + (size_t)(pidx * 2 + strand) * 8 * L;
+            ds[(size_t)c * L + n] = x;
+            ds[(size_t)(4 + c) * L + n] = y;
+          }
+          const float2 z = make_float2(x, y);
+          bufE[stid ^ swz(NT_CORR * it)] = g ? cmul(z, tw2(twLh, twLl, n)) : z;
+        }
+        __syncthreads();
+        fft_forward<LOG2N>(bufE, twNh, twNl, tid, NT_CORR);
+        if (g == 0) {
+          for (int m = tid; m <= N / 2; m += NT_CORR) {
+            const float2 A = bufE[lp<LOG2N>(m)];
+            const float2 B = bufE[lp<LOG2N>((N - m) & (N - 1))];
+            const float2 X = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
+            const float2 Y = make_float2(0.5f * (A.y + B.y), -0.5f * (A.x - B.x));
+            const float2 v = m == N / 2 ? make_float2(X.x, 0.f) : cmulc(Y, X);
+            gaccE[m] = c ? cadd(gaccE[m], v) : v;
+          }
+        } else {
+          for (int m = tid; m < N / 2; m += NT_CORR) {
+            const float2 A = bufE[lp<LOG2N>(m)];
+            const float2 B = bufE[lp<LOG2N>(N - 1 - m)];
+            const float2 X = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
+            const float2 Y = make_float2(0.5f * (A.y + B.y), -0.5f * (A.x - B.x));
+            const float2 v = m == N / 2 - 1 ? X : cmulc(Y, X);
+            gaccO[m] = c ? cadd(gaccO[m], v) : v;
+          }
+        }
+        __syncthreads();
+      }
+      continue;
+    }
+
     // ---- 3. z[n] = target_c[n] + i*query_c[n] to the even buffer and
     //      z[n]*W_L^n to the odd buffer.  Both signals are zero past N, so the
     //      even bins of the L-point transform are the N-point transform of z
@@ -283,7 +349,10 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
   // ---- 4. inverse: half-length complex transform of the Hermitian sum S.
   //      Z(k) = E(k) + i O(k), E = (S(k) + conj S(N-k))/2,
   //      O = (S(k) - conj S(N-k)) conj(W_L^k)/2; z[m] = r[2m] + i r[2m+1]. ----
-  auto S = [&](int k) -> float2 { return (k & 1) ? accO[k >> 1] : accE[k >> 1]; };
+  auto S = [&](int k) -> float2 {
+    if constexpr (SEQ) return (k & 1) ? gaccO[k >> 1] : gaccE[k >> 1];
+    return (k & 1) ? accO[k >> 1] : accE[k >> 1];
+  };
   {
     const int la = lp<LOG2N>(tid);
     const int lb = lp<LOG2N>((NT_CORR - tid) & (NT_CORR - 1));
@@ -310,7 +379,8 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
     }
   }
   __syncthreads();
-  fft_inverse<LOG2N>(bufE, twNh, twNl, tid < 256 ? tid : (1 << 30), 256);
+  if constexpr (SEQ) fft_inverse<LOG2N>(bufE, twNh, twNl, tid, NT_CORR);
+  else fft_inverse<LOG2N>(bufE, twNh, twNl, tid < 256 ? tid : (1 << 30), 256);
 
   // ---- 5. FindTop (SeqAnalyzer::FindTop, CrossCorr.cc:878-944): xc[i] =
   //      r[(i + N) mod L] / N; envelope over 256-sample blocks when L/256 > 8;
@@ -415,6 +485,7 @@ cudaError_t prepare_kernels() {
   if ((e = set_corr_attrs<12>()) != cudaSuccess) return e;
   if ((e = set_corr_attrs<13>()) != cudaSuccess) return e;
   if ((e = set_corr_attrs<14>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<15>()) != cudaSuccess) return e;
   return prepare_scan_kernels();
 }
 
@@ -428,6 +499,7 @@ cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t
     case 12: corr_kernel<12><<<grid, NT_CORR, sm, s>>>(p); break;
     case 13: corr_kernel<13><<<grid, NT_CORR, sm, s>>>(p); break;
     case 14: corr_kernel<14><<<grid, NT_CORR, sm, s>>>(p); break;
+    case 15: corr_kernel<15><<<grid, NT_CORR, sm, s>>>(p); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

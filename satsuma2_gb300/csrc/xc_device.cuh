@@ -69,7 +69,7 @@ __device__ __forceinline__ float2 tw2(const float2* hi, const float2* lo, int m)
 }
 
 // Radix plans (log2 of each pass's radix), shared by the transforms and the
-// digit-reversed position of a bin.  Must match radix_plan() in the runtime.
+// digit-reversed position of a bin (tests/test_smem_layout.py models them).
 template <int LOG2N> struct Plan;
 template <int A, int B, int C, int D>
 struct PlanR {
@@ -81,6 +81,7 @@ template <> struct Plan<10> : PlanR<4, 4, 2, 0> {};
 template <> struct Plan<11> : PlanR<4, 4, 3, 0> {};
 template <> struct Plan<12> : PlanR<4, 4, 4, 0> {};
 template <> struct Plan<13> : PlanR<4, 4, 4, 1> {};
+template <> struct Plan<14> : PlanR<4, 4, 4, 2> {};
 
 // Position of bin k after the forward (decimation-in-frequency) passes: the
 // digit of radix R_s (least significant first in k) moves to place value

@@ -7,7 +7,8 @@
 namespace xc {
 
 constexpr int MIN_LOG2L = 10;    // FFT length 1024
-constexpr int MAX_LOG2L = 14;    // FFT length 16384 (shared-memory resident)
+constexpr int MAX_LOG2L = 15;    // FFT length 32768
+constexpr int MAX_SMEM_LOG2L = 14;  // longest FFT whose two transforms and channel sums fit one SM
 constexpr int NT_CORR = 512;     // threads of the correlation kernel
 constexpr int NT_SCAN = 128;     // threads of the scan kernel
 constexpr int OFF_CHUNK = 512;   // offsets staged per scan chunk
@@ -71,7 +72,14 @@ struct CorrParams {
   uint32_t* pair_flags;     // [pair]
   float* dbg_sig;           // optional: [pair*2+strand][2][4][L]
   float* dbg_xc;            // optional: [pair*2+strand][L]
+  float2* acc;              // L > 2^MAX_SMEM_LOG2L: channel sums, [pair*2+strand][acc_stride(log2L)]
 };
+
+// Global channel-sum scratch of one pair strand for FFT lengths beyond one
+// SM's shared memory: even bins 0..N/2, then odd bins 0..N/2-1 (8 apart).
+__host__ __device__ constexpr size_t acc_stride(int log2L) {
+  return log2L > MAX_SMEM_LOG2L ? ((size_t)1 << (log2L - 1)) + 16 : 0;
+}
 
 struct ScanParams {
   const PairDesc* pairs;

@@ -31,7 +31,8 @@ namespace xc {
 
 namespace {
 
-constexpr int NA_MAX_L = 1 << MAX_LOG2L;   // largest FFT length: 16384
+constexpr int NA_MAX_LOG2L = 14;          // largest FFT length: 16384
+constexpr int NA_MAX_L = 1 << NA_MAX_LOG2L;
 constexpr int NA_SLOTS = 1024;              // kept matches per strand
 constexpr int NA_MAX_DEVICES = 64;
 
@@ -94,9 +95,9 @@ int cuda_fail(cudaError_t e, const char* what) {
 int align_pair_noalloc(Ctx* c, const xc_pair& p, xc_result* out, size_t cap, size_t* n_out) {
   if (p.tlen < 0 || p.qlen < 0 || (p.tlen && !p.tseq) || (p.qlen && !p.qseq)) return XC_ERR_ARG;
   const int lg = pair_log2L(c->prm, p);
-  if (lg < MIN_LOG2L || lg > MAX_LOG2L) {
+  if (lg < MIN_LOG2L || lg > NA_MAX_LOG2L) {
     fprintf(stderr, "satsuma2_gb300: xc_align_pair_noalloc: FFT length 2^%d outside 2^%d..2^%d\n", lg,
-            MIN_LOG2L, MAX_LOG2L);
+            MIN_LOG2L, NA_MAX_LOG2L);
     return XC_ERR_UNSUPPORTED;
   }
   if (p.tlen > (1 << lg) / 2 || p.qlen > (1 << lg) / 2) return XC_ERR_INPUT;

@@ -250,7 +250,7 @@ Batch::~Batch() {
     if (e) cudaEventDestroy(e);
   cudaFree(d_pool); cudaFree(d_desc); cudaFree(d_off); cudaFree(d_offcnt); cudaFree(d_flags);
   cudaFree(d_res); cudaFree(d_rescnt); cudaFree(d_ovf); cudaFree(d_misc); cudaFree(d_base);
-  cudaFree(d_dense); cudaFree(d_dbg); cudaFree(d_dbg_sig); cudaFree(d_dbg_xc);
+  cudaFree(d_dense); cudaFree(d_dbg); cudaFree(d_dbg_sig); cudaFree(d_dbg_xc); cudaFree(d_acc);
   cudaFreeHost(h_pool); cudaFreeHost(h_desc); cudaFreeHost(h_base); cudaFreeHost(h_dense);
   cudaFreeHost(h_misc); cudaFreeHost(h_ovf);
 }
@@ -322,6 +322,9 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   if ((r = dev_grow(b->d_misc, b->cap_misc, 4)) != XC_OK) return r;
   if ((r = dev_grow(b->d_base, b->cap_base, nslots + 1)) != XC_OK) return r;
   if ((r = dev_grow(b->d_dense, b->cap_dense, nslots * slots)) != XC_OK) return r;
+  size_t acc = 0;
+  for (int lg = MAX_SMEM_LOG2L + 1; lg <= MAX_LOG2L; lg++) acc = std::max(acc, (size_t)counts[lg] * 2 * acc_stride(lg));
+  if (acc && (r = dev_grow(b->d_acc, b->cap_acc, acc)) != XC_OK) return r;
   if ((r = host_grow(b->h_base, b->cap_h_base, nslots + 1)) != XC_OK) return r;
   if ((r = host_grow(b->h_misc, b->cap_h_misc, 4)) != XC_OK) return r;
   b->pool_bytes = pool;
@@ -392,6 +395,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     cp.pair_flags = b->d_flags;
     cp.dbg_sig = b->d_dbg_sig;
     cp.dbg_xc = b->d_dbg_xc;
+    cp.acc = b->d_acc;
     XC_CHECK(launch_corr(bk.log2L, cp, bk.count, s));
   }
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[1], s, cudaEventRecordExternal));

@@ -43,6 +43,7 @@ struct Batch {
   int* d_misc = nullptr;          size_t cap_misc = 0;   // [0] ovf count [1] err [2] dbg count
   int* d_base = nullptr;          size_t cap_base = 0;
   DevResult* d_dense = nullptr;   size_t cap_dense = 0;
+  float2* d_acc = nullptr;        size_t cap_acc = 0;     // channel sums of FFT lengths beyond one SM
   DbgSeg* d_dbg = nullptr;
   float* d_dbg_sig = nullptr;
   float* d_dbg_xc = nullptr;

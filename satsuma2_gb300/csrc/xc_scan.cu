@@ -52,6 +52,7 @@ size_t scan_smem_bytes(int log2L) {
     case 12: return ScanGeom<12>::bytes;
     case 13: return ScanGeom<13>::bytes;
     case 14: return ScanGeom<14>::bytes;
+    case 15: return ScanGeom<15>::bytes;
   }
   return 0;
 }
@@ -664,7 +665,8 @@ cudaError_t prepare_scan_kernels() {
   if ((e = set_scan_attrs<11>()) != cudaSuccess) return e;
   if ((e = set_scan_attrs<12>()) != cudaSuccess) return e;
   if ((e = set_scan_attrs<13>()) != cudaSuccess) return e;
-  return set_scan_attrs<14>();
+  if ((e = set_scan_attrs<14>()) != cudaSuccess) return e;
+  return set_scan_attrs<15>();
 }
 
 cudaError_t launch_scan(int log2L, const ScanParams& p, int npairs, cudaStream_t s) {
@@ -677,6 +679,7 @@ cudaError_t launch_scan(int log2L, const ScanParams& p, int npairs, cudaStream_t
     case 12: scan_kernel<12><<<grid, NT_SCAN, sm, s>>>(p); break;
     case 13: scan_kernel<13><<<grid, NT_SCAN, sm, s>>>(p); break;
     case 14: scan_kernel<14><<<grid, NT_SCAN, sm, s>>>(p); break;
+    case 15: scan_kernel<15><<<grid, NT_SCAN, sm, s>>>(p); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

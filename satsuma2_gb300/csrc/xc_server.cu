@@ -76,7 +76,8 @@ struct Server {
 static size_t pair_footprint(const Ctx* c, const xc_pair& p, int slots) {
   const int lg = pair_log2L(c->prm, p);
   const size_t L = lg > 0 ? (size_t)1 << lg : 8192;
-  return (size_t)p.tlen + p.qlen + 32 + 2 * L * sizeof(int) + 2 * (size_t)slots * 2 * sizeof(DevResult) + 64;
+  return (size_t)p.tlen + p.qlen + 32 + 2 * L * sizeof(int) + 2 * (size_t)slots * 2 * sizeof(DevResult) + 64 +
+         2 * acc_stride(lg > 0 ? lg : 13) * sizeof(float2);
 }
 
 static void complete_slot(Server* S, Slot& sl) {

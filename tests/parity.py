@@ -16,6 +16,10 @@ import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 STRADDLE_REL = 2e-5      # band = STRADDLE_REL * max|xc| (FP32 errors measured ~2e-7)
+# At FFT 32768 FFTReal switches to its float rotation oscillator for the passes
+# beyond 12 (FFTReal.h:78): the reference's own FP32 error grows to ~1.5e-4 of
+# the peak (~0.08 absolute near the FindTop threshold), so the band widens there.
+STRADDLE_REL_OSC = 3e-4
 PROB_RTOL = 1e-12
 
 
@@ -63,7 +67,8 @@ def straddles(O, case, strand_q, strand):
     xc64 = O.xcorr64(case["t"], strand_q, case["L"])
     cutoff = case["cutoff"]
     thr = O.thresholds(xc64, cutoff)
-    band = STRADDLE_REL * max(1.0, float(np.abs(xc64).max()))
+    rel = STRADDLE_REL_OSC if case["L"] > 16384 else STRADDLE_REL
+    band = rel * max(1.0, float(np.abs(xc64).max()))
     return set(np.nonzero(np.abs(xc64 - thr) <= band)[0].tolist()), xc64
 
 

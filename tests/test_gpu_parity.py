@@ -45,7 +45,7 @@ def pair_item(case):
                 q_chunk_start=case["q_chunk_start"], query_id=case["query_id"], query_size=case["query_size"])
 
 
-SUPPORTED = [c for c in CASES if c["L"] <= 16384]
+SUPPORTED = CASES
 
 
 def sha1(a):
@@ -102,12 +102,40 @@ def test_results_match_reference(O, case):
     assert parity.same_results(res, want, target_total=case["target_total"])
 
 
-def test_large_fft_unsupported():
+def test_fft_beyond_32768_unsupported():
     import satsuma2_gb300 as sg
-    case = [c for c in CASES if c["L"] == 32768][0]
+    x = sg.XCorr(fft_len=65536, target_total=4096.0)
     with pytest.raises(sg.XCError) as e:
-        ctx_for(case).align([pair_item(case)])
+        x.align([W.plain_pair(3)])
     assert e.value.code == -7
+    x.close()
+
+
+def test_fft32768_batch_vs_oracle(O):
+    """Config-4-shaped pairs (16384 bp, microsatellites, skewed GC) at FFT
+    32768, several in one launch: records equal the oracle's over the GPU's
+    own offsets, and the offsets equal the FP64 oracle's except straddles."""
+    import satsuma2_gb300 as sg
+    items = W.large_batch(6, seed=11)
+    TT = 16384.0 * 6
+    x = sg.XCorr(fft_len=32768, t_chunk=16384, q_chunk=16384, target_total=TT)
+    res, counts = x.align(items, with_counts=True)
+    P = O.params(target_total=TT, fft_len=32768, q_chunk=16384)
+    o = 0
+    for k, (t, q) in enumerate(items):
+        got = res[o:o + int(counts[k])]
+        o += int(counts[k])
+        d = x.debug_pair(t=t, q=q)
+        case = dict(t=t, L=32768, cutoff=1.8)
+        for s, qq in enumerate((q, O.rc(q))):
+            band, xc64 = parity.straddles(O, case, qq, s)
+            err = float(np.abs(d["xc"][s].astype(np.float64) - xc64).max()) / max(1.0, float(np.abs(xc64).max()))
+            assert err <= XC_TOL, err
+            thr = O.thresholds(xc64, 1.8)
+            parity.compare_offsets(d["offsets"][s], np.nonzero(xc64 > thr)[0], band)
+        want, _ = O.align_pair(P, O.pair(t, q), offsets_in=d["offsets"])
+        assert parity.same_results(got, want, target_total=TT)
+    x.close()
 
 
 def test_rejects_non_ascii():
