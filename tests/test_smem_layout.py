@@ -12,7 +12,7 @@ xc_corr.cu): the in-place mixed-radix passes, the digit-reversed bin position
 import numpy as np
 import pytest
 
-PLANS = {9: (3, 3, 3), 10: (4, 4, 2), 11: (4, 4, 3), 12: (4, 4, 4), 13: (4, 4, 4, 1)}
+PLANS = {9: (3, 3, 3), 10: (4, 4, 2), 11: (4, 4, 3), 12: (4, 4, 4), 13: (4, 4, 4, 1), 14: (4, 4, 4, 2)}
 
 
 def swz(p):
