@@ -397,11 +397,11 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
   };
   float thrb[PER_WARP >= 256 ? PER_WARP / 256 : 1];
   if constexpr (L / 256 > 8) {
-    const double cut = (D.flags & PF_FAST) ? P.cutoff_fast : P.cutoff;
+    const float cut = (float)((D.flags & PF_FAST) ? P.cutoff_fast : P.cutoff);
 #pragma unroll
     for (int bb = 0; bb < PER_WARP / 256; bb++) {
       // squares are float products as in the reference; compensated FP32
-      // sum per lane, combined in FP64 across the warp
+      // sum per lane, pairwise across the warp
       float s = 0.f, comp = 0.f;
 #pragma unroll
       for (int e = 0; e < 8; e++) {
@@ -412,21 +412,19 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
         comp = __fsub_rn(__fsub_rn(t2, s), y);
         s = t2;
       }
-      // pairwise FP32 tree across the warp for sum and compensation, then
-      // one FP64 combine per block on lane 0
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         s = __fadd_rn(s, __shfl_xor_sync(0xffffffffu, s, o));
         comp = __fadd_rn(comp, __shfl_xor_sync(0xffffffffu, comp, o));
       }
-      float th = 0.f;
-      if (lane == 0) {
-        const double ds = __dsub_rn((double)s, (double)comp);
-        const double env = __dsqrt_rn(__ddiv_rn(ds, 256.0));
-        // x > t (double) <=> x > round_down_to_float(t) for a float x.
-        th = __double2float_rd(__dadd_rn(__dmul_rn(env, cut), 1.0));
-      }
-      thrb[bb] = __shfl_sync(0xffffffffu, th, 0);
+      // env = sqrt(sum / 256) and the threshold env * cutoff + 1 in FP32.
+      // The reference forms them in double from its own FP32 xc; ours
+      // differ from them by a few FP32 ulps, the order of the difference
+      // between the two FP32 correlations themselves, so decisions can
+      // only part within that band around the threshold.  (FP64 would cost
+      // tens of cycles per warp instruction here.)
+      const float env = __fsqrt_rn(__fmul_rn(__fsub_rn(s, comp), 0.00390625f));
+      thrb[bb] = __fadd_rn(__fmul_rn(env, cut), 1.0f);
     }
   } else {
     thrb[0] = 1.0f;
