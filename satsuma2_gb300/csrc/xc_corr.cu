@@ -379,8 +379,7 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
     }
   }
   __syncthreads();
-  if constexpr (SEQ) fft_inverse<LOG2N>(bufE, twNh, twNl, tid, NT_CORR);
-  else fft_inverse<LOG2N>(bufE, twNh, twNl, tid < 256 ? tid : (1 << 30), 256);
+  fft_inverse<LOG2N>(bufE, twNh, twNl, tid, NT_CORR);
 
   // ---- 5. FindTop (SeqAnalyzer::FindTop, CrossCorr.cc:878-944): xc[i] =
   //      r[(i + N) mod L] / N; envelope over 256-sample blocks when L/256 > 8;
@@ -395,6 +394,18 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
     const float2 z = bufE[swz(n >> 1)];
     return ((n & 1) ? z.y : z.x) * scale;
   };
+  // Up to L = 8192 a lane's 16 values stay in registers across the three
+  // passes (envelope, count, compaction); longer transforms re-read them.
+  constexpr bool KEEP = ITER <= 16;
+  float xs[KEEP ? ITER : 1];
+  if constexpr (KEEP) {
+#pragma unroll
+    for (int e = 0; e < ITER; e++) xs[e] = xval(wbase + e * 32 + lane);
+  }
+  auto xat = [&](int e) -> float {
+    if constexpr (KEEP) return xs[e];
+    else return xval(wbase + e * 32 + lane);
+  };
   float thrb[PER_WARP >= 256 ? PER_WARP / 256 : 1];
   if constexpr (L / 256 > 8) {
     const float cut = (float)((D.flags & PF_FAST) ? P.cutoff_fast : P.cutoff);
@@ -405,7 +416,7 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
       float s = 0.f, comp = 0.f;
 #pragma unroll
       for (int e = 0; e < 8; e++) {
-        const float x = xval(wbase + bb * 256 + e * 32 + lane);
+        const float x = xat(bb * 8 + e);
         const float v = __fmul_rn(x, x);
         const float y = __fsub_rn(v, comp);
         const float t2 = __fadd_rn(s, y);
@@ -430,11 +441,14 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
     thrb[0] = 1.0f;
   }
   int wcount = 0;
-#pragma unroll 4
+  unsigned msk[KEEP ? ITER : 1];
+#pragma unroll(KEEP ? ITER : 4)
   for (int e = 0; e < ITER; e++) {
     const int i = wbase + e * 32 + lane;
-    const float x = xval(i);
-    wcount += __popc(__ballot_sync(0xffffffffu, x > thrb[(L / 256 > 8) ? (e >> 3) : 0]));
+    const float x = xat(e);
+    const unsigned m = __ballot_sync(0xffffffffu, x > thrb[(L / 256 > 8) ? (e >> 3) : 0]);
+    if constexpr (KEEP) msk[e] = m;
+    wcount += __popc(m);
     if (P.dbg_xc) P.dbg_xc[(size_t)(pidx * 2 + strand) * L + i] = x;
   }
   if (lane == 0) s_warp[warp] = wcount;
@@ -454,12 +468,13 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
   int run = s_warp[warp];
   int* out = P.off_list + D.off_base + (size_t)strand * L;
   const unsigned lt = (1u << lane) - 1u;
-#pragma unroll 4
+#pragma unroll(KEEP ? ITER : 4)
   for (int e = 0; e < ITER; e++) {
     const int i = wbase + e * 32 + lane;
-    const bool keep = xval(i) > thrb[(L / 256 > 8) ? (e >> 3) : 0];
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (keep) out[run + __popc(m & lt)] = i;
+    unsigned m;
+    if constexpr (KEEP) m = msk[e];
+    else m = __ballot_sync(0xffffffffu, xat(e) > thrb[(L / 256 > 8) ? (e >> 3) : 0]);
+    if ((m >> lane) & 1u) out[run + __popc(m & lt)] = i;
     run += __popc(m);
   }
 }

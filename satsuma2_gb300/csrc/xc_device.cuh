@@ -86,9 +86,8 @@ template <> struct Plan<14> : PlanR<4, 4, 4, 2> {};
 // Position of bin k after the forward (decimation-in-frequency) passes: the
 // digit of radix R_s (least significant first in k) moves to place value
 // N / (R_0 ... R_s).
-template <int LOG2N>
+template <int LOG2N, class PL = Plan<LOG2N>>
 __host__ __device__ constexpr int posof(int k) {
-  using PL = Plan<LOG2N>;
   int p = 0, off = 0, used = 0;
 #pragma unroll
   for (int s = 0; s < PL::n; s++) {
@@ -101,8 +100,8 @@ __host__ __device__ constexpr int posof(int k) {
 
 // Shared-memory index of bin k: swz(posof(k)).  Both maps are XOR-linear, so
 // lp(a | b) = lp(a) ^ lp(b) for bit-disjoint a and b.
-template <int LOG2N>
-__host__ __device__ constexpr int lp(int k) { return swz(posof<LOG2N>(k)); }
+template <int LOG2N, class PL = Plan<LOG2N>>
+__host__ __device__ constexpr int lp(int k) { return swz(posof<LOG2N, PL>(k)); }
 
 // ---------------------------------------------------------------------------
 // Small DFTs in registers, natural order in and out.  DIR = -1 forward
@@ -234,10 +233,10 @@ __device__ __forceinline__ void pass_lr(float2* buf, const float2* h, const floa
   else fft_pass<16, N, S, INV>(buf, h, l, t, nt);
 }
 
-template <int LOG2N, int s>
+template <int LOG2N, int s, class PL = Plan<LOG2N>>
 __host__ __device__ constexpr int plan_used() {   // sum of the log-radices of passes 0..s-1
   int u = 0;
-  for (int i = 0; i < s; i++) u += Plan<LOG2N>::lr(i);
+  for (int i = 0; i < s; i++) u += PL::lr(i);
   return u;
 }
 
@@ -254,12 +253,12 @@ __device__ __forceinline__ void fft_forward(float2* buf, const float2* h, const 
 
 // Inverse (unnormalised), digit-reversed in, natural order out: the forward
 // passes undone in reverse order.
-template <int LOG2N, int s = Plan<LOG2N>::n - 1>
+template <int LOG2N, class PL = Plan<LOG2N>, int s = PL::n - 1>
 __device__ __forceinline__ void fft_inverse(float2* buf, const float2* h, const float2* l, int t, int nt) {
   if constexpr (s >= 0) {
-    pass_lr<Plan<LOG2N>::lr(s), (1 << LOG2N), ((1 << LOG2N) >> plan_used<LOG2N, s>()), true>(buf, h, l, t, nt);
+    pass_lr<PL::lr(s), (1 << LOG2N), ((1 << LOG2N) >> plan_used<LOG2N, s, PL>()), true>(buf, h, l, t, nt);
     __syncthreads();
-    fft_inverse<LOG2N, s - 1>(buf, h, l, t, nt);
+    fft_inverse<LOG2N, PL, s - 1>(buf, h, l, t, nt);
   }
 }
 

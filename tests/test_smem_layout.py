@@ -20,19 +20,19 @@ def swz(p):
     return p ^ (((p >> 4) ^ (p >> 8) ^ (p >> 12)) & 15)
 
 
-def posof(k, log2n):
+def posof(k, log2n, plans=PLANS):
     p, off, used = 0, 0, 0
-    for lr in PLANS[log2n]:
+    for lr in plans[log2n]:
         used += lr
         p |= ((k >> off) & ((1 << lr) - 1)) << (log2n - used)
         off += lr
     return p
 
 
-def passes(log2n):
+def passes(log2n, plans=PLANS):
     n = 1 << log2n
     out, span = [], n
-    for lr in PLANS[log2n]:
+    for lr in plans[log2n]:
         out.append((1 << lr, span))
         span >>= lr
     return out
@@ -118,3 +118,4 @@ def test_spectrum_phases_conflict_free(log2n):
     assert worst_multiplicity(halfwarps(pos(n - k))) <= lim
     # signal construction and FindTop read natural order
     assert worst_multiplicity(halfwarps(np.arange(n))) == 1
+
