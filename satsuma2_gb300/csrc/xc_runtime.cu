@@ -585,16 +585,29 @@ int ctx_run_pairs(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, xc_result* o
 // one sub-batch overlap the kernels of the one before; results are collected
 // in order.  Sub-batches hold at least 1024 pairs (a launch fills the GPU) and
 // a big call is cut in about four.
+static constexpr size_t FIRST_SUB = 512;
+
 int ctx_align_pipelined(Ctx* c, const xc_pair* pairs, size_t n, xc_result* out, size_t cap, size_t* n_out,
                         size_t* pair_counts) {
   const size_t maxb = c->prm.max_batch > 0 ? (size_t)c->prm.max_batch : 4096;
-  const size_t sub = n <= 1024 ? n : std::min(maxb, std::max<size_t>(1024, (n + 3) / 4));
-  const size_t nchunks = (n + sub - 1) / sub;
+  // sub-batch boundaries: a short first one so the GPU starts early, then
+  // equal ones of at most max(1024, n/4) pairs
+  std::vector<size_t> bound{0};
+  if (n <= 1024) {
+    bound.push_back(n);
+  } else {
+    const size_t first = FIRST_SUB;
+    bound.push_back(first);
+    const size_t rest = n - first, size = std::min(maxb, std::max<size_t>(1024, (n + 3) / 4));
+    const size_t parts = (rest + size - 1) / size;
+    for (size_t i = 1; i <= parts; i++) bound.push_back(first + rest * i / parts);
+  }
+  const size_t nchunks = bound.size() - 1;
   size_t written = 0, need = 0;
   uint64_t h2d = 0, d2h = 0;
   bool full = false;   // output capacity exceeded: later sub-batches are only counted
   auto start = [&](size_t k) -> int {
-    const size_t lo = k * sub, m = std::min(sub, n - lo);
+    const size_t lo = bound[k], m = bound[k + 1] - lo;
     Batch* b = c->work[k & 1];
     const cudaStream_t s = c->work_stream[k & 1];
     int r = batch_pack(c, b, pairs + lo, m, s);
@@ -602,7 +615,7 @@ int ctx_align_pipelined(Ctx* c, const xc_pair* pairs, size_t n, xc_result* out, 
     return r;
   };
   auto finish = [&](size_t k) -> int {
-    const size_t lo = k * sub, m = std::min(sub, n - lo);
+    const size_t lo = bound[k], m = bound[k + 1] - lo;
     Batch* b = c->work[k & 1];
     xc_result* o = (full || !out) ? nullptr : out + written;
     const size_t cp = full ? 0 : (cap >= written ? cap - written : 0);
