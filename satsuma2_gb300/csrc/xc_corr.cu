@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
   float2* vq = vt + NWIN;
   __shared__ int s_cnt4[8];
   __shared__ double s_off[8];
+  __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
   __shared__ int s_warp[NT_CORR / 32];
 
   const int tid = threadIdx.x;
@@ -131,6 +132,14 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
     float E = 0.f;
     if (len < 1024) {
       E = 1.f;
+    } else if (!generic && w * WIN + WIN <= len) {
+      // A/C/G/T pair, full window: base counts from the 2-bit codes (one
+      // 8-bit field per base), weight from the host table
+      const int i0 = w * WIN;
+      uint32_t cnt = 0;
+      for (int j = 0; j < WIN; j++) cnt += 1u << (8 * code_of(s[i0 + j]));
+      const int a = cnt & 255u, c = (cnt >> 8) & 255u, g = (cnt >> 16) & 255u;
+      E = __ldg(&P.tab.ent_acgt[(a * (WIN + 1) + c) * (WIN + 1) + g]);
     } else if (w * WIN < len) {
       const int i0 = w * WIN;
       const int k = min(WIN, len - i0);
@@ -171,9 +180,23 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
   //      sums, or the sequential double sum when one-third letters occur ----
   {
     int cn[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int i = tid; i < N; i += NT_CORR) {
-      if (i < T) { const uchar4 q = c_w4q[st[i]]; cn[0] += q.x; cn[1] += q.y; cn[2] += q.z; cn[3] += q.w; }
-      if (i < Q) { const uchar4 q = c_w4q[sq[i]]; cn[4] += q.x; cn[5] += q.y; cn[6] += q.z; cn[7] += q.w; }
+    if (!generic) {
+      // A/C/G/T: one 8-bit count field per base (at most N / 512 <= 32 per thread)
+      uint32_t ct = 0, cq = 0;
+      for (int i = tid; i < N; i += NT_CORR) {
+        if (i < T) ct += 1u << (8 * code_of(st[i]));
+        if (i < Q) cq += 1u << (8 * code_of(sq[i]));
+      }
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        cn[k] = 4 * (int)((ct >> (8 * k)) & 255u);
+        cn[4 + k] = 4 * (int)((cq >> (8 * k)) & 255u);
+      }
+    } else {
+      for (int i = tid; i < N; i += NT_CORR) {
+        if (i < T) { const uchar4 q = c_w4q[st[i]]; cn[0] += q.x; cn[1] += q.y; cn[2] += q.z; cn[3] += q.w; }
+        if (i < Q) { const uchar4 q = c_w4q[sq[i]]; cn[4] += q.x; cn[5] += q.y; cn[6] += q.z; cn[7] += q.w; }
+      }
     }
 #pragma unroll
     for (int k = 0; k < 8; k++) {
@@ -198,6 +221,8 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
       }
     }
     s_off[tid] = off;
+    s_wmo[0][tid] = __dsub_rn(0.0, off);
+    s_wmo[1][tid] = __dsub_rn(1.0, off);
   }
   __syncthreads();
 
@@ -208,11 +233,10 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
     // Per-window channel values: out = float(entropy * (weight - mean))
     // (CrossCorr.cc:123), weight 0 or 1 for A/C/G/T.
     if (!generic) {
-      const double off = s_off[grp * 4 + c];
       const double E = (double)(grp ? Eq : Et)[gtid];
       float2 v;
-      v.x = __double2float_rn(__dmul_rn(E, __dsub_rn(0.0, off)));
-      v.y = __double2float_rn(__dmul_rn(E, __dsub_rn(1.0, off)));
+      v.x = __double2float_rn(__dmul_rn(E, s_wmo[0][grp * 4 + c]));
+      v.y = __double2float_rn(__dmul_rn(E, s_wmo[1][grp * 4 + c]));
       (grp ? vq : vt)[gtid] = v;
     }
     __syncthreads();

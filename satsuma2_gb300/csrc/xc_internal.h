@@ -39,6 +39,7 @@ struct LTables {
   const float2* twL_hi;    // exp(-2*pi*i*64a/L), a < N/64
   const float2* twL_lo;    // exp(-2*pi*i*b/L), b < 64
   const double* ent;       // Ent(p) for p = (a4/4)/k: [k][a4], k <= win, a4 <= 4*win
+  const float* ent_acgt;   // weight of a full window of a A, c C, g G, t T: [(a*(win+1)+c)*(win+1)+g]
 };
 
 // One kept match, strand-local coordinates.  key = FindTop offset index.

@@ -140,6 +140,7 @@ int align_pair_noalloc(Ctx* c, const xc_pair& p, xc_result* out, size_t cap, siz
   cp.tab.twL_hi = t.tw + NH + 64;
   cp.tab.twL_lo = t.tw + 2 * NH + 64;
   cp.tab.ent = t.ent;
+  cp.tab.ent_acgt = t.ent_acgt;
   cp.cutoff = c->prm.cutoff;
   cp.cutoff_fast = c->prm.cutoff_fast;
   cp.off_list = offl;

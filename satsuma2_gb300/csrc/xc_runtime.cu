@@ -110,11 +110,29 @@ static int build_tables(Ctx* c) {
         p /= (double)k;
         ent[(size_t)k * row + a4] = p < 0.001 ? 0.0 : p * log(p) / 0.69314718056;
       }
+    // Weight of a full window holding a A, c C, g G, t T (ComputeEntropy,
+    // CrossCorr.cc:80-91): -(Ent(a/w) + Ent(c/w) + Ent(g/w) + Ent(t/w)) in
+    // that order, rounded to float, clamped at 0 -- the kernel's own double
+    // steps, done once here.
+    const int W1 = win + 1;
+    std::vector<float> eacgt((size_t)W1 * W1 * W1, 0.f);
+    for (int a = 0; a <= win; a++)
+      for (int cc = 0; a + cc <= win; cc++)
+        for (int g = 0; a + cc + g <= win; g++) {
+          const int tt = win - a - cc - g;
+          const double* er = &ent[(size_t)win * row];
+          const double sv = ((er[4 * a] + er[4 * cc]) + er[4 * g]) + er[4 * tt];
+          float E = (float)(-sv);
+          if (E < 0.f) E = 0.f;
+          eacgt[((size_t)a * W1 + cc) * W1 + g] = E;
+        }
     DevTables& t = c->tab[lg];
     XC_CHECK(cudaMalloc(&t.tw, tw.size() * sizeof(float2)));
     XC_CHECK(cudaMalloc(&t.ent, ent.size() * sizeof(double)));
+    XC_CHECK(cudaMalloc(&t.ent_acgt, eacgt.size() * sizeof(float)));
     XC_CHECK(cudaMemcpy(t.tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice));
     XC_CHECK(cudaMemcpy(t.ent, ent.data(), ent.size() * sizeof(double), cudaMemcpyHostToDevice));
+    XC_CHECK(cudaMemcpy(t.ent_acgt, eacgt.data(), eacgt.size() * sizeof(float), cudaMemcpyHostToDevice));
   }
   const Codec& cd = codec();
   std::vector<int8_t> score(128 * 128);
@@ -388,6 +406,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     cp.tab.twL_hi = t.tw + NH + 64;
     cp.tab.twL_lo = t.tw + 2 * NH + 64;
     cp.tab.ent = t.ent;
+    cp.tab.ent_acgt = t.ent_acgt;
     cp.cutoff = c->prm.cutoff;
     cp.cutoff_fast = c->prm.cutoff_fast;
     cp.off_list = b->d_off;
@@ -718,7 +737,7 @@ int xc_destroy(xc_ctx* c) {
     if (c->work_stream[i]) cudaStreamDestroy(c->work_stream[i]);
   }
   for (auto& t : c->tab) {
-    cudaFree(t.tw); cudaFree(t.ent);
+    cudaFree(t.tw); cudaFree(t.ent); cudaFree(t.ent_acgt);
   }
   cudaFree(c->d_score); cudaFree(c->d_eq); cudaFree(c->d_gcw); cudaFree(c->d_ptable);
   if (c->stream) cudaStreamDestroy(c->stream);

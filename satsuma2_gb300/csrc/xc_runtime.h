@@ -73,6 +73,7 @@ struct Server;
 struct DevTables {
   float2* tw = nullptr;    // W_N hi (N/64), W_N lo (64), W_L hi (N/64), W_L lo (64)
   double* ent = nullptr;
+  float* ent_acgt = nullptr;   // entropy weight of full A/C/G/T windows by base counts
 };
 
 struct Ctx {
