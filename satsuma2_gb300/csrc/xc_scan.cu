@@ -7,12 +7,12 @@
 //       pass 1 (thread = diagonal): on 2-bit bitplanes, 32 equality bits per
 //         word op, a branch-free screen marks the 8-check blocks whose
 //         53-position span holds >= 19 equal bases;
-//       items: the marked blocks of the round laid out contiguously per
+//       items: the marked words of the round laid out contiguously per
 //         diagonal by a prefix sum, processed one per thread --
-//         phase A: the block's 8 exact window bits;
+//         phase A: exact window bits of the word's marked blocks;
 //         phase B: falls and closing ends of runs against the previous
-//           block's last bit, queued as (item, bit) with one atomic per warp;
-//       phase C (thread = segment): run start from the same block or by
+//           word's last bit, queued as (item, bit) with one atomic per warp;
+//       phase C (thread = segment): run start from the same word or by
 //         looking back, equal-base count, FP32 probability screen, exact FP64
 //         GetMatchProbability / PrintMatch for survivors.
 //     Other pairs (N, IUPAC, unknown letters): the reference's byte-table
@@ -37,11 +37,11 @@ template <int LOG2L> struct ScanGeom {
   // Marked-block items of one pass-2 sub-range and the segment queue (4 bytes
   // each; item indices fit 12 bits).  The queue shares its bytes with the
   // chunk byte arrays, which only the byte-table path fills.
-  static constexpr int ICAP = 3072;
+  static constexpr int ICAP = 1536;   // items (8 bytes each: word, passing bits)
   static constexpr int QCAP = 2048;
   static constexpr size_t region = (size_t)QCAP * 4 > 2 * (size_t)N ? (size_t)QCAP * 4 : 2 * (size_t)N;
   static constexpr size_t bytes = region +
-      (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK + FW * NT_SCAN + ICAP + NT_SCAN) * 4 +
+      (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK + FW * NT_SCAN + 2 * ICAP + NT_SCAN) * 4 +
       (size_t)OFF_CHUNK * 2;
 };
 
@@ -95,7 +95,7 @@ __device__ __forceinline__ void gc_prefix(const uint32_t* b0, const uint32_t* b1
 }
 
 template <int LOG2L>
-__global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
+__global__ void __launch_bounds__(NT_SCAN, 6) scan_kernel(const ScanParams P) {
   using Gm = ScanGeom<LOG2L>;
   constexpr int L = Gm::L, N = Gm::N, TW = Gm::TW, TWP = Gm::TWP, QPAD = Gm::QPAD, QWP = Gm::QWP;
   constexpr int ICAP = Gm::ICAP, QCAP = Gm::QCAP, NWARP = NT_SCAN / 32;
@@ -112,13 +112,14 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
   int* qgp = reinterpret_cast<int*>(qb1 + QWP);
   int* offs = qgp + (TW + 1);
   uint32_t* bflags = reinterpret_cast<uint32_t*>(offs + OFF_CHUNK);   // [FW][NT_SCAN] pass-1 block masks
-  uint32_t* items = bflags + Gm::FW * NT_SCAN;                        // [ICAP] diag | block << 7 | G << 24
-  int* dpos = reinterpret_cast<int*>(items + ICAP);                   // [NT_SCAN] offsets of the round
+  uint32_t* items = bflags + Gm::FW * NT_SCAN;                        // [ICAP] diag | word << 7 | blocks << 17
+  uint32_t* gbits = items + ICAP;                                     // [ICAP] passing checks of the word
+  int* dpos = reinterpret_cast<int*>(gbits + ICAP);                   // [NT_SCAN] offsets of the round
   uint16_t* order = reinterpret_cast<uint16_t*>(dpos + NT_SCAN);
   __shared__ int s_hist[64];
   __shared__ int s_wsum[NWARP];
   __shared__ int s_next, s_res, s_qn;
-  __shared__ int s_cy_d[2], s_cy_blk[2], s_cy_g[2], s_cy_start[2];
+  __shared__ int s_cy_d[2], s_cy_w[2], s_cy_g[2], s_cy_start[2];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int pidx = P.first + blockIdx.x;
@@ -409,14 +410,14 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
           acc |= f << (4 * (q & 7));
           if ((q & 7) == 7 || w == wlast) {
             bflags[(q >> 3) * NT_SCAN + tid] = acc;
-            nb += __popc(acc);
+            nb += __popc((acc | (acc >> 1) | (acc >> 2) | (acc >> 3)) & 0x11111111u);   // marked words
             acc = 0;
           }
           e2 = e1;
           e1 = e0;
         }
       }
-      // item index of this diagonal's first marked block: CTA exclusive scan
+      // item index of this diagonal's first marked word: CTA exclusive scan
       const int nincl = warp_incl_sum(nb, lane);
       if (lane == 31) s_wsum[warp] = nincl;
       if (tid == 0) s_cy_d[1] = -1;   // nothing carried into the first sub-range
@@ -429,9 +430,9 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
         total += v;
       }
 
-      // ---- pass 2 over sub-ranges of at most ICAP items.  A sub-range may
-      //      split a diagonal: its last item (block, bits, open-run start)
-      //      is carried into the next one.
+      // ---- pass 2 over sub-ranges of at most ICAP items (one per marked
+      //      word).  A sub-range may split a diagonal: its last item (word,
+      //      bits, open-run start) is carried into the next one.
       int par = 0;
       for (int g0 = 0; g0 < total; g0 += ICAP, par ^= 1) {
         const int n = min(ICAP, total - g0);
@@ -440,85 +441,92 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
           int kk = ibase;
           const int nq8 = (wlast - wfirst + 8) >> 3;
           for (int q8 = 0; q8 < nq8 && kk < g1; q8++) {
-            uint32_t ent = bflags[q8 * NT_SCAN + tid];
-            const int c = __popc(ent);
+            const uint32_t ent = bflags[q8 * NT_SCAN + tid];
+            uint32_t nz = (ent | (ent >> 1) | (ent >> 2) | (ent >> 3)) & 0x11111111u;
+            const int c = __popc(nz);
             if (kk + c <= g0) {
               kk += c;
               continue;
             }
-            while (ent) {
-              const int bi = __ffs(ent) - 1;
-              ent &= ent - 1;
-              if (kk >= g0 && kk < g1) items[kk - g0] = (uint32_t)tid | ((uint32_t)(32 * q8 + bi) << 7);
+            while (nz) {
+              const int bi = __ffs(nz) - 1;   // 4 x word within the entry
+              nz &= nz - 1;
+              if (kk >= g0 && kk < g1)
+                items[kk - g0] = (uint32_t)tid | ((uint32_t)(8 * q8 + (bi >> 2)) << 7) | (((ent >> bi) & 15u) << 17);
               kk++;
             }
           }
         }
         __syncthreads();
 
-        // ---- phase A (thread = item): exact window bits of the block's
-        //      8 checks, window(c) = window(c-1) + e[c] - e[c-46].
+        // ---- phase A (thread = item): exact window bits of the word's
+        //      marked blocks, window(c) = window(c-1) + e[c] - e[c-46];
+        //      unmarked blocks hold no passing check.
         for (int i = tid; i < n; i += NT_SCAN) {
           const uint32_t it = items[i];
-          const int d = (int)(it & 127u), blk = (int)((it >> 7) & 2047u);
+          const int d = (int)(it & 127u), wr = (int)((it >> 7) & 1023u);
+          uint32_t f = (it >> 17) & 15u;
           const int p = dpos[d];
           const int cf = max(0, -p) + 46, cl = min(T - 1, Q - p) - 1;
-          const int sb = blk & 3, w = (cf >> 5) + (blk >> 2);
-          const int cb = 32 * w + 8 * sb;
+          const int w = (cf >> 5) + wr;
           const uint32_t e2 = eword(p, w - 2), e1 = eword(p, w - 1), e0 = eword(p, w);
           const uint64_t U = ((uint64_t)e1 << 32) | e2;
-          const uint32_t Y = e0 >> (8 * sb);
-          const uint32_t X = (uint32_t)(U >> (8 * sb + 18));
-          int c = __popcll(U >> (8 * sb + 19)) + __popc(e0 & lowmask(8 * sb + 1));
-          uint32_t g = (uint32_t)(c >= MIN_HITS);
+          uint32_t g = 0;
+          while (f) {
+            const int sb = __ffs(f) - 1;
+            f &= f - 1;
+            const uint32_t Y = e0 >> (8 * sb);
+            const uint32_t X = (uint32_t)(U >> (8 * sb + 18));
+            int c = __popcll(U >> (8 * sb + 19)) + __popc(e0 & lowmask(8 * sb + 1));
+            uint32_t gb = (uint32_t)(c >= MIN_HITS);
 #pragma unroll
-          for (int u = 1; u < 8; u++) {
-            c += (int)((Y >> u) & 1u) - (int)((X >> u) & 1u);
-            g |= (uint32_t)(c >= MIN_HITS) << u;
+            for (int u = 1; u < 8; u++) {
+              c += (int)((Y >> u) & 1u) - (int)((X >> u) & 1u);
+              gb |= (uint32_t)(c >= MIN_HITS) << u;
+            }
+            g |= gb << (8 * sb);
           }
-          const int lo = max(cf - cb, 0), hi = min(cl - cb, 7);
-          const uint32_t vm8 = (0xffu >> (7 - hi)) & (0xffu << lo);
-          items[i] = it | ((g & vm8) << 24);
+          const int lo = max(cf - 32 * w, 0), hi = min(cl - 32 * w, 31);
+          gbits[i] = g & (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
         }
         __syncthreads();
 
         // ---- phase B (thread = item): falls and closing ends of runs of
         //      passing checks, queued as (item, bit) descriptors.
         const int cy = par ^ 1;   // carry slot written by the previous sub-range
-        auto prev_bit = [&](int i, int d, int blk) -> uint32_t {
+        auto prev_bit = [&](int i, int d, int wr) -> uint32_t {
           if (i > 0) {
             const uint32_t pv = items[i - 1];
-            return ((int)(pv & 127u) == d && (int)((pv >> 7) & 2047u) == blk - 1) ? (pv >> 31) : 0u;
+            return ((int)(pv & 127u) == d && (int)((pv >> 7) & 1023u) == wr - 1) ? (gbits[i - 1] >> 31) : 0u;
           }
-          return (s_cy_d[cy] == d && s_cy_blk[cy] == blk - 1) ? (((uint32_t)s_cy_g[cy] >> 7) & 1u) : 0u;
+          return (s_cy_d[cy] == d && s_cy_w[cy] == wr - 1) ? ((uint32_t)s_cy_g[cy] >> 31) : 0u;
         };
         // check position where the run holding bit u-1 of item i began
-        auto run_start = [&](int i, int d, int blk, uint32_t g, int u) -> int {
-          uint32_t rb = g & ~(((g << 1) | prev_bit(i, d, blk)) & 0xffu) & lowmask(u);
+        auto run_start = [&](int i, int d, int wr, uint32_t g, int u) -> int {
+          uint32_t rb = g & ~((g << 1) | prev_bit(i, d, wr)) & lowmask(u);
           while (!rb) {
             if (--i < 0) return s_cy_start[cy];
-            const uint32_t it = items[i];
-            blk = (int)((it >> 7) & 2047u);
-            g = it >> 24;
-            rb = g & ~(((g << 1) | prev_bit(i, d, blk)) & 0xffu);
+            wr = (int)((items[i] >> 7) & 1023u);
+            g = gbits[i];
+            rb = g & ~((g << 1) | prev_bit(i, d, wr));
           }
-          return 32 * ((max(0, -dpos[d]) + 46) >> 5) + 8 * blk + (31 - __clz((int)rb));
+          return 32 * (((max(0, -dpos[d]) + 46) >> 5) + wr) + (31 - __clz((int)rb));
         };
-        // segment ending at bit u (0..7: a fall; 8: the closing end) of item i
+        // segment ending at bit u (0..31: a fall; 32: the closing end) of item i
         auto segment = [&](int i, int u) {
           const uint32_t it = items[i];
-          const int d = (int)(it & 127u), blk = (int)((it >> 7) & 2047u);
-          const uint32_t g = it >> 24;
+          const int d = (int)(it & 127u), wr = (int)((it >> 7) & 1023u);
+          const uint32_t g = gbits[i];
           const int p = dpos[d];
           const int cf = max(0, -p) + 46, ie = min(T - 1, Q - p), cl = ie - 1;
-          const int cb = 32 * (cf >> 5) + 8 * blk;
-          int s1 = cb + u, ub = u;
-          if (u == 8) {
-            const int hi = min(cl - cb, 7);
-            s1 = cb + hi == cl ? ie : cb + 8;
+          const int cw = 32 * ((cf >> 5) + wr);
+          int s1 = cw + u, ub = u;
+          if (u == 32) {
+            const int hi = min(cl - cw, 31);
+            s1 = cw + hi == cl ? ie : cw + 32;
             ub = hi + 1;
           }
-          const int s0 = run_start(i, d, blk, g, ub) - 45;
+          const int s0 = run_start(i, d, wr, g, ub) - 45;
           if (s0 < 1 || s1 <= s0) {   // cannot happen: a run start precedes its end
             atomicOr(P.err, 4);
             return;
@@ -527,43 +535,48 @@ __global__ void __launch_bounds__(NT_SCAN) scan_kernel(const ScanParams P) {
         };
         for (int ib = 0; ib < n; ib += NT_SCAN) {
           const int i = ib + tid;
-          uint32_t ends = 0;   // fall bits, bit 8 = closing end
+          uint32_t fall = 0;
+          bool close = false;
           if (i < n) {
             const uint32_t it = items[i];
-            const int d = (int)(it & 127u), blk = (int)((it >> 7) & 2047u);
-            const uint32_t g = it >> 24;
+            const int d = (int)(it & 127u), wr = (int)((it >> 7) & 1023u);
+            const uint32_t g = gbits[i];
             const int p = dpos[d];
             const int cf = max(0, -p) + 46, cl = min(T - 1, Q - p) - 1;
-            const int cb = 32 * (cf >> 5) + 8 * blk;
-            const int lo = max(cf - cb, 0), hi = min(cl - cb, 7);
-            const uint32_t vm8 = (0xffu >> (7 - hi)) & (0xffu << lo);
-            ends = ~g & (((g << 1) | prev_bit(i, d, blk)) & 0xffu) & vm8;
-            // a run still open at the block's last valid check ends at the
-            // diagonal's end or at the first check of an unmarked next block
-            if (((g >> hi) & 1u) &&
-                (cb + hi == cl || !((bflags[((blk + 1) >> 5) * NT_SCAN + d] >> ((blk + 1) & 31)) & 1u)))
-              ends |= 0x100u;
+            const int cw = 32 * ((cf >> 5) + wr);
+            const int lo = max(cf - cw, 0), hi = min(cl - cw, 31);
+            const uint32_t vm = (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
+            fall = ~g & ((g << 1) | prev_bit(i, d, wr)) & vm;
+            // a run still open at the word's last valid check ends at the
+            // diagonal's end or at the first check of an unmarked next word
+            if ((g >> hi) & 1u)
+              close = cw + hi == cl ||
+                      !((bflags[((wr + 1) >> 3) * NT_SCAN + d] >> (4 * ((wr + 1) & 7))) & 15u);
             if (i == n - 1) {   // carried into the next sub-range
               s_cy_d[par] = d;
-              s_cy_blk[par] = blk;
+              s_cy_w[par] = wr;
               s_cy_g[par] = (int)g;
-              s_cy_start[par] = ((g >> 7) & 1u) ? run_start(i, d, blk, g, 8) : -1;
+              s_cy_start[par] = (g >> 31) ? run_start(i, d, wr, g, 32) : -1;
             }
           }
-          const int nseg = __popc(ends);
+          const int nseg = __popc(fall) + (close ? 1 : 0);
           const int sincl = warp_incl_sum(nseg, lane);
           int q = 0;
           if (lane == 31 && sincl) q = atomicAdd(&s_qn, sincl);
           q = __shfl_sync(FULL, q, 31) + sincl - nseg;
-          while (ends) {
-            const int u = __ffs(ends) - 1;
-            ends &= ends - 1;
+          auto enqueue = [&](int u) {
             if (q < QCAP)
               queue[q] = (uint32_t)i | ((uint32_t)u << 12);
             else
               segment(i, u);   // full queue: in place
             q++;
+          };
+          while (fall) {
+            const int u = __ffs(fall) - 1;
+            fall &= fall - 1;
+            enqueue(u);
           }
+          if (close) enqueue(32);
         }
         __syncthreads();
 

@@ -275,3 +275,123 @@ def test_item_model_matches_oracle_doone(O, icap):
             got = model_doone_items(t, q, pos, icap)
             want = O.doone(t, q, pos)
             assert [g[:3] for g in got] == [tuple(x) for x in want.tolist()], (pos, icap)
+
+
+def model_doone_words(t, q, pos, icap=4096):
+    """Pass 2 with one item per marked word (its 4-bit block mask from the
+    screen): phase A gives the item the exact bits of its marked blocks
+    (unmarked blocks hold no passing check), phase B finds falls and closing
+    ends against the previous word's bit 31, phase C takes each run start
+    from the same word or by looking back over adjacent items.  Sub-ranges
+    of icap items carry the last item into the next.  Returns segments sorted
+    by start."""
+    T, Q = len(t), len(q)
+    TW = max(T, Q) // 32 + 2
+    tb0, tb1 = planes(t, TW + 2)
+    qb0, qb1 = planes(q, TW + 8, pad=2)
+    i0 = max(0, -pos)
+    iend = min(T - 1, Q - pos)
+    cfirst, clast = i0 + 46, iend - 1
+    if clast < cfirst:
+        return []
+
+    def fs(lo, hi, sh):
+        return ((hi << 32 | lo) >> sh) & M32
+
+    def eword(w):
+        if w < 0:
+            return 0
+        qo = 32 * w + pos + 64
+        qw, sh = qo >> 5, qo & 31
+        return ~((tb0[w] ^ fs(qb0[qw], qb0[qw + 1], sh)) | (tb1[w] ^ fs(qb1[qw], qb1[qw + 1], sh))) & M32
+
+    def vmask(w):
+        lo, hi = max(cfirst - 32 * w, 0), min(clast - 32 * w, 31)
+        return (M32 >> (31 - hi)) & (M32 << lo) & M32
+
+    wfirst, wlast = cfirst >> 5, clast >> 5
+    marked = {}
+    for w in range(wfirst, wlast + 1):
+        e2, e1, e0 = eword(w - 2), eword(w - 1), eword(w)
+        U = (e1 << 32) | e2
+        vm = vmask(w)
+        f = 0
+        for sb in range(4):
+            a = 8 * sb + 19
+            if popc(U >> a) + popc(e0 & lowmask(a - 11)) >= MIN_HITS and (vm >> (8 * sb)) & 0xFF:
+                f |= 1 << sb
+        if f:
+            marked[w] = f
+    words = sorted(marked)
+    # phase A
+    G = []
+    for w in words:
+        e2, e1, e0 = eword(w - 2), eword(w - 1), eword(w)
+        U = (e1 << 32) | e2
+        g = 0
+        for sb in range(4):
+            if not (marked[w] >> sb) & 1:
+                continue
+            for u in range(8 * sb, 8 * sb + 8):
+                if popc(U >> (u + 19)) + popc(e0 & lowmask(u + 1)) >= MIN_HITS:
+                    g |= 1 << u
+        G.append(g & vmask(w))
+
+    segs = []
+    carry = None   # (word, G, open-run start) of the previous sub-range's last item
+    for g0 in range(0, len(words), icap):
+        g1 = min(len(words), g0 + icap)
+
+        def pbit_of(i):
+            if i > g0:
+                return (G[i - 1] >> 31) if words[i - 1] == words[i] - 1 else 0
+            if carry is not None and carry[0] == words[i] - 1:
+                return carry[1] >> 31
+            return 0
+
+        def rise_of(i):
+            return G[i] & ~(((G[i] << 1) | pbit_of(i)) & M32) & M32
+
+        def run_start(i, u):
+            rb = rise_of(i) & lowmask(u)
+            while not rb:
+                i -= 1
+                if i < g0:
+                    return carry[2]
+                rb = rise_of(i)
+            return 32 * words[i] + rb.bit_length() - 1
+
+        for i in range(g0, g1):
+            w, g = words[i], G[i]
+            vm = vmask(w)
+            hi = min(clast - 32 * w, 31)
+            fall = ~g & (((g << 1) | pbit_of(i)) & M32) & vm & M32
+            for u in range(32):
+                if (fall >> u) & 1:
+                    segs.append((run_start(i, u) - 45, 32 * w + u))
+            if (g >> hi) & 1:
+                if 32 * w + hi == clast:
+                    segs.append((run_start(i, hi + 1) - 45, iend))
+                elif w + 1 not in marked:
+                    segs.append((run_start(i, 32) - 45, 32 * w + 32))
+        last = g1 - 1
+        carry = (words[last], G[last], run_start(last, 32) if (G[last] >> 31) & 1 else -1)
+    segs.sort()
+    return [(s, s + pos, e - s, equal_bases(t, q, s, pos, e - s)) for s, e in segs]
+
+
+@pytest.mark.parametrize("icap", [4096, 5, 1])
+def test_word_model_matches_oracle_doone(O, icap):
+    rng = np.random.default_rng(80)
+    cases = W.uniform_batch(4, seed=13) + [W.plain_pair(6)]
+    t = W.random_bases(rng, 4096)
+    cases.append((t.tobytes(), t.tobytes()))
+    cases.append((t.tobytes(), W.tandem_repeat(rng, 4096, 2, 3).tobytes()))
+    for t, q in cases:
+        offs = O.findtop(O.xcorr64(t, q, 8192), 1.8)
+        extra = rng.integers(-4095, 4096, size=10)
+        for i in list(offs[:20]) + [int(x) + 4096 for x in extra]:
+            pos = int(i) - 4096
+            got = model_doone_words(t, q, pos, icap)
+            want = O.doone(t, q, pos)
+            assert [g[:3] for g in got] == [tuple(x) for x in want.tolist()], (pos, icap)
