@@ -192,7 +192,8 @@ def serve_run(x, items, n_threads=4, req_pairs=64, total=16384, rate=None):
     """Submits requests from n_threads threads; rate (pairs/s) None = as fast as
     admission allows.  Returns (pairs/s, p50, p99)."""
     import satsuma2_gb300 as sg
-    reqs = [items[(i * req_pairs) % len(items):(i * req_pairs) % len(items) + req_pairs]
+    # requests built ahead of the clock: the measured path is submit/wait
+    reqs = [sg.make_pairs([items[(i * req_pairs + j) % len(items)] for j in range(req_pairs)])
             for i in range(total // req_pairs)]
     lat = []
     lock = threading.Lock()
@@ -322,9 +323,11 @@ def run_ours(args):
     plain = plain_n / (time.perf_counter() - t0)
 
     # ---- served: continuous batching, saturating and at a fixed arrival rate ----
-    xs = sg.XCorr(target_total=TARGET_TOTAL, device=local, max_batch=2048)
+    xs = sg.XCorr(target_total=TARGET_TOTAL, device=local, max_batch=4096)
     serve_run(xs, items, total=4096)   # warm
-    served, p50_sat, p99_sat = serve_run(xs, items, n_threads=8, req_pairs=64, total=32768)
+    # saturating: 8 client threads, each request one grid block of 24 x 24
+    # chunk pairs (the slave's t_pair unit), as many in flight as admitted
+    served, p50_sat, p99_sat = serve_run(xs, items, n_threads=8, req_pairs=576, total=576 * 256)
     rate = 200000.0
     _, p50, p99 = serve_run(xs, items, n_threads=8, req_pairs=16, total=16384, rate=rate)
     xs.close()
@@ -359,6 +362,7 @@ def run_ours(args):
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "results_match_device_run": bool(same)},
         "plain_pairs_per_s": plain, "served_pairs_per_s": served, "served_vs_plain": served / plain,
+        "served_request_pairs": 576, "latency_request_pairs": 16,
         "served_p50_ms_saturated": p50_sat, "served_p99_ms_saturated": p99_sat,
         "p50_ms": p50, "p99_ms": p99, "latency_arrival_rate_pairs_per_s": rate,
         "stage_ms": {"corr_findtop": corr_ms, "scan_filter": scan_ms, "finalize": fin_ms},

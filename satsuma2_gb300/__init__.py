@@ -207,7 +207,12 @@ class XCorr:
 
     # serving -------------------------------------------------------------------
     def submit(self, items):
-        arr, keep = make_pairs(items)
+        """Queues chunk pairs for the GPU; items as for align, or the (array,
+        keepalive) pair make_pairs returns (built ahead of time)."""
+        if isinstance(items, tuple) and len(items) == 2 and isinstance(items[0], ctypes.Array):
+            arr, keep = items
+        else:
+            arr, keep = make_pairs(items)
         t = ctypes.c_uint64()
         _check(self.lib.xc_submit(self.ctx, arr, len(arr), ctypes.byref(t)), "xc_submit")
         return t.value

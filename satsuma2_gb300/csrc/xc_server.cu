@@ -70,6 +70,9 @@ struct Server {
   uint64_t completed = 0, pairs_done = 0;
   int device = 0;
   size_t max_batch = 4096;
+  size_t min_batch = 1024;   // while the GPU is busy, wait for this many pairs ...
+  double max_wait_ms = 2.0;  // ... or for the oldest request to wait this long
+  size_t res_per_pair = 8;   // read-back buffer estimate (records per pair)
 };
 
 // Device bytes one pair needs inside a batch (sequences, offsets, results).
@@ -84,12 +87,15 @@ static void complete_slot(Server* S, Slot& sl) {
   const size_t n = sl.items.size();
   std::vector<size_t> counts(n);
   size_t need = 0;
-  int r = batch_collect(S->ctx, sl.b, sl.s, nullptr, 0, &need, counts.data());
-  std::vector<xc_result> res;
-  if (r == XC_ERR_CAPACITY || (r == XC_OK && need == 0)) {
+  // one read-back into a buffer sized from the last batch's yield; a second
+  // only when it was too small
+  std::vector<xc_result> res(std::max<size_t>(S->res_per_pair * n + 1024, 4096));
+  int r = batch_collect(S->ctx, sl.b, sl.s, res.data(), res.size(), &need, counts.data());
+  if (r == XC_ERR_CAPACITY && need > res.size() && sl.b->h_misc[1] == 0) {
     res.resize(need);
     r = batch_collect(S->ctx, sl.b, sl.s, res.data(), res.size(), &need, counts.data());
   }
+  if (r == XC_OK && n) S->res_per_pair = std::max<size_t>(4, 2 * need / n);
   const auto now = Clock::now();
   std::lock_guard<std::mutex> lk(S->mu);
   size_t o = 0;
@@ -129,18 +135,28 @@ static void scheduler(Server* S) {
       if (cudaEventQuery(oldest->ev) != cudaSuccess) break;
       complete_slot(S, *oldest);
     }
-    // 2. fill a free slot from the queue
+    // 2. fill a free slot from the queue: at once when the GPU is idle,
+    //    otherwise once a batch worth launching has gathered (or the oldest
+    //    request has waited long enough)
     Slot* free_slot = nullptr;
-    for (auto& sl : S->slots)
-      if (!sl.busy) { free_slot = &sl; break; }
-    bool launched = false;
+    int busy = 0;
+    for (auto& sl : S->slots) {
+      busy += sl.busy;
+      if (!sl.busy && !free_slot) free_slot = &sl;
+    }
+    bool launched = false, holding = false;
     if (free_slot) {
       std::unique_lock<std::mutex> lk(S->mu);
-      if (S->stop && S->queue.empty()) {
-        bool any_busy = false;
-        for (auto& sl : S->slots) any_busy |= sl.busy;
-        if (!any_busy) return;
+      if (S->stop && S->queue.empty() && busy == 0) return;
+      if (busy > 0 && !S->queue.empty() && S->queued_pairs < S->min_batch &&
+          std::chrono::duration<double, std::milli>(Clock::now() - S->queue.front()->t_submit).count() <
+              S->max_wait_ms) {
+        holding = true;
+        lk.unlock();
       }
+    }
+    if (free_slot && !holding) {
+      std::unique_lock<std::mutex> lk(S->mu);
       free_slot->items.clear();
       free_slot->pairs.clear();
       while (!S->queue.empty() && free_slot->pairs.size() < S->max_batch) {
@@ -184,7 +200,7 @@ static void scheduler(Server* S) {
       if (sl.busy && (!oldest || sl.seq < oldest->seq)) oldest = &sl;
     if (oldest) {
       std::unique_lock<std::mutex> lk(S->mu);
-      const bool have_work = !S->queue.empty() && free_slot != nullptr;
+      const bool have_work = !S->queue.empty() && free_slot != nullptr && !holding;
       lk.unlock();
       if (!have_work) {
         // short polling keeps new arrivals flowing into free slots
@@ -212,6 +228,7 @@ static int server_start(Ctx* c) {
   }
   S->budget_bytes = free_b / 2;
   S->max_pairs = 64 * S->max_batch;
+  S->min_batch = std::min<size_t>(S->max_batch, 1024);
   for (auto& sl : S->slots) {
     sl.b = new_batch(c);
     if (cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking) != cudaSuccess ||
