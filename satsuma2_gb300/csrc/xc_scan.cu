@@ -156,24 +156,40 @@ __global__ void __launch_bounds__(NT_SCAN, 6) scan_kernel(const ScanParams P) {
     // 2-bit codes as two bitplanes straight from the pool, bit u of word w =
     // position 32w+u: one warp per word, one ballot per plane.  The pair is
     // all A/C/G/T, whose complement flips both code bits.
-    for (int w = warp; w < TWP; w += NWARP) {
-      const int i = 32 * w + lane;
-      const bool in = i < T;
-      const uint32_t cd = in ? code_of(gt[i]) : 0u;
-      const uint32_t b0 = __ballot_sync(FULL, cd & 1u), b1 = __ballot_sync(FULL, cd & 2u);
-      if (lane == 0) {
-        tb0[w] = b0;
-        tb1[w] = b1;
+    // Eight words per step: their loads are all in flight before the ballots.
+    constexpr int UNR = 8;
+    for (int w0 = warp; w0 < TWP; w0 += NWARP * UNR) {
+      uint32_t cd[UNR];
+#pragma unroll
+      for (int k = 0; k < UNR; k++) {
+        const int i = 32 * (w0 + NWARP * k) + lane;
+        cd[k] = i < T ? code_of(gt[i]) : 0u;
+      }
+#pragma unroll
+      for (int k = 0; k < UNR; k++) {
+        const int w = w0 + NWARP * k;
+        const uint32_t b0 = __ballot_sync(FULL, cd[k] & 1u), b1 = __ballot_sync(FULL, cd[k] & 2u);
+        if (lane == 0 && w < TWP) {
+          tb0[w] = b0;
+          tb1[w] = b1;
+        }
       }
     }
-    for (int w = warp; w < QWP; w += NWARP) {
-      const int i = 32 * (w - QPAD) + lane;
-      const bool in = i >= 0 && i < Q;
-      const uint32_t cd = in ? (strand ? code_of(gq[Q - 1 - i]) ^ 3u : code_of(gq[i])) : 0u;
-      const uint32_t b0 = __ballot_sync(FULL, cd & 1u), b1 = __ballot_sync(FULL, cd & 2u);
-      if (lane == 0) {
-        qb0[w] = b0;
-        qb1[w] = b1;
+    for (int w0 = warp; w0 < QWP; w0 += NWARP * UNR) {
+      uint32_t cd[UNR];
+#pragma unroll
+      for (int k = 0; k < UNR; k++) {
+        const int i = 32 * (w0 + NWARP * k - QPAD) + lane;
+        cd[k] = (i >= 0 && i < Q) ? (strand ? code_of(gq[Q - 1 - i]) ^ 3u : code_of(gq[i])) : 0u;
+      }
+#pragma unroll
+      for (int k = 0; k < UNR; k++) {
+        const int w = w0 + NWARP * k;
+        const uint32_t b0 = __ballot_sync(FULL, cd[k] & 1u), b1 = __ballot_sync(FULL, cd[k] & 2u);
+        if (lane == 0 && w < QWP) {
+          qb0[w] = b0;
+          qb1[w] = b1;
+        }
       }
     }
     __syncthreads();
