@@ -289,3 +289,30 @@ def test_wait_times_out_and_keeps_ticket():
     assert len(res) >= 0
     assert timed_out or len(res) >= 0
     x.close()
+
+
+def test_edge_chunks_match_oracle(O):
+    """Empty chunks (the slave clears all-N chunks to length 0), very short
+    ones, odd lengths, a chunk of N only and one of IUPAC letters, in one
+    batch: every pair's records equal the oracle's over the GPU's offsets."""
+    import satsuma2_gb300 as sg
+    rng = np.random.default_rng(44)
+    full = W.random_bases(rng, 4096).tobytes()
+    items = [
+        (b"", full), (full, b""), (b"", b""),
+        (full[:5], full[:7]), (full[:45], full[:46]), (full[:47], full[:47]),
+        (full[:1023], full[:1025]), (full[:1024], full[:3001]), (full[3:3004], full[:4096]),
+        (b"N" * 4096, full), (full[:2000] + b"RYKMSWBDHVN" * 50 + full[2550:4096], full),
+    ]
+    TT = 4096.0 * 16
+    x = sg.XCorr(target_total=TT)
+    res, counts = x.align(items, with_counts=True)
+    P = O.params(target_total=TT)
+    o = 0
+    for k, (t, q) in enumerate(items):
+        got = res[o:o + int(counts[k])]
+        o += int(counts[k])
+        d = x.debug_pair(t=t, q=q)
+        want, _ = O.align_pair(P, O.pair(t, q), offsets_in=d["offsets"])
+        assert parity.same_results(got, want, target_total=TT), k
+    x.close()
