@@ -11,7 +11,7 @@ constexpr int MAX_LOG2L = 15;    // FFT length 32768
 constexpr int MAX_SMEM_LOG2L = 14;  // longest FFT whose two transforms and channel sums fit one SM
 constexpr int NT_CORR = 512;     // threads of the correlation kernel
 constexpr int NT_SCAN = 128;     // threads of the scan kernel
-constexpr int OFF_CHUNK = 512;   // offsets staged per scan chunk
+constexpr int OFF_CHUNK = 256;   // offsets staged per scan chunk (sized for 7 scan CTAs per SM)
 constexpr int WINDOW = 46;       // DoOne window: m_minLen + 1 positions (CrossCorr.cc:701-705)
 constexpr int MIN_HITS = 19;     // ACGT windows pass when 100*hits > 1889 (CrossCorr.cc:675)
 

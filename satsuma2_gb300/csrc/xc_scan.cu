@@ -37,7 +37,7 @@ template <int LOG2L> struct ScanGeom {
   // Marked-block items of one pass-2 sub-range and the segment queue (4 bytes
   // each; item indices fit 12 bits).  The queue shares its bytes with the
   // chunk byte arrays, which only the byte-table path fills.
-  static constexpr int ICAP = 1536;   // items (8 bytes each: word, passing bits)
+  static constexpr int ICAP = 1280;   // items (8 bytes each: word, passing bits)
   static constexpr int QCAP = 2048;
   static constexpr size_t region = (size_t)QCAP * 4 > 2 * (size_t)N ? (size_t)QCAP * 4 : 2 * (size_t)N;
   static constexpr size_t bytes = region +
@@ -95,7 +95,7 @@ __device__ __forceinline__ void gc_prefix(const uint32_t* b0, const uint32_t* b1
 }
 
 template <int LOG2L>
-__global__ void __launch_bounds__(NT_SCAN, 6) scan_kernel(const ScanParams P) {
+__global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
   using Gm = ScanGeom<LOG2L>;
   constexpr int L = Gm::L, N = Gm::N, TW = Gm::TW, TWP = Gm::TWP, QPAD = Gm::QPAD, QWP = Gm::QWP;
   constexpr int ICAP = Gm::ICAP, QCAP = Gm::QCAP, NWARP = NT_SCAN / 32;
