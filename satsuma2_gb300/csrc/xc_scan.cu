@@ -125,11 +125,15 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
   const int pidx = P.first + blockIdx.x;
   const int strand = blockIdx.y;
   const int slot = pidx * 2 + strand;
+  // Small batches split each strand over gridDim.z CTAs: CTA z takes the
+  // rounds (and byte-table groups) z, z + split, ...; results then take their
+  // slot from the strand's counter in global memory, zeroed by the launcher.
+  const int split = gridDim.z, zi = blockIdx.z;
   const PairDesc D = P.pairs[pidx];
   const uint32_t pflags = P.pair_flags[pidx];
   const int cnt = P.off_cnt[slot];
   if ((pflags & PF_INVALID) || cnt <= 0) {
-    if (tid == 0) P.res_cnt[slot] = 0;
+    if (tid == 0 && split == 1) P.res_cnt[slot] = 0;
     return;
   }
   const int T = D.tlen, Q = D.qlen;
@@ -292,7 +296,7 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
     if (prob < P.min_prob) return;
     DevResult rec;
     rec.key = key; rec.tstart = s0; rec.qstart = s0 + pos; rec.len = len; rec.prob = prob; rec.ident = ident;
-    const int k = atomicAdd(&s_res, 1);
+    const int k = split == 1 ? atomicAdd(&s_res, 1) : atomicAdd(&P.res_cnt[slot], 1);
     if (k < P.slots) {
       P.res[(size_t)slot * P.slots + k] = rec;
     } else {
@@ -307,6 +311,7 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
     }
   };
 
+  int rbase = 0, gbase = 0;   // rounds and byte-table groups of the earlier chunks
   for (int c0 = 0; c0 < cnt; c0 += OFF_CHUNK) {
     const int nc = min(OFF_CHUNK, cnt - c0);
     if (tid < 64) s_hist[tid] = 0;
@@ -339,9 +344,10 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
 
     if (generic) {
       // A warp takes 32 consecutive (similar-length) diagonals at a time.
+      const int gfirst = ((zi - gbase) % split + split) % split;   // first group of this CTA
       for (;;) {
         int k0 = 0;
-        if (lane == 0) k0 = atomicAdd(&s_next, 32);
+        if (lane == 0) k0 = 32 * (gfirst + split * atomicAdd(&s_next, 1));
         k0 = __shfl_sync(FULL, k0, 0);
         if (k0 >= nc) break;
         if (k0 + lane < nc) {
@@ -372,6 +378,7 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
         }
         __syncwarp();
       }
+      gbase += (nc + 31) / 32;
       __syncthreads();
       continue;
     }
@@ -380,7 +387,9 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
     // when it holds >= 19 equal bases.  Check positions c run from i0+46 to
     // iend-1; window(c) = [c-45, c]; a segment is a maximal run of passing
     // checks [a..b], emitted as [a-45, b+1) (or [a-45, iend) at the end).
-    for (int r0 = 0; r0 < nc; r0 += NT_SCAN) {
+    const int rfirst = ((zi - rbase) % split + split) % split;   // first round of this CTA
+    rbase += (nc + NT_SCAN - 1) / NT_SCAN;
+    for (int r0 = NT_SCAN * rfirst; r0 < nc; r0 += NT_SCAN * split) {
       const int k = r0 + tid;
       const bool have = k < nc;
       const int pos = have ? offs[order[k]] - N : 0;
@@ -609,7 +618,7 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
       __syncthreads();
     }
   }
-  if (tid == 0) P.res_cnt[slot] = s_res;
+  if (tid == 0 && split == 1) P.res_cnt[slot] = s_res;
 }
 
 // ---------------------------------------------------------------------------
@@ -700,7 +709,19 @@ cudaError_t prepare_scan_kernels() {
 
 cudaError_t launch_scan(int log2L, const ScanParams& p, int npairs, cudaStream_t s) {
   if (npairs <= 0) return cudaSuccess;
-  const dim3 grid(npairs, 2);
+  // Fewer strands than a wave of CTAs (7 per SM): split them, up to 4 ways.
+  static const int sms = [] {
+    int dev = 0, n = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n;
+  }();
+  int split = 1;
+  while (split < 4 && 2 * npairs * split * 2 <= 7 * sms) split *= 2;
+  if (split > 1) {
+    const cudaError_t e = cudaMemsetAsync(p.res_cnt + 2 * (size_t)p.first, 0, 2 * (size_t)npairs * sizeof(int), s);
+    if (e != cudaSuccess) return e;
+  }
+  const dim3 grid(npairs, 2, split);
   const size_t sm = scan_smem_bytes(log2L);
   switch (log2L) {
     case 10: scan_kernel<10><<<grid, NT_SCAN, sm, s>>>(p); break;
