@@ -71,7 +71,7 @@ struct Server {
   int device = 0;
   size_t max_batch = 4096;
   size_t min_batch = 1024;   // while the GPU is busy, wait for this many pairs ...
-  double max_wait_ms = 2.0;  // ... or for the oldest request to wait this long
+  double max_wait_ms = 1.0;  // ... or for the oldest request to wait this long
   size_t res_per_pair = 8;   // read-back buffer estimate (records per pair)
 };
 
@@ -135,9 +135,9 @@ static void scheduler(Server* S) {
       if (cudaEventQuery(oldest->ev) != cudaSuccess) break;
       complete_slot(S, *oldest);
     }
-    // 2. fill a free slot from the queue: at once when the GPU is idle,
-    //    otherwise once a batch worth launching has gathered (or the oldest
-    //    request has waited long enough)
+    // 2. fill a free slot from the queue: at once while at most one batch
+    //    is in flight, otherwise once a batch worth launching has gathered
+    //    (or the oldest request has waited long enough)
     Slot* free_slot = nullptr;
     int busy = 0;
     for (auto& sl : S->slots) {
@@ -148,7 +148,7 @@ static void scheduler(Server* S) {
     if (free_slot) {
       std::unique_lock<std::mutex> lk(S->mu);
       if (S->stop && S->queue.empty() && busy == 0) return;
-      if (busy > 0 && !S->queue.empty() && S->queued_pairs < S->min_batch &&
+      if (busy >= 2 && !S->queue.empty() && S->queued_pairs < S->min_batch &&
           std::chrono::duration<double, std::milli>(Clock::now() - S->queue.front()->t_submit).count() <
               S->max_wait_ms) {
         holding = true;
