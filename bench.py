@@ -172,8 +172,10 @@ def run_reference(args):
     for _ in range(args.warmup):
         pass
     info = None
+    # each step a bounded sample; the whole run stays near a minute and a half
+    per_step = max(2.0, min(args.ref_seconds, 90.0 / max(1, args.steps)))
     for _ in range(args.steps):
-        info = cpu_baseline(items, seconds=args.ref_seconds)
+        info = cpu_baseline(items, seconds=per_step)
         vals.append(info["value"])
     v = float(np.mean(vals))
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
