@@ -46,9 +46,25 @@ TARGET_TOTAL = 4096.0 * 4096   # sum of the target lengths of the workload
 L2_FLUSH_BYTES = 512 << 20
 
 
-def workload():
+def workload(rank=0):
+    """Rank r's shard: its own seeded batch (rank 0 is the single-GPU workload)."""
     from satsuma2_gb300 import workloads as W
-    return W.uniform_batch(N_PAIRS, seed=SEED)
+    return W.uniform_batch(N_PAIRS, seed=shard_seed(rank))
+
+
+def shard_seed(rank):
+    return SEED + rank
+
+
+def max_over_ranks(v, world):
+    """The largest of each rank's v (the slowest rank's time); v itself at N=1."""
+    if world <= 1:
+        return float(v)
+    import torch
+    dev = "cuda" if torch.distributed.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
 
 
 def dist_env():
@@ -282,7 +298,7 @@ def run_ours(args):
         torch.distributed.init_process_group("nccl")
     torch.cuda.set_device(local)
     build.build()
-    items = workload()
+    items = workload(rank)
     x = sg.XCorr(target_total=TARGET_TOTAL, device=local)
     # A dedicated stream: the library captures its launches into a CUDA graph,
     # which the legacy default stream does not allow.
@@ -313,11 +329,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    ms = float(np.mean(step_ms))
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(float(np.mean(step_ms)), world)
     value = N_PAIRS * world / (ms / 1000.0)
     launches = args.steps * batch.launches()
     res_dev = batch.results()
@@ -337,7 +349,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         e2e_t.append(time.perf_counter() - t0)
     h2d, d2h = x.transfer_stats()
-    e2e_val = N_PAIRS * world / float(np.mean(e2e_t))
+    e2e_val = N_PAIRS * world / max_over_ranks(float(np.mean(e2e_t)), world)
     same = n_out.value == len(res_dev)
 
     # ---- plain: one pair per call ----
