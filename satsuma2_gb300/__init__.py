@@ -173,22 +173,26 @@ class XCorr:
             res = out[:n_out.value].copy()
             return (res, counts) if with_counts else res
 
-    def debug_pair(self, t, q, seg_cap=1 << 16, **kw):
-        """Stage outputs of one pair: signals, xc, offsets, raw segments per strand."""
+    def debug_pair(self, t, q, seg_cap=1 << 16, signals=True, **kw):
+        """Stage outputs of one pair: signals, xc, offsets, raw segments per
+        strand.  With signals=False no signals are written, and an A/C/G/T
+        pair at FFT 8192 runs on the both-strands correlation kernel, as in
+        xc_align_pairs; signal output runs it one CTA per strand."""
         arr, keep = make_pairs([dict(t=t, q=q, **kw)])
         Lmax = MAX_FFT_LEN
-        sig = np.zeros(2 * 8 * Lmax, np.float32)
+        sig = np.zeros(2 * 8 * Lmax if signals else 1, np.float32)
         xcv = np.zeros(2 * Lmax, np.float32)
         offs = np.zeros(2 * Lmax, np.int32)
         noffs = np.zeros(2, np.int32)
         segs = np.zeros(2 * seg_cap * 3, np.int32)
         nsegs = np.zeros(2, np.int32)
         L = ctypes.c_int()
-        _check(self.lib.xc_debug_pair(self.ctx, arr, sig.ctypes.data, xcv.ctypes.data, offs.ctypes.data,
+        _check(self.lib.xc_debug_pair(self.ctx, arr, sig.ctypes.data if signals else None, xcv.ctypes.data,
+                                      offs.ctypes.data,
                                       noffs.ctypes.data, segs.ctypes.data, nsegs.ctypes.data, seg_cap,
                                       ctypes.byref(L)), "xc_debug_pair")
         L = L.value
-        sig = sig[:2 * 8 * L].reshape(2, 2, 4, L)
+        sig = sig[:2 * 8 * L].reshape(2, 2, 4, L) if signals else None
         return {
             "L": L,
             "signals": sig,

@@ -17,6 +17,9 @@
 // semantics cited per step; paths are relative to the satsuma2 source tree.
 #include "xc_device.cuh"
 
+#include <algorithm>
+#include <type_traits>
+
 namespace xc {
 
 size_t corr_smem_bytes(int log2L) {
@@ -29,8 +32,156 @@ size_t corr_smem_bytes(int log2L) {
          + 2 * 256 * sizeof(float2);                                     // per-window channel values
 }
 
+// ---------------------------------------------------------------------------
+// Steps shared by both correlation kernels
+// ---------------------------------------------------------------------------
+
+// Step 4: the half-length complex array of the Hermitian sum S (bins
+// k = 0..N of the L-point spectrum, N = L/2, given by S(k)), ready for the
+// N-point inverse: Z(k) = E(k) + i O(k), E = (S(k) + conj S(N-k))/2,
+// O = (S(k) - conj S(N-k)) conj(W_L^k)/2; the inverse then holds
+// z[m] = r[2m] + i r[2m+1].  Threads t < NT_CORR.
+template <int LOG2L, class SF>
+__device__ __forceinline__ void hermitian_pack(float2* __restrict__ buf, const SF& S, const float2* twLh,
+                                               const float2* twLl, int t) {
+  constexpr int N = 1 << (LOG2L - 1);
+  constexpr int LOG2N = LOG2L - 1;
+  const int la = lp<LOG2N>(t);
+  const int lb = lp<LOG2N>((NT_CORR - t) & (NT_CORR - 1));
+#pragma unroll
+  for (int it = 0; it <= N / (2 * NT_CORR); it++) {
+    const int k = t + NT_CORR * it;
+    if (k > N / 2) break;
+    const float2 Sk = S(k);
+    const float2 Sn = S(N - k);
+    {
+      const float2 Ev = make_float2(0.5f * (Sk.x + Sn.x), 0.5f * (Sk.y - Sn.y));
+      const float2 Dv = make_float2(0.5f * (Sk.x - Sn.x), 0.5f * (Sk.y + Sn.y));
+      const float2 Ov = cmulc(Dv, tw2(twLh, twLl, k));
+      buf[la ^ lp<LOG2N>(NT_CORR * it)] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
+    }
+    if (k != 0 && k != N / 2) {
+      // N-k = (N - NT_CORR(it+1)) | (NT_CORR - t) for t >= 1
+      const int pb = t ? (lb ^ lp<LOG2N>(N - NT_CORR * (it + 1))) : lp<LOG2N>(N - NT_CORR * it);
+      const float2 Ev = make_float2(0.5f * (Sn.x + Sk.x), 0.5f * (Sn.y - Sk.y));
+      const float2 Dv = make_float2(0.5f * (Sn.x - Sk.x), 0.5f * (Sn.y + Sk.y));
+      const float2 Ov = cmulc(Dv, tw2(twLh, twLl, N - k));
+      buf[pb] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
+    }
+  }
+}
+
+// Step 5: FindTop (SeqAnalyzer::FindTop, CrossCorr.cc:878-944) over the
+// inverse in buf, for one strand: xc[i] = r[(i + N) mod L] / N; envelope
+// over 256-sample blocks when L/256 > 8; keep i with xc[i] > env*cutoff + 1
+// in increasing i.  Threads t < NT_CORR; warp w of them owns the contiguous
+// range [w*L/16, (w+1)*L/16), lanes stride by one.  Every thread of the CTA
+// calls it (two CTA barriers).
 template <int LOG2L>
-__global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(const CorrParams P) {
+__device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, uint32_t off_base, int pidx,
+                                         int strand, const float2* __restrict__ buf, int t, int* s_warp) {
+  constexpr int L = 1 << LOG2L;
+  constexpr int N = L >> 1;
+  const int lane = t & 31, warp = t >> 5;
+  constexpr int PER_WARP = L / (NT_CORR / 32);
+  constexpr int ITER = PER_WARP / 32;
+  const int wbase = warp * PER_WARP;
+  const float scale = 1.0f / (float)N;
+  auto xval = [&](int i) -> float {
+    const int n = (i + N) & (L - 1);
+    const float2 z = buf[swz(n >> 1)];
+    return ((n & 1) ? z.y : z.x) * scale;
+  };
+  // Up to L = 8192 a lane's 16 values stay in registers across the three
+  // passes (envelope, count, compaction); longer transforms re-read them.
+  constexpr bool KEEP = ITER <= 16;
+  float xs[KEEP ? ITER : 1];
+  if constexpr (KEEP) {
+#pragma unroll
+    for (int e = 0; e < ITER; e++) xs[e] = xval(wbase + e * 32 + lane);
+  }
+  auto xat = [&](int e) -> float {
+    if constexpr (KEEP) return xs[e];
+    else return xval(wbase + e * 32 + lane);
+  };
+  float thrb[PER_WARP >= 256 ? PER_WARP / 256 : 1];
+  if constexpr (L / 256 > 8) {
+    const float cut = (float)((flags & PF_FAST) ? P.cutoff_fast : P.cutoff);
+#pragma unroll
+    for (int bb = 0; bb < PER_WARP / 256; bb++) {
+      // squares are float products as in the reference; compensated FP32
+      // sum per lane, pairwise across the warp
+      float s = 0.f, comp = 0.f;
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const float x = xat(bb * 8 + e);
+        const float v = __fmul_rn(x, x);
+        const float y = __fsub_rn(v, comp);
+        const float t2 = __fadd_rn(s, y);
+        comp = __fsub_rn(__fsub_rn(t2, s), y);
+        s = t2;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        s = __fadd_rn(s, __shfl_xor_sync(0xffffffffu, s, o));
+        comp = __fadd_rn(comp, __shfl_xor_sync(0xffffffffu, comp, o));
+      }
+      // env = sqrt(sum / 256) and the threshold env * cutoff + 1 in FP32.
+      // The reference forms them in double from its own FP32 xc; ours
+      // differ from them by a few FP32 ulps, the order of the difference
+      // between the two FP32 correlations themselves, so decisions can
+      // only part within that band around the threshold.  (FP64 would cost
+      // tens of cycles per warp instruction here.)
+      const float env = __fsqrt_rn(__fmul_rn(__fsub_rn(s, comp), 0.00390625f));
+      thrb[bb] = __fadd_rn(__fmul_rn(env, cut), 1.0f);
+    }
+  } else {
+    thrb[0] = 1.0f;
+  }
+  int wcount = 0;
+  unsigned msk[KEEP ? ITER : 1];
+#pragma unroll(KEEP ? ITER : 4)
+  for (int e = 0; e < ITER; e++) {
+    const int i = wbase + e * 32 + lane;
+    const float x = xat(e);
+    const unsigned m = __ballot_sync(0xffffffffu, x > thrb[(L / 256 > 8) ? (e >> 3) : 0]);
+    if constexpr (KEEP) msk[e] = m;
+    wcount += __popc(m);
+    if (P.dbg_xc) P.dbg_xc[(size_t)(pidx * 2 + strand) * L + i] = x;
+  }
+  if (lane == 0) s_warp[warp] = wcount;
+  __syncthreads();
+  if (warp == 0) {
+    const int v = lane < NT_CORR / 32 ? s_warp[lane] : 0;
+    int w = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += u;
+    }
+    if (lane < NT_CORR / 32) s_warp[lane] = w - v;
+    if (lane == NT_CORR / 32 - 1) P.off_cnt[pidx * 2 + strand] = w;
+  }
+  __syncthreads();
+  int run = s_warp[warp];
+  int* out = P.off_list + off_base + (size_t)strand * L;
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll(KEEP ? ITER : 4)
+  for (int e = 0; e < ITER; e++) {
+    const int i = wbase + e * 32 + lane;
+    unsigned m;
+    if constexpr (KEEP) m = msk[e];
+    else m = __ballot_sync(0xffffffffu, xat(e) > thrb[(L / 256 > 8) ? (e >> 3) : 0]);
+    if ((m >> lane) & 1u) out[run + __popc(m & lt)] = i;
+    run += __popc(m);
+  }
+}
+
+// One (pair, strand) on the CTA's NT_CORR threads; slot indexes the global
+// channel-sum scratch at L = 32768.
+template <int LOG2L>
+__device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int slot, int strand,
+                                            unsigned char* smem) {
   constexpr int L = 1 << LOG2L;
   constexpr int N = L >> 1;
   constexpr int LOG2N = LOG2L - 1;
@@ -39,7 +190,6 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
   constexpr int NH = N / 64;
   constexpr bool SEQ = LOG2L > MAX_SMEM_LOG2L;   // one transform buffer, channel sums in global memory
 
-  extern __shared__ __align__(16) unsigned char smem[];
   float2* bufE = reinterpret_cast<float2*>(smem);
   float2* bufO = bufE + N;              // (not SEQ)
   float2* accE = bufO + N;              // channel sum at bins 2m, m = 0..N/2 (N/2: Nyquist, real)
@@ -60,9 +210,7 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
   __shared__ int s_warp[NT_CORR / 32];
 
   const int tid = threadIdx.x;
-  const int lane = tid & 31, warp = tid >> 5;
-  const int pidx = P.first + blockIdx.x;
-  const int strand = blockIdx.y;
+  const int lane = tid & 31;
   const PairDesc D = P.pairs[pidx];
   const int T = D.tlen, Q = D.qlen;
   const uint8_t* __restrict__ gt = P.pool + D.t_off;
@@ -115,7 +263,7 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
   float2* gaccE = nullptr;   // SEQ: this strand's channel sums in global memory
   float2* gaccO = nullptr;
   if constexpr (SEQ) {
-    gaccE = P.acc + (size_t)(blockIdx.x * 2 + strand) * acc_stride(LOG2L);
+    gaccE = P.acc + (size_t)(slot * 2 + strand) * acc_stride(LOG2L);
     gaccO = gaccE + (N / 2 + 8);
   }
 
@@ -377,130 +525,316 @@ __global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(co
     if constexpr (SEQ) return (k & 1) ? gaccO[k >> 1] : gaccE[k >> 1];
     return (k & 1) ? accO[k >> 1] : accE[k >> 1];
   };
-  {
-    const int la = lp<LOG2N>(tid);
-    const int lb = lp<LOG2N>((NT_CORR - tid) & (NT_CORR - 1));
-#pragma unroll
-    for (int it = 0; it <= N / (2 * NT_CORR); it++) {
-      const int k = tid + NT_CORR * it;
-      if (k > N / 2) break;
-      const float2 Sk = S(k);
-      const float2 Sn = S(N - k);
-      {
-        const float2 Ev = make_float2(0.5f * (Sk.x + Sn.x), 0.5f * (Sk.y - Sn.y));
-        const float2 Dv = make_float2(0.5f * (Sk.x - Sn.x), 0.5f * (Sk.y + Sn.y));
-        const float2 Ov = cmulc(Dv, tw2(twLh, twLl, k));
-        bufE[la ^ lp<LOG2N>(NT_CORR * it)] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
-      }
-      if (k != 0 && k != N / 2) {
-        // N-k = (N - NT_CORR(it+1)) | (NT_CORR - tid) for tid >= 1
-        const int pb = tid ? (lb ^ lp<LOG2N>(N - NT_CORR * (it + 1))) : lp<LOG2N>(N - NT_CORR * it);
-        const float2 Ev = make_float2(0.5f * (Sn.x + Sk.x), 0.5f * (Sn.y - Sk.y));
-        const float2 Dv = make_float2(0.5f * (Sn.x - Sk.x), 0.5f * (Sn.y + Sk.y));
-        const float2 Ov = cmulc(Dv, tw2(twLh, twLl, N - k));
-        bufE[pb] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
-      }
-    }
-  }
+  hermitian_pack<LOG2L>(bufE, S, twLh, twLl, tid);
   __syncthreads();
   fft_inverse<LOG2N>(bufE, twNh, twNl, tid, NT_CORR);
 
-  // ---- 5. FindTop (SeqAnalyzer::FindTop, CrossCorr.cc:878-944): xc[i] =
-  //      r[(i + N) mod L] / N; envelope over 256-sample blocks when L/256 > 8;
-  //      keep i with xc[i] > env*cutoff + 1 in increasing i.  Warp w owns the
-  //      contiguous range [w*L/16, (w+1)*L/16), lanes stride by one. ----
-  constexpr int PER_WARP = L / (NT_CORR / 32);
-  constexpr int ITER = PER_WARP / 32;
-  const int wbase = warp * PER_WARP;
-  const float scale = 1.0f / (float)N;
-  auto xval = [&](int i) -> float {
-    const int n = (i + N) & (L - 1);
-    const float2 z = bufE[swz(n >> 1)];
-    return ((n & 1) ? z.y : z.x) * scale;
-  };
-  // Up to L = 8192 a lane's 16 values stay in registers across the three
-  // passes (envelope, count, compaction); longer transforms re-read them.
-  constexpr bool KEEP = ITER <= 16;
-  float xs[KEEP ? ITER : 1];
-  if constexpr (KEEP) {
-#pragma unroll
-    for (int e = 0; e < ITER; e++) xs[e] = xval(wbase + e * 32 + lane);
+  // ---- 5. FindTop ----
+  find_top<LOG2L>(P, D.flags, D.off_base, pidx, strand, bufE, tid, s_warp);
+}
+
+template <int LOG2L>
+__global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(const CorrParams P) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  // One pair per CTA column, or (fb_list) the pairs corr_pair_kernel handed
+  // back, CTA columns striding over the list.
+  const int cnt = P.fb_list ? *P.fb_cnt : (int)blockIdx.x + 1;
+  for (int j = blockIdx.x; j < cnt; j += gridDim.x) {
+    corr_strand<LOG2L>(P, P.fb_list ? P.fb_list[j] : P.first + j, j, blockIdx.y, smem);
+    __syncthreads();
   }
-  auto xat = [&](int e) -> float {
-    if constexpr (KEEP) return xs[e];
-    else return xval(wbase + e * 32 + lane);
-  };
-  float thrb[PER_WARP >= 256 ? PER_WARP / 256 : 1];
-  if constexpr (L / 256 > 8) {
-    const float cut = (float)((D.flags & PF_FAST) ? P.cutoff_fast : P.cutoff);
-#pragma unroll
-    for (int bb = 0; bb < PER_WARP / 256; bb++) {
-      // squares are float products as in the reference; compensated FP32
-      // sum per lane, pairwise across the warp
-      float s = 0.f, comp = 0.f;
-#pragma unroll
-      for (int e = 0; e < 8; e++) {
-        const float x = xat(bb * 8 + e);
-        const float v = __fmul_rn(x, x);
-        const float y = __fsub_rn(v, comp);
-        const float t2 = __fadd_rn(s, y);
-        comp = __fsub_rn(__fsub_rn(t2, s), y);
-        s = t2;
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        s = __fadd_rn(s, __shfl_xor_sync(0xffffffffu, s, o));
-        comp = __fadd_rn(comp, __shfl_xor_sync(0xffffffffu, comp, o));
-      }
-      // env = sqrt(sum / 256) and the threshold env * cutoff + 1 in FP32.
-      // The reference forms them in double from its own FP32 xc; ours
-      // differ from them by a few FP32 ulps, the order of the difference
-      // between the two FP32 correlations themselves, so decisions can
-      // only part within that band around the threshold.  (FP64 would cost
-      // tens of cycles per warp instruction here.)
-      const float env = __fsqrt_rn(__fmul_rn(__fsub_rn(s, comp), 0.00390625f));
-      thrb[bb] = __fadd_rn(__fmul_rn(env, cut), 1.0f);
+}
+
+size_t corr_pair_smem_bytes(int log2L) {
+  const size_t N = (size_t)1 << (log2L - 1);
+  const size_t NH = N / 64;
+  return (4 * N + 2 * (N + 8) + 2 * (NH + 64)) * sizeof(float2)   // transforms, two sums, twiddles
+         + 2 * N                                                    // target and query bytes
+         + 2 * 256 * sizeof(float)                                  // entropy weight per window
+         + 4 * 256 * sizeof(float2);                                // per-window channel values
+}
+
+// corr_pair_kernel<log2 L>: one CTA of 1024 threads per chunk pair, both
+// strands from one set of spectra.  For A/C/G/T chunks the reverse strand's
+// query signal in channel c is the forward query's signal in the complement
+// channel comp(c), reversed in time: the per-channel means are equal (the
+// same base counts), and when the query length is a multiple of the entropy
+// window (or below 1024, weight 1) every reverse window holds the complement
+// bases of one forward window, whose weight the host table gives identically
+// (the host checks the table's complement symmetry before enabling this
+// kernel).  With q_r[n] = q_comp[Q-1-n], Q_r(k) = W_L^((Q-1)k) conj(Q_comp(k)),
+// so the reverse strand's product sum is
+//   sum_c conj(T_c) Q_r,c = W_L^((Q-1)k) conj(R(k)),  R = sum_c T_c Q_comp(c).
+// Channels go in two stages, (A, T) then (C, G): z = t_c0 + i t_c1 and
+// w = q_c0 + i q_c1, each as its even-bin and odd-bin N-point transform, the
+// four on 256 threads each; the per-bin step separates T_c0, T_c1, Q_c0,
+// Q_c1 and adds conj(T_c)Q_c to the forward sum and T_c0 Q_c1 + T_c1 Q_c0
+// to R.  Eight N-point transforms and two inverses per pair, where two
+// corr_kernel CTAs take sixteen and two.  Pairs outside that case (a byte
+// other than A/C/G/T, a ragged query window, debug signal output) go on
+// P.fb_list for corr_kernel; pairs with a byte >= 128 are rejected here.
+template <int LOG2L>
+__global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams P) {
+  constexpr int L = 1 << LOG2L;
+  constexpr int N = L >> 1;
+  constexpr int LOG2N = LOG2L - 1;
+  constexpr int WIN = L / 512;
+  constexpr int NWIN = 256;
+  constexpr int NH = N / 64;
+  static_assert(N % 1024 == 0, "two 512-thread halves over N/2 bins");
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* ZE = reinterpret_cast<float2*>(smem);   // z = t_c0 + i t_c1, even-bin transform
+  float2* ZO = ZE + N;                            // z * W_L^n, odd-bin transform
+  float2* WE = ZO + N;                            // w = q_c0 + i q_c1
+  float2* WO = WE + N;
+  float2* aFE = WO + N;                           // forward-strand sum, bins 2m, m <= N/2
+  float2* aFO = aFE + (N / 2 + 8);                // bins 2m+1
+  float2* aRE = aFO + N / 2;                      // R, bins 2m (m < N/2)
+  float2* aRO = aRE + (N / 2 + 8);                // R, bins 2m+1
+  float2* twNh = aRO + N / 2;
+  float2* twNl = twNh + NH;
+  float2* twLh = twNl + 64;
+  float2* twLl = twLh + NH;
+  uint8_t* st = reinterpret_cast<uint8_t*>(twLl + 64);
+  uint8_t* sq = st + N;
+  float* Et = reinterpret_cast<float*>(sq + N);
+  float* Eq = Et + NWIN;
+  float2* vv = reinterpret_cast<float2*>(Eq + NWIN);   // [t c0, t c1, q c0, q c1][window]
+  __shared__ int s_cnt4[8];
+  __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
+  __shared__ int s_warp[2][NT_CORR / 32];
+
+  const int tid = threadIdx.x;
+  const int half = tid >> 9;       // steps 3b-5: 0 target / forward strand, 1 query / reverse strand
+  const int ht = tid & 511;
+  const int pidx = P.first + blockIdx.x;
+  const int T = P.pairs[pidx].tlen, Q = P.pairs[pidx].qlen;
+  const uint8_t* __restrict__ gt = P.pool + P.pairs[pidx].t_off;
+  const uint8_t* __restrict__ gq = P.pool + P.pairs[pidx].q_off;
+
+  // ---- 1. chunk bytes, forward strand only ----
+  int high = 0, nonacgt = 0;
+  for (int i = tid; i < N; i += NT_PAIR) {
+    unsigned b = 0, c = 0;
+    if (i < T) {
+      b = gt[i];
+      high |= b >> 7;
+      nonacgt |= !is_acgt(b);
     }
+    if (i < Q) {
+      c = gq[i];
+      high |= c >> 7;
+      nonacgt |= !is_acgt(c);
+    }
+    st[i] = (uint8_t)b;
+    sq[i] = (uint8_t)c;
+  }
+  for (int i = tid; i < NH; i += NT_PAIR) {
+    twNh[i] = P.tab.twN_hi[i];
+    twLh[i] = P.tab.twL_hi[i];
+  }
+  if (tid < 64) {
+    twNl[tid] = P.tab.twN_lo[tid];
+    twLl[tid] = P.tab.twL_lo[tid];
+  }
+  if (tid < 8) s_cnt4[tid] = 0;
+  const int any_high = __syncthreads_or(high);
+  const int generic = __syncthreads_or(nonacgt);
+  if (any_high) {
+    if (tid == 0) {
+      P.off_cnt[pidx * 2] = 0;
+      P.off_cnt[pidx * 2 + 1] = 0;
+      P.pair_flags[pidx] = PF_INVALID;
+    }
+    return;
+  }
+  if (generic || (Q >= 1024 && Q % WIN != 0) || P.dbg_sig) {
+    if (tid == 0) P.fb_list[atomicAdd(P.fb_cnt, 1)] = pidx;
+    return;
+  }
+  if (tid == 0) P.pair_flags[pidx] = P.pairs[pidx].flags & PF_FAST;
+  for (int i = tid; i < 2 * N + 16; i += NT_PAIR) aFE[i] = make_float2(0.f, 0.f);   // both sums
+
+  // ---- 2a. entropy weight per window (CCSignal::ComputeEntropy,
+  //      CrossCorr.cc:35-93), A/C/G/T only: threads 0..255 target windows,
+  //      256..511 query windows ----
+  if (tid < 512) {
+    const int which = tid >> 8, w = tid & 255;
+    const uint8_t* s = which ? sq : st;
+    const int len = which ? Q : T;
+    float E = 0.f;
+    if (len < 1024) {
+      E = 1.f;
+    } else if (w * WIN + WIN <= len) {
+      const int i0 = w * WIN;
+      uint32_t cnt = 0;
+      for (int j = 0; j < WIN; j++) cnt += 1u << (8 * code_of(s[i0 + j]));
+      const int a = cnt & 255u, c = (cnt >> 8) & 255u, g = (cnt >> 16) & 255u;
+      E = __ldg(&P.tab.ent_acgt[(a * (WIN + 1) + c) * (WIN + 1) + g]);
+    } else if (w * WIN < len) {
+      const int i0 = w * WIN;
+      const int k = len - i0;
+      int a4 = 0, c4 = 0, g4 = 0, t4 = 0;
+      for (int j = 0; j < k; j++) {
+        const uchar4 q = c_w4q[s[i0 + j]];
+        a4 += q.x; c4 += q.y; g4 += q.z; t4 += q.w;
+      }
+      const double* et = P.tab.ent + k * (4 * WIN + 1);
+      const double sv =
+          __dadd_rn(__dadd_rn(__dadd_rn(__ldg(et + a4), __ldg(et + c4)), __ldg(et + g4)), __ldg(et + t4));
+      E = __double2float_rn(-sv);
+      if (E < 0.f) E = 0.f;
+    }
+    (which ? Eq : Et)[w] = E;
+  }
+
+  // ---- 2b. channel means (SeqToPCM, CrossCorr.cc:108-116): exact quarter-unit sums ----
+  {
+    uint32_t ct = 0, cq = 0;   // one 8-bit count field per base, at most N / 1024 each
+    for (int i = tid; i < N; i += NT_PAIR) {
+      if (i < T) ct += 1u << (8 * code_of(st[i]));
+      if (i < Q) cq += 1u << (8 * code_of(sq[i]));
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int vt = __reduce_add_sync(0xffffffffu, 4 * (int)((ct >> (8 * k)) & 255u));
+      const int vq = __reduce_add_sync(0xffffffffu, 4 * (int)((cq >> (8 * k)) & 255u));
+      if ((tid & 31) == 0) {
+        if (vt) atomicAdd(&s_cnt4[k], vt);
+        if (vq) atomicAdd(&s_cnt4[4 + k], vq);
+      }
+    }
+  }
+  __syncthreads();
+  if (tid < 8) {
+    const int len = (tid >> 2) ? Q : T;
+    const double off = len > 0 ? __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len) : 0.0;
+    s_wmo[0][tid] = __dsub_rn(0.0, off);
+    s_wmo[1][tid] = __dsub_rn(1.0, off);
+  }
+  __syncthreads();
+
+  // one stage per channel pair, the channels compile-time constants
+  auto stage = [&](auto C0, auto C1) {
+    constexpr int c0 = decltype(C0)::value, c1 = decltype(C1)::value;
+    // ---- 3a. per-window channel values float(entropy * (weight - mean))
+    //      (CrossCorr.cc:123), weight 0 or 1 ----
+    {
+      const int which = tid >> 8, w = tid & 255;
+      const int seq = which >> 1, ch = (which & 1) ? c1 : c0;
+      const double E = (double)(seq ? Eq : Et)[w];
+      float2 v;
+      v.x = __double2float_rn(__dmul_rn(E, s_wmo[0][seq * 4 + ch]));
+      v.y = __double2float_rn(__dmul_rn(E, s_wmo[1][seq * 4 + ch]));
+      vv[which * NWIN + w] = v;
+    }
+    __syncthreads();
+    // ---- 3b. z (threads 0..511) or w (512..1023) to its even buffer and
+    //      times W_L^n to its odd buffer, as corr_kernel builds its z ----
+    {
+      const uint8_t* src = half ? sq : st;
+      const int len = half ? Q : T;
+      const float2* va = vv + 2 * half * NWIN;
+      const float2* vb = va + NWIN;
+      float2* bE = half ? WE : ZE;
+      float2* bO = bE + N;
+      const int sl = swz(ht);
+#pragma unroll 4   // (full unrolling spills at 64 registers)
+      for (int it = 0; it < N / 512; it++) {
+        const int n = ht + 512 * it;
+        float x = 0.f, y = 0.f;
+        if (n < len) {
+          const int w = n / WIN;
+          const uint32_t code = code_of(src[n]);
+          const float2 a = va[w], b = vb[w];
+          x = code == (uint32_t)c0 ? a.y : a.x;
+          y = code == (uint32_t)c1 ? b.y : b.x;
+        }
+        const int sn = sl ^ swz(512 * it);   // ht and 512*it share no bit
+        bE[sn] = make_float2(x, y);
+        bO[sn] = cmul(make_float2(x, y), tw2(twLh, twLl, n));   // W_L^n, n < L/2
+      }
+    }
+    __syncthreads();
+    // ---- 3c. the four N-point transforms, 256 threads each ----
+    fft_forward<LOG2N>(ZE + (tid >> 8) * N, twNh, twNl, tid & 255, 256);
+    // ---- 3d. per-bin step (CrossCorrelation::DoOne, CrossCorr.cc:477-492):
+    //      bin 0 is the product of real values; bins N-1 and N keep the
+    //      targets' own values, which the reference's loop leaves
+    //      unmultiplied, for both strands.  Threads 0..511: even bins,
+    //      512..1023: odd bins. ----
+    auto split = [](float2 A, float2 B, float2& X, float2& Y) {
+      X = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
+      Y = make_float2(0.5f * (A.y + B.y), -0.5f * (A.x - B.x));
+    };
+    if (half == 0) {
+      const int la = lp<LOG2N>(ht);
+      const int lb = lp<LOG2N>((512 - ht) & 511);
+#pragma unroll
+      for (int it = 0; it <= N / 1024; it++) {
+        const int m = ht + 512 * it;
+        if (m > N / 2) break;
+        const int pa = la ^ lp<LOG2N>(512 * it);
+        // partner N-m = (N - 512(it+1)) | (512 - ht) for ht >= 1
+        const int pb = ht ? (lb ^ lp<LOG2N>(N - 512 * (it + 1))) : lp<LOG2N>((N - 512 * it) & (N - 1));
+        float2 t0, t1, q0, q1;
+        split(ZE[pa], ZE[pb], t0, t1);
+        split(WE[pa], WE[pb], q0, q1);
+        if (m == N / 2) {
+          aFE[m].x += t0.x + t1.x;
+        } else {
+          aFE[m] = cadd(aFE[m], cadd(cmulc(q0, t0), cmulc(q1, t1)));
+          aRE[m] = cadd(aRE[m], cadd(cmul(t0, q1), cmul(t1, q0)));
+        }
+      }
+    } else {
+      const int la = lp<LOG2N>(ht);
+#pragma unroll
+      for (int it = 0; it < N / 1024; it++) {
+        const int m = ht + 512 * it;
+        const int pa = la ^ lp<LOG2N>(512 * it);
+        const int pb = pa ^ lp<LOG2N>(N - 1);   // N-1-m = m ^ (N-1)
+        float2 t0, t1, q0, q1;
+        split(ZO[pa], ZO[pb], t0, t1);
+        split(WO[pa], WO[pb], q0, q1);
+        if (m == N / 2 - 1) {
+          aFO[m] = cadd(aFO[m], cadd(t0, t1));
+        } else {
+          aFO[m] = cadd(aFO[m], cadd(cmulc(q0, t0), cmulc(q1, t1)));
+          aRO[m] = cadd(aRO[m], cadd(cmul(t0, q1), cmul(t1, q0)));
+        }
+      }
+    }
+    __syncthreads();
+  };
+  stage(std::integral_constant<int, 0>(), std::integral_constant<int, 3>());   // A, T
+  stage(std::integral_constant<int, 1>(), std::integral_constant<int, 2>());   // C, G
+
+  // ---- 4. inverses: forward strand into ZE (threads 0..511), reverse strand
+  //      S_r(k) = W_L^((Q-1)k) conj(R(k)) into WE (512..1023); the two
+  //      target-only bins are the same for both strands ----
+  float2* buf = half ? WE : ZE;
+  if (half == 0) {
+    hermitian_pack<LOG2L>(ZE, [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; }, twLh, twLl,
+                          ht);
   } else {
-    thrb[0] = 1.0f;
-  }
-  int wcount = 0;
-  unsigned msk[KEEP ? ITER : 1];
-#pragma unroll(KEEP ? ITER : 4)
-  for (int e = 0; e < ITER; e++) {
-    const int i = wbase + e * 32 + lane;
-    const float x = xat(e);
-    const unsigned m = __ballot_sync(0xffffffffu, x > thrb[(L / 256 > 8) ? (e >> 3) : 0]);
-    if constexpr (KEEP) msk[e] = m;
-    wcount += __popc(m);
-    if (P.dbg_xc) P.dbg_xc[(size_t)(pidx * 2 + strand) * L + i] = x;
-  }
-  if (lane == 0) s_warp[warp] = wcount;
-  __syncthreads();
-  if (warp == 0) {
-    const int v = lane < NT_CORR / 32 ? s_warp[lane] : 0;
-    int w = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int u = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += u;
-    }
-    if (lane < NT_CORR / 32) s_warp[lane] = w - v;
-    if (lane == NT_CORR / 32 - 1) P.off_cnt[pidx * 2 + strand] = w;
+    hermitian_pack<LOG2L>(WE,
+                          [&](int k) -> float2 {
+                            if (k >= N - 1) return (k & 1) ? aFO[k >> 1] : aFE[k >> 1];
+                            const float2 r = (k & 1) ? aRO[k >> 1] : aRE[k >> 1];
+                            const int j = ((Q - 1) * k) & (L - 1);
+                            float2 w = tw2(twLh, twLl, j & (N - 1));   // W_L^j, j < L/2
+                            if (j & N) w = make_float2(-w.x, -w.y);   // W_L^(j + L/2) = -W_L^j
+                            return cmulc(w, r);
+                          },
+                          twLh, twLl, ht);
   }
   __syncthreads();
-  int run = s_warp[warp];
-  int* out = P.off_list + D.off_base + (size_t)strand * L;
-  const unsigned lt = (1u << lane) - 1u;
-#pragma unroll(KEEP ? ITER : 4)
-  for (int e = 0; e < ITER; e++) {
-    const int i = wbase + e * 32 + lane;
-    unsigned m;
-    if constexpr (KEEP) m = msk[e];
-    else m = __ballot_sync(0xffffffffu, xat(e) > thrb[(L / 256 > 8) ? (e >> 3) : 0]);
-    if ((m >> lane) & 1u) out[run + __popc(m & lt)] = i;
-    run += __popc(m);
-  }
+  fft_inverse<LOG2N>(buf, twNh, twNl, ht, NT_CORR);
+
+  // ---- 5. FindTop, one strand per half ----
+  find_top<LOG2L>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, half, buf, ht, s_warp[half]);
 }
 
 // ---------------------------------------------------------------------------
@@ -516,7 +850,9 @@ static cudaError_t set_corr_attrs() {
 }
 
 cudaError_t prepare_kernels() {
-  cudaError_t e;
+  cudaError_t e = cudaFuncSetAttribute(corr_pair_kernel<PAIR_LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)corr_pair_smem_bytes(PAIR_LOG2L));
+  if (e != cudaSuccess) return e;
   if ((e = set_corr_attrs<10>()) != cudaSuccess) return e;
   if ((e = set_corr_attrs<11>()) != cudaSuccess) return e;
   if ((e = set_corr_attrs<12>()) != cudaSuccess) return e;
@@ -528,8 +864,20 @@ cudaError_t prepare_kernels() {
 
 cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t s) {
   if (npairs <= 0) return cudaSuccess;
-  const dim3 grid(npairs, 2);
+  dim3 grid(npairs, 2);
   const size_t sm = corr_smem_bytes(log2L);
+  if (p.fb_list) {
+    // both strands per CTA, then corr_kernel over the pairs handed back:
+    // one wave of CTAs striding over the list (*fb_cnt starts at zero)
+    if (log2L != PAIR_LOG2L) return cudaErrorInvalidValue;
+    corr_pair_kernel<PAIR_LOG2L><<<npairs, NT_PAIR, corr_pair_smem_bytes(PAIR_LOG2L), s>>>(p);
+    static const int sms = [] {
+      int dev = 0, n = 152;
+      if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+      return n;
+    }();
+    grid.x = std::min(npairs, sms);
+  }
   switch (log2L) {
     case 10: corr_kernel<10><<<grid, NT_CORR, sm, s>>>(p); break;
     case 11: corr_kernel<11><<<grid, NT_CORR, sm, s>>>(p); break;

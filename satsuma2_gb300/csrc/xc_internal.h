@@ -9,7 +9,9 @@ namespace xc {
 constexpr int MIN_LOG2L = 10;    // FFT length 1024
 constexpr int MAX_LOG2L = 15;    // FFT length 32768
 constexpr int MAX_SMEM_LOG2L = 14;  // longest FFT whose two transforms and channel sums fit one SM
-constexpr int NT_CORR = 512;     // threads of the correlation kernel
+constexpr int NT_CORR = 512;     // threads of the correlation kernel (one pair strand)
+constexpr int NT_PAIR = 1024;    // threads of the both-strands correlation kernel
+constexpr int PAIR_LOG2L = 13;   // FFT length of the both-strands kernel (its buffers fill one SM)
 constexpr int NT_SCAN = 128;     // threads of the scan kernel
 constexpr int OFF_CHUNK = 256;   // offsets staged per scan chunk (sized for 7 scan CTAs per SM)
 constexpr int WINDOW = 46;       // DoOne window: m_minLen + 1 positions (CrossCorr.cc:701-705)
@@ -74,6 +76,8 @@ struct CorrParams {
   float* dbg_sig;           // optional: [pair*2+strand][2][4][L]
   float* dbg_xc;            // optional: [pair*2+strand][L]
   float2* acc;              // L > 2^MAX_SMEM_LOG2L: channel sums, [pair*2+strand][acc_stride(log2L)]
+  int* fb_list;             // log2L == PAIR_LOG2L: both-strands kernel first; the pairs it
+  int* fb_cnt;              //   hands back ([*fb_cnt], zeroed before) go to corr_kernel
 };
 
 // Global channel-sum scratch of one pair strand for FFT lengths beyond one
@@ -118,6 +122,7 @@ cudaError_t launch_finalize(const int* res_cnt, const DevResult* res, int slots,
 cudaError_t upload_constants(const unsigned char* rc256, const uchar4* w4q128,
                              const double* w4d /*4*128*/);
 size_t corr_smem_bytes(int log2L);
+size_t corr_pair_smem_bytes(int log2L);
 size_t scan_smem_bytes(int log2L);
 cudaError_t prepare_kernels();
 

@@ -9,6 +9,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <mutex>
@@ -126,6 +127,19 @@ static int build_tables(Ctx* c) {
           if (E < 0.f) E = 0.f;
           eacgt[((size_t)a * W1 + cc) * W1 + g] = E;
         }
+    if (lg == PAIR_LOG2L) {
+      // corr_pair_kernel takes a reverse-strand window (the complement bases
+      // of a forward window: t A, g C, c G, a T) at the forward window's weight
+      bool sym = true;
+      for (int a = 0; a <= win; a++)
+        for (int cc = 0; a + cc <= win; cc++)
+          for (int g = 0; a + cc + g <= win; g++) {
+            const int tt = win - a - cc - g;
+            sym = sym && eacgt[((size_t)a * W1 + cc) * W1 + g] == eacgt[((size_t)tt * W1 + g) * W1 + cc];
+          }
+      const char* env = getenv("SATSUMA2_GB300_PAIR_KERNEL");   // "0": one corr_kernel CTA per strand
+      c->pair_kernel = sym && !(env && env[0] == '0');
+    }
     DevTables& t = c->tab[lg];
     XC_CHECK(cudaMalloc(&t.tw, tw.size() * sizeof(float2)));
     XC_CHECK(cudaMalloc(&t.ent, ent.size() * sizeof(double)));
@@ -268,7 +282,7 @@ Batch::~Batch() {
     if (e) cudaEventDestroy(e);
   cudaFree(d_pool); cudaFree(d_desc); cudaFree(d_off); cudaFree(d_offcnt); cudaFree(d_flags);
   cudaFree(d_res); cudaFree(d_rescnt); cudaFree(d_ovf); cudaFree(d_misc); cudaFree(d_base);
-  cudaFree(d_dense); cudaFree(d_dbg); cudaFree(d_dbg_sig); cudaFree(d_dbg_xc); cudaFree(d_acc);
+  cudaFree(d_dense); cudaFree(d_dbg); cudaFree(d_dbg_sig); cudaFree(d_dbg_xc); cudaFree(d_acc); cudaFree(d_fb);
   cudaFreeHost(h_pool); cudaFreeHost(h_desc); cudaFreeHost(h_base); cudaFreeHost(h_dense);
   cudaFreeHost(h_misc); cudaFreeHost(h_ovf);
 }
@@ -338,6 +352,7 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   if ((r = dev_grow(b->d_rescnt, b->cap_rescnt, nslots)) != XC_OK) return r;
   if ((r = dev_grow(b->d_ovf, b->cap_ovf, (size_t)b->ovf_cap)) != XC_OK) return r;
   if ((r = dev_grow(b->d_misc, b->cap_misc, 4)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_fb, b->cap_fb, n)) != XC_OK) return r;
   if ((r = dev_grow(b->d_base, b->cap_base, nslots + 1)) != XC_OK) return r;
   if ((r = dev_grow(b->d_dense, b->cap_dense, nslots * slots)) != XC_OK) return r;
   size_t acc = 0;
@@ -415,6 +430,10 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     cp.dbg_sig = b->d_dbg_sig;
     cp.dbg_xc = b->d_dbg_xc;
     cp.acc = b->d_acc;
+    if (bk.log2L == PAIR_LOG2L && c->pair_kernel) {
+      cp.fb_list = b->d_fb;
+      cp.fb_cnt = b->d_misc + 3;   // zeroed above
+    }
     XC_CHECK(launch_corr(bk.log2L, cp, bk.count, s));
   }
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[1], s, cudaEventRecordExternal));
@@ -453,7 +472,11 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
   return XC_OK;
 }
 
-int batch_launch_count(const Batch* b) { return 2 * (int)b->buckets.size() + 2; }
+int batch_launch_count(const Ctx* c, const Batch* b) {
+  int n = 2 * (int)b->buckets.size() + 2;
+  for (const Bucket& bk : b->buckets) n += bk.log2L == PAIR_LOG2L && c->pair_kernel;   // pair kernel + hand-back
+  return n;
+}
 
 // Runs the batch; replays a captured CUDA graph when the batch is unchanged.
 int batch_run(Ctx* c, Batch* b, cudaStream_t s, bool use_graph, bool timed) {
@@ -796,7 +819,7 @@ int xc_batch_free(xc_ctx* c, xc_batch* b) {
 
 int xc_batch_launches(xc_ctx* c, xc_batch* b) {
   if (!c || !b) return XC_ERR_ARG;
-  return batch_launch_count(b);
+  return batch_launch_count(c, b);
 }
 
 int xc_batch_run_timed(xc_ctx* c, xc_batch* b, void* stream, float* stage_ms) {
@@ -832,8 +855,10 @@ int xc_debug_pair(xc_ctx* c, const xc_pair* pair, float* sig, float* xcv, int* o
   if (fft_len_out) *fft_len_out = L;
   b.dbg_cap = 1 << 20;
   XC_CHECK(cudaMalloc(&b.d_dbg, (size_t)b.dbg_cap * sizeof(DbgSeg)));
-  XC_CHECK(cudaMalloc(&b.d_dbg_sig, (size_t)2 * 8 * L * sizeof(float)));
-  XC_CHECK(cudaMemset(b.d_dbg_sig, 0, (size_t)2 * 8 * L * sizeof(float)));
+  if (sig) {   // signal output runs the pair on corr_kernel, one CTA per strand
+    XC_CHECK(cudaMalloc(&b.d_dbg_sig, (size_t)2 * 8 * L * sizeof(float)));
+    XC_CHECK(cudaMemset(b.d_dbg_sig, 0, (size_t)2 * 8 * L * sizeof(float)));
+  }
   XC_CHECK(cudaMalloc(&b.d_dbg_xc, (size_t)2 * L * sizeof(float)));
   if ((r = batch_run(c, &b, c->stream, false)) != XC_OK) return r;
   XC_CHECK(cudaStreamSynchronize(c->stream));

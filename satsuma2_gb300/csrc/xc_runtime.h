@@ -41,6 +41,8 @@ struct Batch {
   int* d_rescnt = nullptr;        size_t cap_rescnt = 0;
   DevResultX* d_ovf = nullptr;    size_t cap_ovf = 0;
   int* d_misc = nullptr;          size_t cap_misc = 0;   // [0] ovf count [1] err [2] dbg count
+                                                         // [3] pairs corr_pair_kernel handed back
+  int* d_fb = nullptr;            size_t cap_fb = 0;     // those pairs' indices
   int* d_base = nullptr;          size_t cap_base = 0;
   DevResult* d_dense = nullptr;   size_t cap_dense = 0;
   float2* d_acc = nullptr;        size_t cap_acc = 0;     // channel sums of FFT lengths beyond one SM
@@ -92,6 +94,7 @@ struct Ctx {
   Server* server = nullptr;
   char devname[256] = {0};
   uint64_t last_h2d = 0, last_d2h = 0;
+  bool pair_kernel = false;    // both-strands correlation kernel usable (entropy table complement-symmetric)
 };
 
 
@@ -102,7 +105,7 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
 int batch_run(Ctx* c, Batch* b, cudaStream_t s, bool use_graph, bool timed = false);
 int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, size_t* n_out,
                   size_t* pair_counts);
-int batch_launch_count(const Batch* b);
+int batch_launch_count(const Ctx* c, const Batch* b);
 // z-score threshold of the scan kernel's FP32 probability screen.
 float screen_z(double min_prob, double target_total);
 int ctx_run_pairs(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, xc_result* out, size_t cap,

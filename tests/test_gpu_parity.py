@@ -63,23 +63,27 @@ def test_stages_match_reference(O, case):
     assert [sha1(d["signals"][0, 0, c]) for c in range(4)] == case["signal_sha1"][0]
     assert [sha1(d["signals"][0, 1, c]) for c in range(4)] == case["signal_sha1"][1]
     assert [sha1(d["signals"][1, 1, c]) for c in range(4)] == case["signal_sha1"][2]
-    for s, qq in enumerate((case["q"], rcq)):
-        band, xc64 = parity.straddles(O, case, qq, s)
-        scale = max(1.0, float(np.abs(xc64).max()))
-        err = float(np.abs(d["xc"][s].astype(np.float64) - xc64).max()) / scale
-        assert err <= XC_TOL, err
-        parity.compare_offsets(d["offsets"][s], case["ref_offsets"][s], band)
-        # DoOne segments over the GPU's own offsets: exact
-        want = [O.doone(case["t"], qq, int(i) - L // 2) for i in d["offsets"][s]]
-        want = np.concatenate(want) if want else np.zeros((0, 3), np.int32)
-        assert np.array_equal(d["segments"][s].reshape(-1, 3), want.reshape(-1, 3))
+    # correlation, offsets and segments from both correlation kernels: with
+    # signal output one CTA per strand, without it (A/C/G/T pairs at FFT 8192)
+    # the both-strands kernel that xc_align_pairs runs
+    for dd in (d, x.debug_pair(signals=False, **pair_item(case))):
+        for s, qq in enumerate((case["q"], rcq)):
+            band, xc64 = parity.straddles(O, case, qq, s)
+            scale = max(1.0, float(np.abs(xc64).max()))
+            err = float(np.abs(dd["xc"][s].astype(np.float64) - xc64).max()) / scale
+            assert err <= XC_TOL, err
+            parity.compare_offsets(dd["offsets"][s], case["ref_offsets"][s], band)
+            # DoOne segments over the GPU's own offsets: exact
+            want = [O.doone(case["t"], qq, int(i) - L // 2) for i in dd["offsets"][s]]
+            want = np.concatenate(want) if want else np.zeros((0, 3), np.int32)
+            assert np.array_equal(dd["segments"][s].reshape(-1, 3), want.reshape(-1, 3))
 
 
 @pytest.mark.parametrize("case", SUPPORTED, ids=[c["name"] for c in SUPPORTED])
 def test_results_match_reference(O, case):
     x = ctx_for(case)
     res = x.align([pair_item(case)])
-    d = x.debug_pair(**pair_item(case))
+    d = x.debug_pair(signals=False, **pair_item(case))   # the kernel align ran
     rcq = O.rc(case["q"])
     dropped = set()
     for s, qq in enumerate((case["q"], rcq)):
@@ -125,7 +129,7 @@ def test_fft32768_batch_vs_oracle(O):
     for k, (t, q) in enumerate(items):
         got = res[o:o + int(counts[k])]
         o += int(counts[k])
-        d = x.debug_pair(t=t, q=q)
+        d = x.debug_pair(t=t, q=q, signals=False)
         case = dict(t=t, L=32768, cutoff=1.8)
         for s, qq in enumerate((q, O.rc(q))):
             band, xc64 = parity.straddles(O, case, qq, s)
@@ -173,7 +177,7 @@ def test_uniform_batch_vs_oracle(O):
     for k, (t, q) in enumerate(items):
         got = res[o:o + int(counts[k])]
         o += int(counts[k])
-        d = x.debug_pair(t=t, q=q)
+        d = x.debug_pair(t=t, q=q, signals=False)
         want, _ = O.align_pair(P, O.pair(t, q), offsets_in=d["offsets"])
         assert parity.same_results(got, want, target_total=4096.0 * 4096)
     x.close()
@@ -233,7 +237,7 @@ def test_slave_end_to_end(O):
         assert parity.same_results(theirs, want, target_total=m["target_total"]), "oracle no longer splits the slave stream at pair %d" % k
         case = dict(L=8192, t_chunk_start=it["t_chunk_start"], q_chunk_start=it["q_chunk_start"],
                     query_size=it["query_size"], query_chunk=m["q_chunk"], cutoff=m["cutoff"], t=it["t"])
-        dbg = x.debug_pair(**it)
+        dbg = x.debug_pair(signals=False, **it)
         dropped = set()
         for s, qq in enumerate((it["q"], O.rc(it["q"]))):
             band, _ = parity.straddles(O, case, qq, s)
@@ -312,7 +316,85 @@ def test_edge_chunks_match_oracle(O):
     for k, (t, q) in enumerate(items):
         got = res[o:o + int(counts[k])]
         o += int(counts[k])
-        d = x.debug_pair(t=t, q=q)
+        d = x.debug_pair(t=t, q=q, signals=False)
         want, _ = O.align_pair(P, O.pair(t, q), offsets_in=d["offsets"])
         assert parity.same_results(got, want, target_total=TT), k
     x.close()
+
+
+def _mixed_items(rng):
+    """A/C/G/T pairs (both-strands kernel) interleaved with pairs it hands
+    back to the per-strand kernel: an N run, IUPAC letters, query lengths
+    that are not a multiple of the 16-base entropy window."""
+    items = []
+    for k in range(48):
+        t = W.random_bases(rng, 4096).tobytes()
+        q = bytearray(t[500:3500] + W.random_bases(rng, 1096).tobytes())
+        for i in rng.choice(len(q), 300, replace=False):
+            q[i] = b"ACGT"[rng.integers(4)]
+        q = bytes(q)
+        kind = k % 4
+        if kind == 1:
+            q = q[:2000] + b"N" * 100 + q[2100:]
+        elif kind == 2:
+            q = q[:4096 - 7]
+        elif kind == 3:
+            t = t[:1500] + b"RYKM" * 10 + t[1540:]
+        items.append((t, q))
+    return items
+
+
+def test_mixed_batch_both_kernels_vs_oracle(O):
+    """One launch where the both-strands kernel hands every fourth pair or
+    so back to the per-strand kernel: each pair's records equal the oracle's
+    over the GPU's own offsets."""
+    import satsuma2_gb300 as sg
+    rng = np.random.default_rng(71)
+    items = _mixed_items(rng)
+    TT = 4096.0 * 48
+    x = sg.XCorr(target_total=TT)
+    res, counts = x.align(items, with_counts=True)
+    P = O.params(target_total=TT)
+    o = 0
+    n_rec = 0
+    for k, (t, q) in enumerate(items):
+        got = res[o:o + int(counts[k])]
+        o += int(counts[k])
+        n_rec += len(got)
+        d = x.debug_pair(t=t, q=q, signals=False)
+        want, _ = O.align_pair(P, O.pair(t, q), offsets_in=d["offsets"])
+        assert parity.same_results(got, want, target_total=TT), k
+    assert n_rec > 48
+    x.close()
+
+
+def test_strand_kernel_switch_vs_oracle(O, monkeypatch):
+    """SATSUMA2_GB300_PAIR_KERNEL=0 at context creation runs every pair one
+    CTA per strand; its records equal the oracle's over its own offsets, and
+    the offsets agree with the both-strands kernel's except inside the
+    straddle band."""
+    import satsuma2_gb300 as sg
+    items = W.uniform_batch(24, seed=9)
+    TT = 4096.0 * 4096
+    x2 = sg.XCorr(target_total=TT)
+    monkeypatch.setenv("SATSUMA2_GB300_PAIR_KERNEL", "0")
+    x1 = sg.XCorr(target_total=TT)
+    monkeypatch.delenv("SATSUMA2_GB300_PAIR_KERNEL")
+    res, counts = x1.align(items, with_counts=True)
+    P = O.params(target_total=TT)
+    o = 0
+    for k, (t, q) in enumerate(items):
+        got = res[o:o + int(counts[k])]
+        o += int(counts[k])
+        d1 = x1.debug_pair(t=t, q=q, signals=False)
+        want, _ = O.align_pair(P, O.pair(t, q), offsets_in=d1["offsets"])
+        assert parity.same_results(got, want, target_total=TT), k
+        d2 = x2.debug_pair(t=t, q=q, signals=False)
+        case = dict(L=8192, cutoff=1.8, t=t)
+        for s, qq in enumerate((q, O.rc(q))):
+            band, _ = parity.straddles(O, case, qq, s)
+            parity.compare_offsets(d2["offsets"][s], d1["offsets"][s], band)
+            xa, xb = d1["xc"][s].astype(np.float64), d2["xc"][s].astype(np.float64)
+            assert np.abs(xa - xb).max() <= 1e-4 * max(1.0, np.abs(xa).max())
+    x1.close()
+    x2.close()
