@@ -5,11 +5,12 @@
 //                        FilterMatches on the raw segments.
 //     A/C/G/T pairs, in rounds of 128 diagonals (longest first):
 //       pass 1 (thread = diagonal): on 2-bit bitplanes, 32 equality bits per
-//         word op, a branch-free screen marks the 8-check blocks whose
-//         53-position span holds >= 19 equal bases;
+//         word op, a branch-free screen marks the words holding a 4-check
+//         block whose 49-position span holds >= 19 equal bases (the eight
+//         blocks of a word tested at once in byte lanes);
 //       items: the marked words of the round laid out contiguously per
 //         diagonal by a prefix sum, processed one per thread --
-//         phase A: exact window bits of the word's marked blocks;
+//         phase A: the word's 32 exact window bits, four byte lanes at once;
 //         phase B: falls and closing ends of runs against the previous
 //           word's last bit, queued as (item, bit) with one atomic per warp;
 //       phase C (thread = segment): run start from the same word or by
@@ -33,7 +34,7 @@ template <int LOG2L> struct ScanGeom {
   static constexpr int TWP = TW + 2;       // target plane words (zero padded)
   static constexpr int QPAD = 2;           // leading zero words of the query planes
   static constexpr int QWP = TW + 6;       // query plane words
-  static constexpr int FW = (TW + 7) / 8;  // flag entries per diagonal (8 words x 4 blocks each)
+  static constexpr int MW = (TW + 31) / 32;  // marked-word mask entries per diagonal
   // Marked-block items of one pass-2 sub-range and the segment queue (4 bytes
   // each; item indices fit 12 bits).  The queue shares its bytes with the
   // chunk byte arrays, which only the byte-table path fills.
@@ -41,7 +42,7 @@ template <int LOG2L> struct ScanGeom {
   static constexpr int QCAP = 2048;
   static constexpr size_t region = (size_t)QCAP * 4 > 2 * (size_t)N ? (size_t)QCAP * 4 : 2 * (size_t)N;
   static constexpr size_t bytes = region +
-      (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK + FW * NT_SCAN + 2 * ICAP + NT_SCAN) * 4 +
+      (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK + MW * NT_SCAN + 2 * ICAP + NT_SCAN) * 4 +
       (size_t)OFF_CHUNK * 2;
 };
 
@@ -94,6 +95,55 @@ __device__ __forceinline__ void gc_prefix(const uint32_t* b0, const uint32_t* b1
   if (lane == 0) pref[nw] = run;
 }
 
+// Per-nibble popcount of a 32-bit word.
+__device__ __forceinline__ uint32_t nib_popc(uint32_t x) {
+  x = x - ((x >> 1) & 0x55555555u);
+  return (x & 0x33333333u) + ((x >> 2) & 0x33333333u);
+}
+
+// Pass-1 screen of one word (equality words e2, e1, e0 of the word and the
+// two before it; check u of the word has the window of positions u-45..u,
+// bits u+19..u+64 of e2:e1:e0).  True when some block of four checks
+// 4b..4b+3 (b < 8) has >= MIN_HITS equal bases in its 49-position span, a
+// necessary condition for any of its checks to pass.  The span counts are
+// c(b) = c(0) + sum_{k<b} (entering nibble k - leaving nibble k), formed for
+// all eight blocks at once in byte lanes: even blocks 2j in one word, odd
+// blocks 2j+1 in another, each count biased by 128 - MIN_HITS so that bit 7
+// of its byte is the test.  Every byte stays within 0..255 (counts <= 49,
+// nibble differences biased by 4, prefix sums <= 48).
+__device__ __forceinline__ bool screen_word(uint32_t e2, uint32_t e1, uint32_t e0) {
+  const uint32_t pl = nib_popc(__funnelshift_r(e2, e1, 19));   // nibble k: bits 19+4k.. leaving
+  const uint32_t pe = nib_popc(e0 >> 4);                        // nibble k: bits 68+4k.. entering
+  const uint32_t de = (pe & 0x0f0f0f0fu) + 0x04040404u - (pl & 0x0f0f0f0fu);                 // 4 + d(2j)
+  const uint32_t dd = ((pe >> 4) & 0x0f0f0f0fu) + 0x04040404u - ((pl >> 4) & 0x0f0f0f0fu);   // 4 + d(2j+1)
+  const uint32_t sx = (de + dd) * 0x01010100u;   // byte j: sum_{i<j} (8 + d(2i) + d(2i+1))
+  const uint32_t c0 = __popc(e2 >> 19) + __popc(e1) + __popc(e0 & 15u);
+  const uint32_t x = sx + (c0 + (128 - MIN_HITS)) * 0x01010101u - 0x18100800u;   // 128 - 19 + c(2j)
+  const uint32_t x2 = x + de - 0x04040404u;                                        // 128 - 19 + c(2j+1)
+  return ((x | x2) & 0x80808080u) != 0u;
+}
+
+// Exact window bits of one word: bit u set when check u's window holds
+// >= MIN_HITS equal bases.  Four byte lanes (checks 8j + s) step s = 0..7
+// together: count(u+1) = count(u) + bit u+65 - bit u+19 of e2:e1:e0; the
+// counts stay within 0..46, so no lane borrows from or carries into the next.
+__device__ __forceinline__ uint32_t exact_word(uint32_t e2, uint32_t e1, uint32_t e0) {
+  const uint64_t U = ((uint64_t)e1 << 32) | e2;
+  uint32_t w = (uint32_t)(__popcll(U >> 19) + __popc(e0 & 1u)) |
+               (uint32_t)(__popcll(U >> 27) + __popc(e0 & 0x1ffu)) << 8 |
+               (uint32_t)(__popcll(U >> 35) + __popc(e0 & 0x1ffffu)) << 16 |
+               (uint32_t)(__popcll(U >> 43) + __popc(e0 & 0x1ffffffu)) << 24;
+  const uint32_t lv = __funnelshift_r(e2, e1, 19);   // bit 8j+s: leaves after check 8j+s
+  const uint32_t en = e0 >> 1;                       // bit 8j+s: enters at check 8j+s+1
+  uint32_t g = 0;
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    if (s) w = w + ((en >> (s - 1)) & 0x01010101u) - ((lv >> (s - 1)) & 0x01010101u);
+    g |= (((w + (128 - MIN_HITS) * 0x01010101u) >> 7) & 0x01010101u) << s;
+  }
+  return g;
+}
+
 template <int LOG2L>
 __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
   using Gm = ScanGeom<LOG2L>;
@@ -111,8 +161,8 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
   uint32_t* qb1 = qb0 + QWP;
   int* qgp = reinterpret_cast<int*>(qb1 + QWP);
   int* offs = qgp + (TW + 1);
-  uint32_t* bflags = reinterpret_cast<uint32_t*>(offs + OFF_CHUNK);   // [FW][NT_SCAN] pass-1 block masks
-  uint32_t* items = bflags + Gm::FW * NT_SCAN;                        // [ICAP] diag | word << 7 | blocks << 17
+  uint32_t* wmask = reinterpret_cast<uint32_t*>(offs + OFF_CHUNK);    // [MW][NT_SCAN] pass-1 marked words
+  uint32_t* items = wmask + Gm::MW * NT_SCAN;                         // [ICAP] diag | word << 7
   uint32_t* gbits = items + ICAP;                                     // [ICAP] passing checks of the word
   int* dpos = reinterpret_cast<int*>(gbits + ICAP);                   // [NT_SCAN] offsets of the round
   uint16_t* order = reinterpret_cast<uint16_t*>(dpos + NT_SCAN);
@@ -400,17 +450,13 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
       const bool valid = have && clast >= cfirst;
       const int wfirst = cfirst >> 5, wlast = clast >> 5;
 
-      // ---- pass 1 (thread = diagonal): a 4-bit block mask per word, eight
-      //      words per entry in bflags[q >> 3][tid]; no window inside an
-      //      unmarked block can pass.
+      // ---- pass 1 (thread = diagonal): one bit per word, 32 words per entry
+      //      of wmask[q >> 5][tid]; no check of an unmarked word can pass.
       int nb = 0;
       if (valid) {
         // The query word pair of target word w is (w + qd, w + qd + 1) at bit
         // shift sh: one new query word per step.
         const int qd = (pos + 32 * QPAD) >> 5, sh = (pos + 32 * QPAD) & 31;
-        // blocks holding valid checks in the first and last words
-        const uint32_t bm_first = (0xfu << ((cfirst & 31) >> 3)) & 0xfu;
-        const uint32_t bm_last = 0xfu >> (3 - ((clast & 31) >> 3));
         uint32_t e2 = eword(pos, wfirst - 2), e1 = eword(pos, wfirst - 1);
         int qi = wfirst + qd;
         uint32_t a0 = qb0[qi], a1 = qb1[qi];
@@ -421,21 +467,11 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
           a0 = n0;
           a1 = n1;
           qi++;
-          const uint64_t U = ((uint64_t)e1 << 32) | e2;
-          uint32_t f = 0;
-#pragma unroll
-          for (int sb = 0; sb < 4; sb++) {
-            const int a = 8 * sb + 19;
-            const int c53 = __popcll(U >> a) + __popc(e0 & lowmask(a - 11));
-            f |= (uint32_t)(c53 >= MIN_HITS) << sb;
-          }
-          if (w == wfirst) f &= bm_first;
-          if (w == wlast) f &= bm_last;
           const int q = w - wfirst;
-          acc |= f << (4 * (q & 7));
-          if ((q & 7) == 7 || w == wlast) {
-            bflags[(q >> 3) * NT_SCAN + tid] = acc;
-            nb += __popc((acc | (acc >> 1) | (acc >> 2) | (acc >> 3)) & 0x11111111u);   // marked words
+          acc |= (uint32_t)screen_word(e2, e1, e0) << (q & 31);
+          if ((q & 31) == 31 || w == wlast) {
+            wmask[(q >> 5) * NT_SCAN + tid] = acc;
+            nb += __popc(acc);
             acc = 0;
           }
           e2 = e1;
@@ -464,53 +500,32 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
         const int g1 = g0 + n;
         if (nb && ibase < g1 && ibase + nb > g0) {
           int kk = ibase;
-          const int nq8 = (wlast - wfirst + 8) >> 3;
-          for (int q8 = 0; q8 < nq8 && kk < g1; q8++) {
-            const uint32_t ent = bflags[q8 * NT_SCAN + tid];
-            uint32_t nz = (ent | (ent >> 1) | (ent >> 2) | (ent >> 3)) & 0x11111111u;
-            const int c = __popc(nz);
+          const int nq = (wlast - wfirst + 32) >> 5;
+          for (int q32 = 0; q32 < nq && kk < g1; q32++) {
+            uint32_t ent = wmask[q32 * NT_SCAN + tid];
+            const int c = __popc(ent);
             if (kk + c <= g0) {
               kk += c;
               continue;
             }
-            while (nz) {
-              const int bi = __ffs(nz) - 1;   // 4 x word within the entry
-              nz &= nz - 1;
-              if (kk >= g0 && kk < g1)
-                items[kk - g0] = (uint32_t)tid | ((uint32_t)(8 * q8 + (bi >> 2)) << 7) | (((ent >> bi) & 15u) << 17);
+            while (ent && kk < g1) {
+              const int bi = __ffs(ent) - 1;
+              ent &= ent - 1;
+              if (kk >= g0) items[kk - g0] = (uint32_t)tid | ((uint32_t)(32 * q32 + bi) << 7);
               kk++;
             }
           }
         }
         __syncthreads();
 
-        // ---- phase A (thread = item): exact window bits of the word's
-        //      marked blocks, window(c) = window(c-1) + e[c] - e[c-46];
-        //      unmarked blocks hold no passing check.
+        // ---- phase A (thread = item): the word's exact window bits ----
         for (int i = tid; i < n; i += NT_SCAN) {
           const uint32_t it = items[i];
           const int d = (int)(it & 127u), wr = (int)((it >> 7) & 1023u);
-          uint32_t f = (it >> 17) & 15u;
           const int p = dpos[d];
           const int cf = max(0, -p) + 46, cl = min(T - 1, Q - p) - 1;
           const int w = (cf >> 5) + wr;
-          const uint32_t e2 = eword(p, w - 2), e1 = eword(p, w - 1), e0 = eword(p, w);
-          const uint64_t U = ((uint64_t)e1 << 32) | e2;
-          uint32_t g = 0;
-          while (f) {
-            const int sb = __ffs(f) - 1;
-            f &= f - 1;
-            const uint32_t Y = e0 >> (8 * sb);
-            const uint32_t X = (uint32_t)(U >> (8 * sb + 18));
-            int c = __popcll(U >> (8 * sb + 19)) + __popc(e0 & lowmask(8 * sb + 1));
-            uint32_t gb = (uint32_t)(c >= MIN_HITS);
-#pragma unroll
-            for (int u = 1; u < 8; u++) {
-              c += (int)((Y >> u) & 1u) - (int)((X >> u) & 1u);
-              gb |= (uint32_t)(c >= MIN_HITS) << u;
-            }
-            g |= gb << (8 * sb);
-          }
+          const uint32_t g = exact_word(eword(p, w - 2), eword(p, w - 1), eword(p, w));
           const int lo = max(cf - 32 * w, 0), hi = min(cl - 32 * w, 31);
           gbits[i] = g & (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
         }
@@ -575,8 +590,7 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
             // a run still open at the word's last valid check ends at the
             // diagonal's end or at the first check of an unmarked next word
             if ((g >> hi) & 1u)
-              close = cw + hi == cl ||
-                      !((bflags[((wr + 1) >> 3) * NT_SCAN + d] >> (4 * ((wr + 1) & 7))) & 15u);
+              close = cw + hi == cl || !((wmask[((wr + 1) >> 5) * NT_SCAN + d] >> ((wr + 1) & 31)) & 1u);
             if (i == n - 1) {   // carried into the next sub-range
               s_cy_d[par] = d;
               s_cy_w[par] = wr;

@@ -395,3 +395,158 @@ def test_word_model_matches_oracle_doone(O, icap):
             got = model_doone_words(t, q, pos, icap)
             want = O.doone(t, q, pos)
             assert [g[:3] for g in got] == [tuple(x) for x in want.tolist()], (pos, icap)
+
+
+# ---------------------------------------------------------------------------
+# Word screen on 4-check blocks and byte-lane exact bits (the kernel's current
+# form).  The arithmetic below is the kernel's, on 32-bit words.
+# ---------------------------------------------------------------------------
+def nib_popc(x):
+    """Per-nibble popcount of a 32-bit word."""
+    x = (x - ((x >> 1) & 0x55555555)) & M32
+    return ((x & 0x33333333) + ((x >> 2) & 0x33333333)) & M32
+
+
+def screen_word(e2, e1, e0):
+    """True when some 4-check block of the word (checks 4b..4b+3, b < 8) has
+    >= 19 equal bases in its 49-position span: the block count c(b) = c(0) +
+    sum_{k<b} (entering nibble k - leaving nibble k), formed for the eight
+    blocks at once in byte lanes (even blocks 2j, odd blocks 2j+1)."""
+    U = (e1 << 32) | e2
+    pl = nib_popc((U >> 19) & M32)   # nibble k: span bits leaving between blocks k and k+1
+    pe = nib_popc(e0 >> 4)           # nibble k: bits entering
+    de = ((pe & 0x0F0F0F0F) + 0x04040404 - (pl & 0x0F0F0F0F)) & M32          # 4 + d(2j)
+    do = (((pe >> 4) & 0x0F0F0F0F) + 0x04040404 - ((pl >> 4) & 0x0F0F0F0F)) & M32   # 4 + d(2j+1)
+    sx = (((de + do) & M32) * 0x01010100) & M32                                # sum_{i<j} (8 + d(2i) + d(2i+1))
+    c0 = popc(U >> 19) + popc(e0 & 0xF)
+    x = (sx + (c0 + 128 - MIN_HITS) * 0x01010101 - 0x18100800) & M32           # 128 - 19 + c(2j)
+    x2 = (x + de - 0x04040404) & M32                                           # 128 - 19 + c(2j+1)
+    return ((x | x2) & 0x80808080) != 0
+
+
+def exact_word(e2, e1, e0):
+    """Bit u set when check u's window [u-45, u] (in the word's frame) holds
+    >= 19 equal bases: four byte lanes (u = 8j + s) step s = 0..7 together."""
+    U = (e1 << 32) | e2
+    w = 0
+    for j in range(4):
+        u = 8 * j
+        w |= (popc(U >> (u + 19)) + popc(e0 & lowmask(u + 1))) << (8 * j)
+    lv = (U >> 19) & M32   # bit 8j+s: the position leaving after check 8j+s
+    en = e0 >> 1           # bit 8j+s: the position entering at check 8j+s+1
+    g = 0
+    for s in range(8):
+        if s:
+            w = (w + ((en >> (s - 1)) & 0x01010101) - ((lv >> (s - 1)) & 0x01010101)) & M32
+        g |= (((w + (128 - MIN_HITS) * 0x01010101) >> 7) & 0x01010101) << s
+    return g
+
+
+def test_word_screen_and_exact_bits_bruteforce():
+    rng = np.random.default_rng(81)
+    for it in range(4000):
+        dens = rng.choice([0.25, 0.4, 0.55, 0.9])
+        e = [int(sum(int(b) << k for k, b in enumerate(rng.random(32) < dens))) for _ in range(3)]
+        e2, e1, e0 = e
+        V = e2 | (e1 << 32) | (e0 << 64)
+        win = [popc((V >> (u + 19)) & ((1 << 46) - 1)) for u in range(32)]
+        want_g = sum(1 << u for u in range(32) if win[u] >= MIN_HITS)
+        assert exact_word(e2, e1, e0) == want_g
+        spans = [popc((V >> (4 * b + 19)) & ((1 << 49) - 1)) for b in range(8)]
+        assert screen_word(e2, e1, e0) == any(s >= MIN_HITS for s in spans)
+        # necessary condition: a word with a passing check is marked
+        assert not want_g or screen_word(e2, e1, e0)
+
+
+def model_doone_words4(t, q, pos, icap=4096):
+    """Pass 1 marks words (screen_word); phase A gives each marked word its
+    exact bits (exact_word); phases B and C as in model_doone_words, a run
+    open at a word's last check closing when the next word is unmarked."""
+    T, Q = len(t), len(q)
+    TW = max(T, Q) // 32 + 2
+    tb0, tb1 = planes(t, TW + 2)
+    qb0, qb1 = planes(q, TW + 8, pad=2)
+    i0 = max(0, -pos)
+    iend = min(T - 1, Q - pos)
+    cfirst, clast = i0 + 46, iend - 1
+    if clast < cfirst:
+        return []
+
+    def fs(lo, hi, sh):
+        return ((hi << 32 | lo) >> sh) & M32
+
+    def eword(w):
+        if w < 0:
+            return 0
+        qo = 32 * w + pos + 64
+        qw, sh = qo >> 5, qo & 31
+        return ~((tb0[w] ^ fs(qb0[qw], qb0[qw + 1], sh)) | (tb1[w] ^ fs(qb1[qw], qb1[qw + 1], sh))) & M32
+
+    def vmask(w):
+        lo, hi = max(cfirst - 32 * w, 0), min(clast - 32 * w, 31)
+        return (M32 >> (31 - hi)) & (M32 << lo) & M32
+
+    wfirst, wlast = cfirst >> 5, clast >> 5
+    words = [w for w in range(wfirst, wlast + 1) if screen_word(eword(w - 2), eword(w - 1), eword(w))]
+    marked = set(words)
+    G = [exact_word(eword(w - 2), eword(w - 1), eword(w)) & vmask(w) for w in words]
+
+    segs = []
+    carry = None
+    for g0 in range(0, len(words), icap):
+        g1 = min(len(words), g0 + icap)
+
+        def pbit_of(i):
+            if i > g0:
+                return (G[i - 1] >> 31) if words[i - 1] == words[i] - 1 else 0
+            if carry is not None and carry[0] == words[i] - 1:
+                return carry[1] >> 31
+            return 0
+
+        def rise_of(i):
+            return G[i] & ~(((G[i] << 1) | pbit_of(i)) & M32) & M32
+
+        def run_start(i, u):
+            rb = rise_of(i) & lowmask(u)
+            while not rb:
+                i -= 1
+                if i < g0:
+                    return carry[2]
+                rb = rise_of(i)
+            return 32 * words[i] + rb.bit_length() - 1
+
+        for i in range(g0, g1):
+            w, g = words[i], G[i]
+            vm = vmask(w)
+            hi = min(clast - 32 * w, 31)
+            fall = ~g & (((g << 1) | pbit_of(i)) & M32) & vm & M32
+            for u in range(32):
+                if (fall >> u) & 1:
+                    segs.append((run_start(i, u) - 45, 32 * w + u))
+            if (g >> hi) & 1:
+                if 32 * w + hi == clast:
+                    segs.append((run_start(i, hi + 1) - 45, iend))
+                elif w + 1 not in marked:
+                    segs.append((run_start(i, 32) - 45, 32 * w + 32))
+        last = g1 - 1
+        carry = (words[last], G[last], run_start(last, 32) if (G[last] >> 31) & 1 else -1)
+    segs.sort()
+    return [(s, s + pos, e - s, equal_bases(t, q, s, pos, e - s)) for s, e in segs]
+
+
+@pytest.mark.parametrize("icap", [4096, 5, 1])
+def test_word4_model_matches_oracle_doone(O, icap):
+    rng = np.random.default_rng(82)
+    cases = W.uniform_batch(4, seed=17) + [W.plain_pair(7)]
+    t = W.random_bases(rng, 4096)
+    cases.append((t.tobytes(), t.tobytes()))
+    cases.append((t.tobytes(), W.tandem_repeat(rng, 4096, 2, 3).tobytes()))
+    cases.append((t[:1000].tobytes(), t[:999].tobytes()))
+    for t, q in cases:
+        offs = O.findtop(O.xcorr64(t, q, 8192), 1.8)
+        extra = rng.integers(-len(t) + 1, len(q), size=10)
+        for i in list(offs[:20]) + [int(x) + 4096 for x in extra]:
+            pos = int(i) - 4096
+            got = model_doone_words4(t, q, pos, icap)
+            want = O.doone(t, q, pos)
+            assert [g[:3] for g in got] == [tuple(x) for x in want.tolist()], (pos, icap)
