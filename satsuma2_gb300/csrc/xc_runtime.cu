@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -262,17 +263,82 @@ static int host_grow(T*& ptr, size_t& cap, size_t need) {
   return XC_OK;
 }
 
-static void parallel_for(size_t n, size_t grain, const std::function<void(size_t, size_t)>& f) {
-  unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  if (n < grain * 2 || nt == 1) {
-    f(0, n);
-    return;
+// Worker threads kept for the host-side copies of batch_pack: the calling
+// thread and up to 15 workers split one job's index range into chunks.  A
+// thread that starts a job while another job runs does its own range.
+class HostPool {
+ public:
+  static HostPool& get() {
+    static HostPool* p = new HostPool();   // never destroyed: workers may outlive static destructors
+    return *p;
   }
-  nt = (unsigned)std::min<size_t>(nt, (n + grain - 1) / grain);
-  std::vector<std::thread> th;
-  for (unsigned w = 1; w < nt; w++) th.emplace_back(f, n * w / nt, n * (w + 1) / nt);
-  f(0, n / nt);
-  for (auto& t : th) t.join();
+  void run(size_t n, size_t grain, const std::function<void(size_t, size_t)>& f) {
+    const size_t chunks = std::min<size_t>(workers_ + 1, (n + grain - 1) / std::max<size_t>(grain, 1));
+    std::unique_lock<std::mutex> busy(run_mu_, std::defer_lock);
+    if (chunks <= 1 || !busy.try_lock()) {
+      f(0, n);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      job_ = &f;
+      n_ = n;
+      chunks_ = chunks;
+      next_ = 0;
+      left_ = chunks;
+      gen_++;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return left_ == 0; });
+    job_ = nullptr;
+  }
+
+ private:
+  HostPool() {
+    const unsigned hc = std::thread::hardware_concurrency();
+    workers_ = std::max(1u, std::min(16u, hc ? hc : 1u)) - 1;
+    for (unsigned i = 0; i < workers_; i++) std::thread([this] { loop(); }).detach();
+  }
+  void loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+      }
+      work();
+    }
+  }
+  void work() {   // takes chunks of the current job until none is left
+    for (;;) {
+      const std::function<void(size_t, size_t)>* f;
+      size_t k, n, ch;
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (!job_ || next_ >= chunks_) return;
+        k = next_++;
+        f = job_;
+        n = n_;
+        ch = chunks_;
+      }
+      (*f)(n * k / ch, n * (k + 1) / ch);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--left_ == 0) done_cv_.notify_all();
+    }
+  }
+  unsigned workers_ = 0;
+  std::mutex run_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(size_t, size_t)>* job_ = nullptr;
+  size_t n_ = 0, chunks_ = 0, next_ = 0, left_ = 0;
+  uint64_t gen_ = 0;
+};
+
+static void parallel_for(size_t n, size_t grain, const std::function<void(size_t, size_t)>& f) {
+  HostPool::get().run(n, grain, f);
 }
 
 Batch::~Batch() {
@@ -364,7 +430,7 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   // gather sequences into pinned staging (threads for large batches)
   uint8_t* hp = b->h_pool;
   const std::vector<int>& ord = b->order;
-  parallel_for(n, 256, [&](size_t lo, size_t hi) {
+  parallel_for(n, 64, [&](size_t lo, size_t hi) {   // chunks of >= 64 pairs (0.5 MB)
     for (size_t d = lo; d < hi; d++) {
       const xc_pair& p = pairs[ord[d]];
       if (p.tlen) memcpy(hp + toff[d], p.tseq, (size_t)p.tlen);
@@ -625,22 +691,21 @@ int ctx_run_pairs(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, xc_result* o
 // xc_align_pairs: the pairs run as sub-batches alternating between two
 // batches and two streams, so the host packing and the host-to-device copy of
 // one sub-batch overlap the kernels of the one before; results are collected
-// in order.  Sub-batches hold at least 1024 pairs (a launch fills the GPU) and
-// a big call is cut in about four.
-static constexpr size_t FIRST_SUB = 512;
-
+// in order.  Sub-batch sizes count in waves of the FFT-8192 correlation kernel
+// (one CTA per SM): a first one of 3 waves so the GPU starts early, then
+// equal ones of at most 12 waves and max_batch pairs.  On GB300 a 4096-pair
+// call took 2.28 ms as 456 + 2 x 1820 pairs, 2.57 ms as 512 + 4 x 896 and
+// 2.59 ms in one batch.
 int ctx_align_pipelined(Ctx* c, const xc_pair* pairs, size_t n, xc_result* out, size_t cap, size_t* n_out,
                         size_t* pair_counts) {
   const size_t maxb = c->prm.max_batch > 0 ? (size_t)c->prm.max_batch : 4096;
-  // sub-batch boundaries: a short first one so the GPU starts early, then
-  // equal ones of at most max(1024, n/4) pairs
+  const size_t first = std::min(maxb, (size_t)3 * c->sms), size = std::min(maxb, (size_t)12 * c->sms);
   std::vector<size_t> bound{0};
-  if (n <= 1024) {
+  if (n <= 2 * first && n <= maxb) {
     bound.push_back(n);
   } else {
-    const size_t first = FIRST_SUB;
     bound.push_back(first);
-    const size_t rest = n - first, size = std::min(maxb, std::max<size_t>(1024, (n + 3) / 4));
+    const size_t rest = n - first;
     const size_t parts = (rest + size - 1) / size;
     for (size_t i = 1; i <= parts; i++) bound.push_back(first + rest * i / parts);
   }
@@ -723,6 +788,7 @@ int xc_create(const xc_params* params, int device, xc_ctx** out) {
   if (c->prm.q_chunk <= 0) c->prm.q_chunk = 4096;
   c->device = device;
   int r = cuda_err(cudaSetDevice(device), "cudaSetDevice");
+  if (r == XC_OK) r = cuda_err(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device), "SM count");
   if (r == XC_OK) r = cuda_err(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
   if (r == XC_OK) r = cuda_err(prepare_kernels(), "kernel attributes");
   if (r == XC_OK) r = build_tables(c);

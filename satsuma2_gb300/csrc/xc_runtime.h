@@ -94,6 +94,7 @@ struct Ctx {
   Server* server = nullptr;
   char devname[256] = {0};
   uint64_t last_h2d = 0, last_d2h = 0;
+  int sms = 152;               // multiprocessors of the device (sub-batch sizing)
   bool pair_kernel = false;    // both-strands correlation kernel usable (entropy table complement-symmetric)
 };
 
