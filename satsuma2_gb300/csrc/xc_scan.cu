@@ -95,6 +95,40 @@ __device__ __forceinline__ void gc_prefix(const uint32_t* b0, const uint32_t* b1
   if (lane == 0) pref[nw] = run;
 }
 
+// 2-bit code planes of len bytes at g (16-byte aligned, readable up to the
+// next 16-byte boundary) into p0/p1 words 0..nw-1, positions >= len zero.
+// Each lane loads 16 bytes, forms four codes per 32-bit word
+// ((b>>1 ^ b>>2) & 3, A=0 C=1 G=2 T=3), gathers their plane bits with one
+// multiply per word, and lanes 2j, 2j+1 join their 16 bits into one word.
+// Every thread of the CTA calls it.
+__device__ __forceinline__ void build_planes(const uint8_t* __restrict__ g, int len, uint32_t* p0, uint32_t* p1,
+                                             int nw, int tid) {
+  for (int c0 = 0; c0 < 2 * nw; c0 += NT_SCAN) {
+    const int c = c0 + tid;
+    uint32_t m0 = 0u, m1 = 0u;
+    if (c < 2 * nw && 16 * c < len) {
+      const uint4 v = *reinterpret_cast<const uint4*>(g + 16 * c);
+      const uint32_t x[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const uint32_t cd = ((x[k] >> 1) ^ (x[k] >> 2)) & 0x03030303u;
+        m0 |= (((cd & 0x01010101u) * 0x10204080u) >> 28) << (4 * k);          // bit 0 of byte j -> bit j
+        m1 |= ((((cd >> 1) & 0x01010101u) * 0x10204080u) >> 28) << (4 * k);
+      }
+      const int valid = len - 16 * c;
+      if (valid < 16) {
+        m0 &= (1u << valid) - 1u;
+        m1 &= (1u << valid) - 1u;
+      }
+    }
+    const uint32_t h0 = __shfl_down_sync(0xffffffffu, m0, 1), h1 = __shfl_down_sync(0xffffffffu, m1, 1);
+    if (!(tid & 1) && c < 2 * nw) {
+      p0[c >> 1] = m0 | (h0 << 16);
+      p1[c >> 1] = m1 | (h1 << 16);
+    }
+  }
+}
+
 // Per-nibble popcount of a 32-bit word.
 __device__ __forceinline__ uint32_t nib_popc(uint32_t x) {
   x = x - ((x >> 1) & 0x55555555u);
@@ -208,42 +242,43 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
     }
   } else {
     // 2-bit codes as two bitplanes straight from the pool, bit u of word w =
-    // position 32w+u: one warp per word, one ballot per plane.  The pair is
-    // all A/C/G/T, whose complement flips both code bits.
-    // Eight words per step: their loads are all in flight before the ballots.
-    constexpr int UNR = 8;
-    for (int w0 = warp; w0 < TWP; w0 += NWARP * UNR) {
-      uint32_t cd[UNR];
-#pragma unroll
-      for (int k = 0; k < UNR; k++) {
-        const int i = 32 * (w0 + NWARP * k) + lane;
-        cd[k] = i < T ? code_of(gt[i]) : 0u;
-      }
-#pragma unroll
-      for (int k = 0; k < UNR; k++) {
-        const int w = w0 + NWARP * k;
-        const uint32_t b0 = __ballot_sync(FULL, cd[k] & 1u), b1 = __ballot_sync(FULL, cd[k] & 2u);
-        if (lane == 0 && w < TWP) {
-          tb0[w] = b0;
-          tb1[w] = b1;
-        }
-      }
+    // position 32w+u.  The pair is all A/C/G/T, whose complement flips both
+    // code bits.  Strand 1 builds the query's forward planes in the (here
+    // unused) byte region first and reads them backwards.
+    if (tid < QPAD) {
+      qb0[tid] = 0u;
+      qb1[tid] = 0u;
     }
-    for (int w0 = warp; w0 < QWP; w0 += NWARP * UNR) {
-      uint32_t cd[UNR];
-#pragma unroll
-      for (int k = 0; k < UNR; k++) {
-        const int i = 32 * (w0 + NWARP * k - QPAD) + lane;
-        cd[k] = (i >= 0 && i < Q) ? (strand ? code_of(gq[Q - 1 - i]) ^ 3u : code_of(gq[i])) : 0u;
-      }
-#pragma unroll
-      for (int k = 0; k < UNR; k++) {
-        const int w = w0 + NWARP * k;
-        const uint32_t b0 = __ballot_sync(FULL, cd[k] & 1u), b1 = __ballot_sync(FULL, cd[k] & 2u);
-        if (lane == 0 && w < QWP) {
-          qb0[w] = b0;
-          qb1[w] = b1;
+    build_planes(gt, T, tb0, tb1, TWP, tid);
+    if (!strand) {
+      build_planes(gq, Q, qb0 + QPAD, qb1 + QPAD, QWP - QPAD, tid);
+    } else {
+      uint32_t* f0 = reinterpret_cast<uint32_t*>(smem);
+      uint32_t* f1 = f0 + (TW + 2);
+      build_planes(gq, Q, f0, f1, TW + 2, tid);
+      __syncthreads();
+      // word w of the reverse complement: forward positions Q-32-32w ..
+      // Q-1-32w, bit-reversed and complemented; positions past Q are zero
+      for (int w = tid; w < QWP - QPAD; w += NT_SCAN) {
+        const int lim = Q - 32 * w;   // valid bits of the word
+        uint32_t r0 = 0u, r1 = 0u;
+        if (lim > 0) {
+          const int s0 = lim - 32;  // forward start, > -32
+          uint32_t g0, g1;
+          if (s0 >= 0) {
+            const int fw = s0 >> 5, sh = s0 & 31;
+            g0 = __funnelshift_r(f0[fw], f0[fw + 1], sh);
+            g1 = __funnelshift_r(f1[fw], f1[fw + 1], sh);
+          } else {
+            g0 = f0[0] << -s0;
+            g1 = f1[0] << -s0;
+          }
+          const uint32_t m = lowmask(lim);
+          r0 = ~__brev(g0) & m;
+          r1 = ~__brev(g1) & m;
         }
+        qb0[QPAD + w] = r0;
+        qb1[QPAD + w] = r1;
       }
     }
     __syncthreads();
