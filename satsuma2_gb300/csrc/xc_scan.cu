@@ -298,7 +298,8 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
     const uint32_t q1 = __funnelshift_r(qb1[qw], qb1[qw + 1], sh);
     return ~((tb0[w] ^ q0) | (tb1[w] ^ q1));
   };
-  // Equal bases of segment [s0, s1) on diagonal pos.
+  // Equal bases of segment [s0, s1) on diagonal pos.  (A version streaming
+  // one query word per target word measured 17% slower over the whole scan.)
   auto seg_hits = [&](int pos, int s0, int s1) -> int {
     int h = 0;
     const int wa = s0 >> 5, wb = (s1 - 1) >> 5;
@@ -309,6 +310,17 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
       h += __popc(eword(pos, w) & m);
     }
     return h;
+  };
+  // eword(pos, w - 2), eword(pos, w - 1), eword(pos, w) for w >= 1, sharing
+  // the four query words they read.
+  auto ewords3 = [&](int pos, int w, uint32_t& e2, uint32_t& e1, uint32_t& e0) {
+    const int qo = 32 * (w - 2) + pos + 32 * QPAD;
+    const int qw = qo >> 5, sh = qo & 31;
+    const uint32_t x0 = qb0[qw], x1 = qb0[qw + 1], x2 = qb0[qw + 2], x3 = qb0[qw + 3];
+    const uint32_t y0 = qb1[qw], y1 = qb1[qw + 1], y2 = qb1[qw + 2], y3 = qb1[qw + 3];
+    e2 = w >= 2 ? ~((tb0[w - 2] ^ __funnelshift_r(x0, x1, sh)) | (tb1[w - 2] ^ __funnelshift_r(y0, y1, sh))) : 0u;
+    e1 = ~((tb0[w - 1] ^ __funnelshift_r(x1, x2, sh)) | (tb1[w - 1] ^ __funnelshift_r(y1, y2, sh)));
+    e0 = ~((tb0[w] ^ __funnelshift_r(x2, x3, sh)) | (tb1[w] ^ __funnelshift_r(y2, y3, sh)));
   };
 
   // One DoOne segment [s0, s1) on offset pos (CrossCorr.cc:693,713) through
@@ -560,7 +572,9 @@ __global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
           const int p = dpos[d];
           const int cf = max(0, -p) + 46, cl = min(T - 1, Q - p) - 1;
           const int w = (cf >> 5) + wr;
-          const uint32_t g = exact_word(eword(p, w - 2), eword(p, w - 1), eword(p, w));
+          uint32_t e2, e1, e0;
+          ewords3(p, w, e2, e1, e0);
+          const uint32_t g = exact_word(e2, e1, e0);
           const int lo = max(cf - 32 * w, 0), hi = min(cl - 32 * w, 31);
           gbits[i] = g & (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
         }
