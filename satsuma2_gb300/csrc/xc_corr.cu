@@ -613,22 +613,32 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
   const uint8_t* __restrict__ gt = P.pool + P.pairs[pidx].t_off;
   const uint8_t* __restrict__ gq = P.pool + P.pairs[pidx].q_off;
 
-  // ---- 1. chunk bytes, forward strand only ----
+  // ---- 1. chunk bytes, forward strand only: threads 0..N/16-1 take one
+  //      16-byte piece of the target each, the next N/16 one of the query
+  //      (pool chunks are 16-byte aligned and padded to 16); bytes past the
+  //      chunk end are zeroed.  Per byte, exactly: (y & 0x7f) + 0x7f | y has
+  //      bit 7 clear iff y == 0. ----
+  static_assert(2 * (N / 16) <= NT_PAIR, "one 16-byte piece per thread");
   int high = 0, nonacgt = 0;
-  for (int i = tid; i < N; i += NT_PAIR) {
-    unsigned b = 0, c = 0;
-    if (i < T) {
-      b = gt[i];
-      high |= b >> 7;
-      nonacgt |= !is_acgt(b);
+  if (tid < 2 * (N / 16)) {
+    const int which = tid / (N / 16), c = tid % (N / 16);
+    const int len = which ? Q : T;
+    const int valid = len - 16 * c;   // bytes of this piece inside the chunk
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (valid > 0) v = *reinterpret_cast<const uint4*>((which ? gq : gt) + 16 * c);
+    uint32_t x[4] = {v.x, v.y, v.z, v.w};
+    auto nz = [](uint32_t y) { return (((y & 0x7f7f7f7fu) + 0x7f7f7f7fu) | y) & 0x80808080u; };
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int vk = min(max(valid - 4 * k, 0), 4);
+      const uint32_t m = vk >= 4 ? 0xffffffffu : (1u << (8 * vk)) - 1u;
+      x[k] &= m;
+      high |= (x[k] & 0x80808080u) != 0u;
+      const uint32_t bad = nz(x[k] ^ 0x41414141u) & nz(x[k] ^ 0x43434343u) & nz(x[k] ^ 0x47474747u) &
+                           nz(x[k] ^ 0x54545454u);   // bit 7: byte is not A, C, G or T
+      nonacgt |= (bad & m & 0x80808080u) != 0u;
     }
-    if (i < Q) {
-      c = gq[i];
-      high |= c >> 7;
-      nonacgt |= !is_acgt(c);
-    }
-    st[i] = (uint8_t)b;
-    sq[i] = (uint8_t)c;
+    *reinterpret_cast<uint4*>((which ? sq : st) + 16 * c) = make_uint4(x[0], x[1], x[2], x[3]);
   }
   for (int i = tid; i < NH; i += NT_PAIR) {
     twNh[i] = P.tab.twN_hi[i];
