@@ -207,6 +207,7 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
   __shared__ int s_cnt4[8];
   __shared__ double s_off[8];
   __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
+  __shared__ Split3 s_wf[2][8];    // the same as three floats each
   __shared__ int s_warp[NT_CORR / 32];
 
   const int tid = threadIdx.x;
@@ -371,6 +372,8 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
     s_off[tid] = off;
     s_wmo[0][tid] = __dsub_rn(0.0, off);
     s_wmo[1][tid] = __dsub_rn(1.0, off);
+    s_wf[0][tid] = split3(s_wmo[0][tid]);
+    s_wf[1][tid] = split3(s_wmo[1][tid]);
   }
   __syncthreads();
 
@@ -381,10 +384,11 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
     // Per-window channel values: out = float(entropy * (weight - mean))
     // (CrossCorr.cc:123), weight 0 or 1 for A/C/G/T.
     if (!generic) {
-      const double E = (double)(grp ? Eq : Et)[gtid];
+      const float E = (grp ? Eq : Et)[gtid];
+      const int k = grp * 4 + c;
       float2 v;
-      v.x = __double2float_rn(__dmul_rn(E, s_wmo[0][grp * 4 + c]));
-      v.y = __double2float_rn(__dmul_rn(E, s_wmo[1][grp * 4 + c]));
+      v.x = mul_round_f32(E, s_wf[0][k], s_wmo[0][k]);
+      v.y = mul_round_f32(E, s_wf[1][k], s_wmo[1][k]);
       (grp ? vq : vt)[gtid] = v;
     }
     __syncthreads();
@@ -603,6 +607,7 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
   float2* vv = reinterpret_cast<float2*>(Eq + NWIN);   // [t c0, t c1, q c0, q c1][window]
   __shared__ int s_cnt4[8];
   __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
+  __shared__ Split3 s_wf[2][8];    // the same as three floats each
   __shared__ int s_warp[2][NT_CORR / 32];
 
   const int tid = threadIdx.x;
@@ -722,6 +727,8 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
     const double off = len > 0 ? __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len) : 0.0;
     s_wmo[0][tid] = __dsub_rn(0.0, off);
     s_wmo[1][tid] = __dsub_rn(1.0, off);
+    s_wf[0][tid] = split3(s_wmo[0][tid]);
+    s_wf[1][tid] = split3(s_wmo[1][tid]);
   }
   __syncthreads();
 
@@ -733,10 +740,11 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
     {
       const int which = tid >> 8, w = tid & 255;
       const int seq = which >> 1, ch = (which & 1) ? c1 : c0;
-      const double E = (double)(seq ? Eq : Et)[w];
+      const float E = (seq ? Eq : Et)[w];
+      const int k = seq * 4 + ch;
       float2 v;
-      v.x = __double2float_rn(__dmul_rn(E, s_wmo[0][seq * 4 + ch]));
-      v.y = __double2float_rn(__dmul_rn(E, s_wmo[1][seq * 4 + ch]));
+      v.x = mul_round_f32(E, s_wf[0][k], s_wmo[0][k]);
+      v.y = mul_round_f32(E, s_wf[1][k], s_wmo[1][k]);
       vv[which * NWIN + w] = v;
     }
     __syncthreads();

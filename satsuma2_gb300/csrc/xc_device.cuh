@@ -265,6 +265,44 @@ __device__ __forceinline__ void fft_inverse(float2* buf, const float2* h, const 
   }
 }
 
+// W = h + l + r exactly, three floats (h = float(W), l = float(W - h), r the
+// rest, at most a few bits), for mul_round_f32.
+struct Split3 {
+  float h, l, r;
+};
+__device__ __forceinline__ Split3 split3(double W) {
+  Split3 s;
+  s.h = __double2float_rn(W);
+  const double d = __dsub_rn(W, (double)s.h);   // exact
+  s.l = __double2float_rn(d);
+  s.r = __double2float_rn(__dsub_rn(d, (double)s.l));   // exact, representable
+  return s;
+}
+
+// __double2float_rn(__dmul_rn((double)E, W)) without FP64 in the common
+// case, for finite E and W with |E*W| >= 2^-100 or zero.  E*W = E*h + E*l +
+// E*r is formed as p1 + t to within 2^-45 |E*W| from FMA-exact products; the
+// FP32 rounding f of p1 + t then equals the rounding of the double product,
+// except within 2^-16 ulp of a rounding boundary (where the double rounding
+// may part) or when f is a power of two (a boundary a half-ulp nearer below),
+// which take the FP64 product.  Zero keeps the sign the double product has.
+__device__ __forceinline__ float mul_round_f32(float E, const Split3& w, double W) {
+  const float p1 = __fmul_rn(E, w.h);
+  if (p1 == 0.f) return p1;
+  const float e1 = __fmaf_rn(E, w.h, -p1);
+  const float p2 = __fmul_rn(E, w.l);
+  const float e2 = __fmaf_rn(E, w.l, -p2);
+  const float p3 = __fmul_rn(E, w.r);
+  const float t = __fadd_rn(__fadd_rn(e1, p2), __fadd_rn(e2, p3));
+  const float f = __fadd_rn(p1, t);
+  const float r = __fadd_rn(__fsub_rn(p1, f), t);   // p1 - f exact
+  const uint32_t fb = __float_as_uint(f);
+  const float ulp = __uint_as_float((fb & 0x7f800000u) - (23u << 23));
+  if ((fb & 0x007fffffu) == 0u || fabsf(r) >= __fmul_rn(ulp, 0.49998f))
+    return __double2float_rn(__dmul_rn((double)E, W));
+  return f;
+}
+
 // Ent (CrossCorr.cc:28-33) for windows holding a one-third IUPAC letter.
 __device__ __forceinline__ double ent_dev(double p) {
   if (p < 0.001) return 0.0;

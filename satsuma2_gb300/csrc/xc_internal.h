@@ -13,7 +13,8 @@ constexpr int NT_CORR = 512;     // threads of the correlation kernel (one pair 
 constexpr int NT_PAIR = 1024;    // threads of the both-strands correlation kernel
 constexpr int PAIR_LOG2L = 13;   // FFT length of the both-strands kernel (its buffers fill one SM)
 constexpr int NT_SCAN = 128;     // threads of the scan kernel
-constexpr int OFF_CHUNK = 256;   // offsets staged per scan chunk (sized for 7 scan CTAs per SM)
+constexpr int OFF_CHUNK = 256;   // offsets staged per scan chunk
+constexpr int SCAN_CTAS_PER_SM = 8;   // scan register budget: 64 per thread (8 measured 3% faster than 7)
 constexpr int WINDOW = 46;       // DoOne window: m_minLen + 1 positions (CrossCorr.cc:701-705)
 constexpr int MIN_HITS = 19;     // ACGT windows pass when 100*hits > 1889 (CrossCorr.cc:675)
 

@@ -179,7 +179,7 @@ __device__ __forceinline__ uint32_t exact_word(uint32_t e2, uint32_t e1, uint32_
 }
 
 template <int LOG2L>
-__global__ void __launch_bounds__(NT_SCAN, 7) scan_kernel(const ScanParams P) {
+__global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const ScanParams P) {
   using Gm = ScanGeom<LOG2L>;
   constexpr int L = Gm::L, N = Gm::N, TW = Gm::TW, TWP = Gm::TWP, QPAD = Gm::QPAD, QWP = Gm::QWP;
   constexpr int ICAP = Gm::ICAP, QCAP = Gm::QCAP, NWARP = NT_SCAN / 32;
@@ -772,14 +772,14 @@ cudaError_t prepare_scan_kernels() {
 
 cudaError_t launch_scan(int log2L, const ScanParams& p, int npairs, cudaStream_t s) {
   if (npairs <= 0) return cudaSuccess;
-  // Fewer strands than a wave of CTAs (7 per SM): split them, up to 4 ways.
+  // Fewer strands than a wave of CTAs: split them, up to 4 ways.
   static const int sms = [] {
     int dev = 0, n = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     return n;
   }();
   int split = 1;
-  while (split < 4 && 2 * npairs * split * 2 <= 7 * sms) split *= 2;
+  while (split < 4 && 2 * npairs * split * 2 <= SCAN_CTAS_PER_SM * sms) split *= 2;
   if (split > 1) {
     const cudaError_t e = cudaMemsetAsync(p.res_cnt + 2 * (size_t)p.first, 0, 2 * (size_t)npairs * sizeof(int), s);
     if (e != cudaSuccess) return e;
