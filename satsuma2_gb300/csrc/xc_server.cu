@@ -45,6 +45,7 @@ struct Slot {
   Batch* b = nullptr;
   cudaStream_t s = nullptr;
   cudaEvent_t ev = nullptr;
+  cudaEvent_t kend = nullptr;   // this slot's kernels done
   std::vector<std::pair<Request*, size_t>> items;
   std::vector<xc_pair> pairs;
   bool busy = false;
@@ -66,6 +67,7 @@ struct Server {
   std::thread sched;
   Slot slots[NSLOTS];
   uint64_t launch_seq = 0;
+  cudaEvent_t last_kend = nullptr;   // kernels of the last launched batch done
   std::vector<double> lat_ms;
   uint64_t completed = 0, pairs_done = 0;
   int device = 0;
@@ -172,7 +174,15 @@ static void scheduler(Server* S) {
       lk.unlock();
       if (!free_slot->pairs.empty()) {
         int r = batch_pack(S->ctx, free_slot->b, free_slot->pairs.data(), free_slot->pairs.size(), free_slot->s);
+        // The slots' kernels run one batch after another: the host-to-device
+        // copy above still overlaps the batch before, but two batches' kernels
+        // sharing the SMs ran 27% slower (a correlation CTA needs a whole SM's
+        // shared memory, so it waits for every scan CTA there to finish).
+        if (r == XC_OK && S->last_kend && cudaStreamWaitEvent(free_slot->s, S->last_kend, 0) != cudaSuccess)
+          r = XC_ERR_CUDA;
         if (r == XC_OK) r = batch_run(S->ctx, free_slot->b, free_slot->s, false);
+        if (r == XC_OK && cudaEventRecord(free_slot->kend, free_slot->s) != cudaSuccess) r = XC_ERR_CUDA;
+        if (r == XC_OK) S->last_kend = free_slot->kend;
         if (r == XC_OK && cudaEventRecord(free_slot->ev, free_slot->s) != cudaSuccess) r = XC_ERR_CUDA;
         free_slot->busy = true;
         free_slot->seq = ++S->launch_seq;
@@ -232,7 +242,8 @@ static int server_start(Ctx* c) {
   for (auto& sl : S->slots) {
     sl.b = new_batch(c);
     if (cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.kend, cudaEventDisableTiming) != cudaSuccess) {
       delete S;
       return XC_ERR_CUDA;
     }
@@ -256,6 +267,7 @@ void server_stop(Ctx* c) {
     if (sl.s) cudaStreamSynchronize(sl.s);
     delete sl.b;
     if (sl.ev) cudaEventDestroy(sl.ev);
+    if (sl.kend) cudaEventDestroy(sl.kend);
     if (sl.s) cudaStreamDestroy(sl.s);
   }
   for (auto& kv : S->reqs) delete kv.second;
