@@ -34,7 +34,9 @@ struct Request {
   std::vector<xc_pair> pairs;
   size_t next = 0;          // next pair to schedule
   size_t done = 0;          // pairs with results
-  std::vector<std::vector<xc_result>> per_pair;
+  // Results in pair order: a request's pairs are scheduled in order and
+  // batches retire oldest first, so each batch appends the next ones.
+  std::vector<xc_result> results;
   int status = XC_OK;
   bool complete = false;
   size_t footprint = 0;     // device bytes accounted at admission
@@ -103,10 +105,13 @@ static void complete_slot(Server* S, Slot& sl) {
   size_t o = 0;
   for (size_t i = 0; i < n; i++) {
     Request* q = sl.items[i].first;
-    const size_t pi = sl.items[i].second;
     if (r == XC_OK) {
-      q->per_pair[pi].assign(res.begin() + o, res.begin() + o + counts[i]);
-      o += counts[i];
+      // one append per run of this request's consecutive pairs
+      size_t j = i, cnt = 0;
+      while (j < n && sl.items[j].first == q) cnt += counts[j++];
+      q->results.insert(q->results.end(), res.begin() + o, res.begin() + o + cnt);
+      o += cnt;
+      for (; i + 1 < j; i++) q->done++;   // all but the last of the run; the last below
     } else {
       q->status = r;
     }
@@ -321,7 +326,7 @@ int xc_submit(xc_ctx* c, const xc_pair* pairs, size_t n, uint64_t* ticket) {
     p.qseq = q->bytes.data() + o;
     o += p.qlen;
   }
-  q->per_pair.resize(n);
+  q->results.reserve(n * 4);
   std::unique_lock<std::mutex> lk(S->mu);
   if (S->stop) {
     delete q;
@@ -360,15 +365,10 @@ int xc_wait(xc_ctx* c, uint64_t ticket, int timeout_ms, xc_result* out, size_t c
     delete q;
     return st;
   }
-  size_t need = 0;
-  for (auto& v : q->per_pair) need += v.size();
+  const size_t need = q->results.size();
   if (n_out) *n_out = need;
   if (need > cap || (!out && need)) return XC_ERR_CAPACITY;
-  size_t o = 0;
-  for (auto& v : q->per_pair) {
-    if (!v.empty()) memcpy(out + o, v.data(), v.size() * sizeof(xc_result));
-    o += v.size();
-  }
+  if (need) memcpy(out, q->results.data(), need * sizeof(xc_result));
   S->reqs.erase(it);
   delete q;
   return XC_OK;
