@@ -350,7 +350,7 @@ Batch::~Batch() {
   cudaFree(d_res); cudaFree(d_rescnt); cudaFree(d_ovf); cudaFree(d_misc); cudaFree(d_base);
   cudaFree(d_dense); cudaFree(d_dbg); cudaFree(d_dbg_sig); cudaFree(d_dbg_xc); cudaFree(d_acc); cudaFree(d_fb);
   cudaFreeHost(h_pool); cudaFreeHost(h_desc); cudaFreeHost(h_base); cudaFreeHost(h_dense);
-  cudaFreeHost(h_misc); cudaFreeHost(h_ovf);
+  cudaFreeHost(h_misc); cudaFreeHost(h_ovf); cudaFreeHost(h_flags);
 }
 
 // Packs pairs into the batch's pinned staging and device buffers (async H2D
@@ -358,6 +358,7 @@ Batch::~Batch() {
 int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t stream) {
   if (n > (size_t)INT32_MAX / 4) return XC_ERR_ARG;
   b->n = (int)n;
+  b->rb_pending = false;
   b->meta.assign(pairs, pairs + n);
   b->order.resize(n);
   b->log2L.resize(n);
@@ -572,39 +573,63 @@ int batch_run(Ctx* c, Batch* b, cudaStream_t s, bool use_graph, bool timed) {
   return XC_OK;
 }
 
+int batch_readback_async(Ctx* c, Batch* b, cudaStream_t s) {
+  (void)c;
+  const int n = b->n, nslots = 2 * n;
+  int r;
+  if ((r = host_grow(b->h_base, b->cap_h_base, (size_t)nslots + 1)) != XC_OK) return r;
+  if ((r = host_grow(b->h_misc, b->cap_h_misc, 4)) != XC_OK) return r;
+  if ((r = host_grow(b->h_flags, b->cap_h_flags, (size_t)n)) != XC_OK) return r;
+  size_t est = std::max(b->est_dense, (size_t)4 * n);
+  est = std::min(est, b->cap_dense);
+  if ((r = host_grow(b->h_dense, b->cap_h_dense, est + 1)) != XC_OK) return r;
+  XC_CHECK(cudaMemcpyAsync(b->h_base, b->d_base, (nslots + 1) * sizeof(int), cudaMemcpyDeviceToHost, s));
+  XC_CHECK(cudaMemcpyAsync(b->h_misc, b->d_misc, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  XC_CHECK(cudaMemcpyAsync(b->h_flags, b->d_flags, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  if (est) XC_CHECK(cudaMemcpyAsync(b->h_dense, b->d_dense, est * sizeof(DevResult), cudaMemcpyDeviceToHost, s));
+  b->pre_dense = est;
+  b->rb_pending = true;
+  return XC_OK;
+}
+
 // Reads results back and assembles xc_result records in original pair order.
 int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, size_t* n_out,
                   size_t* pair_counts) {
   const int n = b->n, nslots = 2 * n;
-  XC_CHECK(cudaMemcpyAsync(b->h_base, b->d_base, (nslots + 1) * sizeof(int), cudaMemcpyDeviceToHost, s));
-  XC_CHECK(cudaMemcpyAsync(b->h_misc, b->d_misc, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  int r;
+  if (!b->rb_pending && (r = batch_readback_async(c, b, s)) != XC_OK) return r;
   XC_CHECK(cudaStreamSynchronize(s));
+  b->rb_pending = false;
   const int total = b->h_base[nslots];
   const int novf = b->h_misc[0];
   const int err = b->h_misc[1];
+  uint64_t d2h = (uint64_t)(nslots + 1) * sizeof(int) + 4 * sizeof(int) + (uint64_t)n * sizeof(uint32_t) +
+                 (uint64_t)b->pre_dense * sizeof(DevResult);
   if (err & 1) return XC_ERR_CAPACITY;   // caller re-runs with a bigger overflow pool
   if (err & 4) {
     fprintf(stderr, "satsuma2_gb300: scan kernel: inconsistent segment bounds\n");
     return XC_ERR_CUDA;
   }
-  int r;
-  if ((r = host_grow(b->h_dense, b->cap_h_dense, (size_t)total + 1)) != XC_OK) return r;
-  if (total) XC_CHECK(cudaMemcpyAsync(b->h_dense, b->d_dense, total * sizeof(DevResult), cudaMemcpyDeviceToHost, s));
-  std::vector<int> flags(n);
-  XC_CHECK(cudaMemcpyAsync(flags.data(), b->d_flags, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  b->est_dense = (size_t)total + (size_t)total / 4;
+  const bool again = (size_t)total > b->pre_dense;   // the estimate fell short: read all of them
+  if (again) {
+    if ((r = host_grow(b->h_dense, b->cap_h_dense, (size_t)total + 1)) != XC_OK) return r;
+    XC_CHECK(cudaMemcpyAsync(b->h_dense, b->d_dense, total * sizeof(DevResult), cudaMemcpyDeviceToHost, s));
+    d2h += (uint64_t)total * sizeof(DevResult);
+  }
   std::vector<DevResultX> ovf;
   if (novf > 0) {
     ovf.resize(novf);
     XC_CHECK(cudaMemcpyAsync(ovf.data(), b->d_ovf, novf * sizeof(DevResultX), cudaMemcpyDeviceToHost, s));
+    d2h += (uint64_t)novf * sizeof(DevResultX);
   }
-  XC_CHECK(cudaStreamSynchronize(s));
-  b->d2h_bytes = (uint64_t)(nslots + 1) * sizeof(int) + 4 * sizeof(int) + (uint64_t)total * sizeof(DevResult) +
-                 (uint64_t)n * sizeof(uint32_t) + (uint64_t)novf * sizeof(DevResultX);
+  if (again || novf > 0) XC_CHECK(cudaStreamSynchronize(s));
+  b->d2h_bytes = d2h;
   c->last_h2d = b->h2d_bytes;
   c->last_d2h = b->d2h_bytes;
   for (int d = 0; d < n; d++)
-    if (flags[d] & PF_INVALID) return XC_ERR_INPUT;
-  // per slot record lists (device order)
+    if (b->h_flags[d] & PF_INVALID) return XC_ERR_INPUT;
+  // per slot record lists of the overflow pool (device order)
   std::vector<std::vector<DevResult>> extra;
   std::vector<int> extra_of;
   if (novf > 0) {
@@ -638,20 +663,26 @@ int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, 
   if (need > cap || (!out && need)) return XC_ERR_CAPACITY;
   size_t o = 0;
   const int qchunk = c->prm.q_chunk;
+  std::vector<DevResult> merged;
   for (int i = 0; i < n; i++) {
     const int d = dev_of[i];
     const xc_pair& p = b->meta[i];
     for (int s2 = 0; s2 < 2; s2++) {
       const int sl = 2 * d + s2;
-      std::vector<DevResult> recs(b->h_dense + b->h_base[sl], b->h_dense + b->h_base[sl + 1]);
-      if (novf > 0 && extra_of[sl] >= 0) {
+      const DevResult* rec = b->h_dense + b->h_base[sl];
+      size_t nrec = (size_t)(b->h_base[sl + 1] - b->h_base[sl]);
+      if (novf > 0 && extra_of[sl] >= 0) {   // slot records plus its overflow records, reordered
         const auto& e = extra[extra_of[sl]];
-        recs.insert(recs.end(), e.begin(), e.end());
-        std::sort(recs.begin(), recs.end(), [](const DevResult& a, const DevResult& q) {
+        merged.assign(rec, rec + nrec);
+        merged.insert(merged.end(), e.begin(), e.end());
+        std::sort(merged.begin(), merged.end(), [](const DevResult& a, const DevResult& q) {
           return a.key < q.key || (a.key == q.key && a.tstart < q.tstart);
         });
+        rec = merged.data();
+        nrec = merged.size();
       }
-      for (const DevResult& rr : recs) {
+      for (size_t j = 0; j < nrec; j++) {
+        const DevResult& rr = rec[j];
         xc_result& x = out[o++];
         memset(&x, 0, sizeof(x));
         // FilterMatches coordinate mapping (HomologyByXCorrSlave.cc:175-181, RCQuery :56-60)
@@ -719,6 +750,7 @@ int ctx_align_pipelined(Ctx* c, const xc_pair* pairs, size_t n, xc_result* out, 
     const cudaStream_t s = c->work_stream[k & 1];
     int r = batch_pack(c, b, pairs + lo, m, s);
     if (r == XC_OK) r = batch_run(c, b, s, false);
+    if (r == XC_OK) r = batch_readback_async(c, b, s);
     return r;
   };
   auto finish = [&](size_t k) -> int {

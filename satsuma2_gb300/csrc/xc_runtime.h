@@ -54,6 +54,10 @@ struct Batch {
   PairDesc* h_desc = nullptr;     size_t cap_h_desc = 0;
   int* h_base = nullptr;          size_t cap_h_base = 0;
   DevResult* h_dense = nullptr;   size_t cap_h_dense = 0;
+  uint32_t* h_flags = nullptr;    size_t cap_h_flags = 0;
+  size_t pre_dense = 0;           // dense records the queued read-back copies
+  size_t est_dense = 0;           // estimate for the next read-back (last total + 25%)
+  bool rb_pending = false;        // batch_readback_async queued, not yet collected
   int* h_misc = nullptr;          size_t cap_h_misc = 0;
   DevResultX* h_ovf = nullptr;
 
@@ -104,6 +108,9 @@ int pair_log2L(const xc_params& p, const xc_pair& q);
 Batch* new_batch(Ctx* c);
 int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t stream);
 int batch_run(Ctx* c, Batch* b, cudaStream_t s, bool use_graph, bool timed = false);
+// Queues the result read-back (counts, flags, an estimate of the dense
+// records) on s behind the batch's kernels; batch_collect then waits once.
+int batch_readback_async(Ctx* c, Batch* b, cudaStream_t s);
 int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, size_t* n_out,
                   size_t* pair_counts);
 int batch_launch_count(const Ctx* c, const Batch* b);

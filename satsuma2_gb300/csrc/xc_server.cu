@@ -188,6 +188,7 @@ static void scheduler(Server* S) {
         if (r == XC_OK) r = batch_run(S->ctx, free_slot->b, free_slot->s, false);
         if (r == XC_OK && cudaEventRecord(free_slot->kend, free_slot->s) != cudaSuccess) r = XC_ERR_CUDA;
         if (r == XC_OK) S->last_kend = free_slot->kend;
+        if (r == XC_OK) r = batch_readback_async(S->ctx, free_slot->b, free_slot->s);
         if (r == XC_OK && cudaEventRecord(free_slot->ev, free_slot->s) != cudaSuccess) r = XC_ERR_CUDA;
         free_slot->busy = true;
         free_slot->seq = ++S->launch_seq;
