@@ -388,7 +388,11 @@ def run_ours(args):
     serve_run(xs, items, total=4096)   # warm
     # saturating: 8 client threads, each request one grid block of 24 x 24
     # chunk pairs (the slave's t_pair unit), as many in flight as admitted
-    served, p50_sat, p99_sat = serve_run(xs, items, n_threads=8, req_pairs=576, total=576 * 256)
+    # (three runs of 147k pairs, ~80 ms each; the median run is reported:
+    #  single runs vary by about 10% with host thread scheduling)
+    runs = sorted((serve_run(xs, items, n_threads=8, req_pairs=576, total=576 * 256) for _ in range(3)),
+                  key=lambda r: r[0])
+    served, p50_sat, p99_sat = runs[1]
     xs.close()
     # latency at a fixed arrival rate: each client has a waiter thread that
     # blocks on its oldest ticket, so a result is timed when it is ready
@@ -430,7 +434,7 @@ def run_ours(args):
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "results_match_device_run": bool(same)},
         "plain_pairs_per_s": plain, "served_pairs_per_s": served, "served_vs_plain": served / plain,
-        "served_request_pairs": 576, "latency_request_pairs": 16,
+        "served_request_pairs": 576, "served_runs": "median of 3", "latency_request_pairs": 16,
         "served_p50_ms_saturated": p50_sat, "served_p99_ms_saturated": p99_sat,
         "p50_ms": p50, "p99_ms": p99, "latency_arrival_rate_pairs_per_s": rate,
         "latency_clients": "8 submitters at Poisson arrivals, each with a waiter thread on its oldest ticket",
