@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
   __shared__ int s_hist[64];
   __shared__ int s_wsum[NWARP];
   __shared__ int s_next, s_res, s_qn;
-  __shared__ int s_cy_d[2], s_cy_w[2], s_cy_g[2], s_cy_start[2];
+  __shared__ int s_cy_start[2];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int pidx = P.first + blockIdx.x;
@@ -528,7 +528,7 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
       // item index of this diagonal's first marked word: CTA exclusive scan
       const int nincl = warp_incl_sum(nb, lane);
       if (lane == 31) s_wsum[warp] = nincl;
-      if (tid == 0) s_cy_d[1] = -1;   // nothing carried into the first sub-range
+      if (tid == 0) s_cy_start[1] = -1;   // no run open into the first sub-range
       __syncthreads();
       int ibase = nincl - nb, total = 0;
 #pragma unroll
@@ -565,40 +565,41 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
         }
         __syncthreads();
 
-        // ---- phase A (thread = item): the word's exact window bits ----
-        for (int i = tid; i < n; i += NT_SCAN) {
-          const uint32_t it = items[i];
+        // ---- phase AB (thread = item): the word's exact window bits, the bit
+        //      of the check before it, and the falls and closing ends of its
+        //      runs, queued as (item, bit) descriptors.  The check before the
+        //      word (bit 31 of the previous word) is tested from the same
+        //      equality words: its window is bits 18..63 of e2:e1, and a
+        //      passing check lies in a marked word, so a run crossing into the
+        //      word always comes from the item before it (or the carry). ----
+        constexpr uint32_t IT_PREV = 1u << 31;    // items[i]: the check before the word passes
+        constexpr uint32_t IT_DEFER = 1u << 30;   // items[i]: its segments did not fit the queue
+        constexpr uint32_t NO_SEG = 0xffffffffu;  // queue slot of a deferred item
+        const int cy = par ^ 1;   // carry slot written by the previous sub-range
+        // falls and closing end of item i (word bits g, previous-check bit pb)
+        auto runs_of = [&](uint32_t it, uint32_t g, uint32_t pb, uint32_t& fall, bool& close) {
           const int d = (int)(it & 127u), wr = (int)((it >> 7) & 1023u);
           const int p = dpos[d];
           const int cf = max(0, -p) + 46, cl = min(T - 1, Q - p) - 1;
-          const int w = (cf >> 5) + wr;
-          uint32_t e2, e1, e0;
-          ewords3(p, w, e2, e1, e0);
-          const uint32_t g = exact_word(e2, e1, e0);
-          const int lo = max(cf - 32 * w, 0), hi = min(cl - 32 * w, 31);
-          gbits[i] = g & (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
-        }
-        __syncthreads();
-
-        // ---- phase B (thread = item): falls and closing ends of runs of
-        //      passing checks, queued as (item, bit) descriptors.
-        const int cy = par ^ 1;   // carry slot written by the previous sub-range
-        auto prev_bit = [&](int i, int d, int wr) -> uint32_t {
-          if (i > 0) {
-            const uint32_t pv = items[i - 1];
-            return ((int)(pv & 127u) == d && (int)((pv >> 7) & 1023u) == wr - 1) ? (gbits[i - 1] >> 31) : 0u;
-          }
-          return (s_cy_d[cy] == d && s_cy_w[cy] == wr - 1) ? ((uint32_t)s_cy_g[cy] >> 31) : 0u;
+          const int cw = 32 * ((cf >> 5) + wr);
+          const int lo = max(cf - cw, 0), hi = min(cl - cw, 31);
+          const uint32_t vm = (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
+          fall = ~g & ((g << 1) | pb) & vm;
+          // a run still open at the word's last valid check ends at the
+          // diagonal's end or at the first check of an unmarked next word
+          close = ((g >> hi) & 1u) &&
+                  (cw + hi == cl || !((wmask[((wr + 1) >> 5) * NT_SCAN + d] >> ((wr + 1) & 31)) & 1u));
         };
         // check position where the run holding bit u-1 of item i began
-        auto run_start = [&](int i, int d, int wr, uint32_t g, int u) -> int {
-          uint32_t rb = g & ~((g << 1) | prev_bit(i, d, wr)) & lowmask(u);
+        auto run_start = [&](int i, uint32_t g, int u) -> int {
+          uint32_t rb = g & ~((g << 1) | (items[i] >> 31)) & lowmask(u);
           while (!rb) {
             if (--i < 0) return s_cy_start[cy];
-            wr = (int)((items[i] >> 7) & 1023u);
             g = gbits[i];
-            rb = g & ~((g << 1) | prev_bit(i, d, wr));
+            rb = g & ~((g << 1) | (items[i] >> 31));
           }
+          const uint32_t it = items[i];
+          const int d = (int)(it & 127u), wr = (int)((it >> 7) & 1023u);
           return 32 * (((max(0, -dpos[d]) + 46) >> 5) + wr) + (31 - __clz((int)rb));
         };
         // segment ending at bit u (0..31: a fall; 32: the closing end) of item i
@@ -615,7 +616,7 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
             s1 = cw + hi == cl ? ie : cw + 32;
             ub = hi + 1;
           }
-          const int s0 = run_start(i, d, wr, g, ub) - 45;
+          const int s0 = run_start(i, g, ub) - 45;
           if (s0 < 1 || s1 <= s0) {   // cannot happen: a run start precedes its end
             atomicOr(P.err, 4);
             return;
@@ -629,51 +630,66 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
           if (i < n) {
             const uint32_t it = items[i];
             const int d = (int)(it & 127u), wr = (int)((it >> 7) & 1023u);
-            const uint32_t g = gbits[i];
             const int p = dpos[d];
             const int cf = max(0, -p) + 46, cl = min(T - 1, Q - p) - 1;
-            const int cw = 32 * ((cf >> 5) + wr);
-            const int lo = max(cf - cw, 0), hi = min(cl - cw, 31);
-            const uint32_t vm = (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
-            fall = ~g & ((g << 1) | prev_bit(i, d, wr)) & vm;
-            // a run still open at the word's last valid check ends at the
-            // diagonal's end or at the first check of an unmarked next word
-            if ((g >> hi) & 1u)
-              close = cw + hi == cl || !((wmask[((wr + 1) >> 5) * NT_SCAN + d] >> ((wr + 1) & 31)) & 1u);
-            if (i == n - 1) {   // carried into the next sub-range
-              s_cy_d[par] = d;
-              s_cy_w[par] = wr;
-              s_cy_g[par] = (int)g;
-              s_cy_start[par] = (g >> 31) ? run_start(i, d, wr, g, 32) : -1;
-            }
+            const int w = (cf >> 5) + wr;
+            uint32_t e2, e1, e0;
+            ewords3(p, w, e2, e1, e0);
+            const int lo = max(cf - 32 * w, 0), hi = min(cl - 32 * w, 31);
+            const uint32_t g = exact_word(e2, e1, e0) & (0xffffffffu >> (31 - hi)) & (0xffffffffu << lo);
+            const uint32_t pb =
+                (32 * w - 1 >= cf && __popcll((((uint64_t)e1 << 32) | e2) >> 18) >= MIN_HITS) ? 1u : 0u;
+            gbits[i] = g;
+            items[i] = it | (pb ? IT_PREV : 0u);
+            runs_of(it, g, pb, fall, close);
           }
           const int nseg = __popc(fall) + (close ? 1 : 0);
           const int sincl = warp_incl_sum(nseg, lane);
           int q = 0;
           if (lane == 31 && sincl) q = atomicAdd(&s_qn, sincl);
           q = __shfl_sync(FULL, q, 31) + sincl - nseg;
-          auto enqueue = [&](int u) {
-            if (q < QCAP)
-              queue[q] = (uint32_t)i | ((uint32_t)u << 12);
-            else
-              segment(i, u);   // full queue: in place
-            q++;
-          };
-          while (fall) {
-            const int u = __ffs(fall) - 1;
-            fall &= fall - 1;
-            enqueue(u);
+          if (nseg && q + nseg > QCAP) {
+            // does not fit: the item's segments run in place after the barrier
+            for (int x = q; x < min(q + nseg, QCAP); x++) queue[x] = NO_SEG;
+            items[i] |= IT_DEFER;
+          } else {
+            while (fall) {
+              const int u = __ffs(fall) - 1;
+              fall &= fall - 1;
+              queue[q++] = (uint32_t)i | ((uint32_t)u << 12);
+            }
+            if (close) queue[q] = (uint32_t)i | (32u << 12);
           }
-          if (close) enqueue(32);
         }
         __syncthreads();
 
+        // ---- the run open at the sub-range's end, carried into the next ----
+        if (tid == 0) {
+          const uint32_t g = gbits[n - 1];
+          s_cy_start[par] = (g >> 31) ? run_start(n - 1, g, 32) : -1;
+        }
+
         // ---- phase C (thread = segment): run start, equal-base count,
-        //      FilterMatches.
+        //      FilterMatches; then the deferred items in place. ----
         const int qn = min(s_qn, QCAP);
         for (int e = tid; e < qn; e += NT_SCAN) {
           const uint32_t sg = queue[e];
-          segment((int)(sg & 4095u), (int)(sg >> 12));
+          if (sg != NO_SEG) segment((int)(sg & 4095u), (int)(sg >> 12));
+        }
+        if (s_qn > QCAP) {
+          for (int i = tid; i < n; i += NT_SCAN) {
+            const uint32_t it = items[i];
+            if (!(it & IT_DEFER)) continue;
+            uint32_t fall;
+            bool close;
+            runs_of(it, gbits[i], it >> 31, fall, close);
+            while (fall) {
+              const int u = __ffs(fall) - 1;
+              fall &= fall - 1;
+              segment(i, u);
+            }
+            if (close) segment(i, 32);
+          }
         }
         __syncthreads();
         if (tid == 0) s_qn = 0;

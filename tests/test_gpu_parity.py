@@ -30,10 +30,11 @@ _CTX = {}
 
 def ctx_for(case):
     import satsuma2_gb300 as sg
+    from satsuma2_gb300 import build
     key = (case["cutoff"], case["min_prob"], case["target_total"], case["min_len"], case["query_chunk"],
            case["L"], case["probtable"], case["probtable_cutoff"])
     if key not in _CTX:
-        sg.build.build()
+        build.build()
         _CTX[key] = sg.XCorr(cutoff=case["cutoff"], min_prob=case["min_prob"], target_total=case["target_total"],
                              min_len=case["min_len"], q_chunk=case["query_chunk"], fft_len=case["L"],
                              prob_table=bool(case["probtable"]), prob_table_cutoff=case["probtable_cutoff"])
@@ -398,3 +399,53 @@ def test_strand_kernel_switch_vs_oracle(O, monkeypatch):
             assert np.abs(xa - xb).max() <= 1e-4 * max(1.0, np.abs(xa).max())
     x1.close()
     x2.close()
+
+
+def _oscillating_pair():
+    """Target periodic in 64 bp; the query equals it exactly where a bit
+    pattern e is 1, so every diagonal at a multiple of 64 has equality bits e
+    (shifted).  e keeps the 46-wide window count at 18/19, flipping about ten
+    times per 32-check word, so those diagonals carry ~10 DoOne segments per
+    word where random ones carry ~1."""
+    n = 4096
+    rng = np.random.default_rng(38)
+    e = np.zeros(n, np.int64)
+    e[rng.choice(46, 19, replace=False)] = 1
+    W = int(e[:46].sum())
+    for c in range(46, n):
+        base = W - e[c - 46]
+        e[c] = 1 if W < 19 else 0
+        W = base + e[c]
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    rng2 = np.random.default_rng(5)
+    t = np.tile(acgt[rng2.integers(0, 4, 64)], n // 64)
+    code = {65: 0, 67: 1, 71: 2, 84: 3}
+    q = t.copy()
+    for i in np.nonzero(e == 0)[0]:
+        q[i] = acgt[(code[int(t[i])] + int(rng2.integers(1, 4))) % 4]
+    return t.tobytes(), q.tobytes()
+
+
+def test_scan_queue_overflow_vs_oracle(O):
+    """Sub-ranges of up to 1280 marked words, ~10 segments each on the
+    oscillating diagonals, against a queue of 2048 segment descriptors: the
+    items that do not fit run their segments in place after the barrier.  All
+    raw DoOne segments equal the oracle's on the GPU's offsets, and so do the
+    records."""
+    import satsuma2_gb300 as sg
+    t, q = _oscillating_pair()
+    TT = 4096.0 * 64
+    x = sg.XCorr(target_total=TT)
+    d = x.debug_pair(t=t, q=q, signals=False, seg_cap=1 << 19)
+    total = 0
+    for s, qq in enumerate((q, O.rc(q))):
+        want = [O.doone(t, qq, int(i) - 4096) for i in d["offsets"][s]]
+        want = np.concatenate(want) if want else np.zeros((0, 3), np.int32)
+        total += len(want)
+        assert np.array_equal(d["segments"][s].reshape(-1, 3), want.reshape(-1, 3)), s
+    assert total > 20 * 2048   # far more segments than a sub-range's queue holds
+    res = x.align([(t, q)])
+    P = O.params(target_total=TT)
+    want, _ = O.align_pair(P, O.pair(t, q), offsets_in=d["offsets"])
+    assert parity.same_results(res, want, target_total=TT)
+    x.close()

@@ -490,6 +490,14 @@ def model_doone_words4(t, q, pos, icap=4096):
     words = [w for w in range(wfirst, wlast + 1) if screen_word(eword(w - 2), eword(w - 1), eword(w))]
     marked = set(words)
     G = [exact_word(eword(w - 2), eword(w - 1), eword(w)) & vmask(w) for w in words]
+    # the kernel's bit of the check before each word, from the word's own
+    # equality words (window bits 18..63 of e2:e1), equals bit 31 of the
+    # previous word's exact bits when that word is marked, else 0
+    for k, w in enumerate(words):
+        U = (eword(w - 1) << 32) | eword(w - 2)
+        pb = int(32 * w - 1 >= cfirst and popc(U >> 18) >= MIN_HITS)
+        prev = (G[k - 1] >> 31) if k > 0 and words[k - 1] == w - 1 else 0
+        assert pb == prev, (pos, w)
 
     segs = []
     carry = None
