@@ -1,4 +1,4 @@
-// Internal definitions shared by the kernels (xc_kernels.cu) and the host
+// Internal definitions shared by the kernels (xc_corr.cu, xc_scan.cu) and the host
 // runtime (xc_runtime.cu).  Not part of the public ABI.
 #pragma once
 #include <cuda_runtime.h>
@@ -115,7 +115,7 @@ struct ScanParams {
   int dbg_cap;
 };
 
-// Launchers (xc_kernels.cu).
+// Launchers (xc_corr.cu, xc_scan.cu).
 cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t s);
 cudaError_t launch_scan(int log2L, const ScanParams& p, int npairs, cudaStream_t s);
 cudaError_t launch_finalize(const int* res_cnt, const DevResult* res, int slots, int nslots,

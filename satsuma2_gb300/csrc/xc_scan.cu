@@ -9,10 +9,11 @@
 //         block whose 49-position span holds >= 19 equal bases (the eight
 //         blocks of a word tested at once in byte lanes);
 //       items: the marked words of the round laid out contiguously per
-//         diagonal by a prefix sum, processed one per thread --
-//         phase A: the word's 32 exact window bits, four byte lanes at once;
-//         phase B: falls and closing ends of runs against the previous
-//           word's last bit, queued as (item, bit) with one atomic per warp;
+//         diagonal by a prefix sum, processed one per thread (phase AB): the
+//         word's 32 exact window bits, four byte lanes at once; the bit of
+//         the check before the word from the same equality words; falls and
+//         closing ends of runs, queued as (item, bit) with one atomic per
+//         warp (items that overrun the queue run in place after it);
 //       phase C (thread = segment): run start from the same word or by
 //         looking back, equal-base count, FP32 probability screen, exact FP64
 //         GetMatchProbability / PrintMatch for survivors.
