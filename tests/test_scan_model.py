@@ -558,3 +558,71 @@ def test_word4_model_matches_oracle_doone(O, icap):
             got = model_doone_words4(t, q, pos, icap)
             want = O.doone(t, q, pos)
             assert [g[:3] for g in got] == [tuple(x) for x in want.tolist()], (pos, icap)
+
+
+# ---------------------------------------------------------------------------
+# Bitplanes from 16-byte pieces and reverse-complement planes (build_planes
+# and the strand-1 construction in scan_kernel), 32-bit arithmetic as there.
+# ---------------------------------------------------------------------------
+def build_planes_model(buf, ln, nw):
+    """buf: the chunk bytes padded to 16 (bytes past ln are garbage)."""
+    p0 = [0] * nw
+    p1 = [0] * nw
+    half = {}
+    for c in range(2 * nw):
+        m0 = m1 = 0
+        if 16 * c < ln:
+            for k in range(4):
+                x = int.from_bytes(buf[16 * c + 4 * k:16 * c + 4 * k + 4], "little")
+                cd = ((x >> 1) ^ (x >> 2)) & 0x03030303
+                m0 |= ((((cd & 0x01010101) * 0x10204080) & M32) >> 28) << (4 * k)
+                m1 |= (((((cd >> 1) & 0x01010101) * 0x10204080) & M32) >> 28) << (4 * k)
+            valid = ln - 16 * c
+            if valid < 16:
+                m0 &= (1 << valid) - 1
+                m1 &= (1 << valid) - 1
+        half[c] = (m0, m1)
+    for j in range(nw):
+        (a0, a1), (b0, b1) = half[2 * j], half[2 * j + 1]
+        p0[j] = a0 | (b0 << 16)
+        p1[j] = a1 | (b1 << 16)
+    return p0, p1
+
+
+def brev32(x):
+    return int("{:032b}".format(x)[::-1], 2)
+
+
+def rc_planes_model(f0, f1, Q, nw):
+    r0, r1 = [0] * nw, [0] * nw
+    for w in range(nw):
+        lim = Q - 32 * w
+        if lim <= 0:
+            continue
+        s0 = lim - 32
+        if s0 >= 0:
+            fw, sh = s0 >> 5, s0 & 31
+            g0 = ((f0[fw + 1] << 32 | f0[fw]) >> sh) & M32
+            g1 = ((f1[fw + 1] << 32 | f1[fw]) >> sh) & M32
+        else:
+            g0 = (f0[0] << -s0) & M32
+            g1 = (f1[0] << -s0) & M32
+        m = lowmask(lim)
+        r0[w] = ~brev32(g0) & m & M32
+        r1[w] = ~brev32(g1) & m & M32
+    return r0, r1
+
+
+@pytest.mark.parametrize("n", [0, 1, 15, 16, 17, 31, 32, 33, 1000, 4095, 4096])
+def test_plane_build_and_reverse_complement(O, n):
+    rng = np.random.default_rng(90 + n)
+    seq = W.random_bases(rng, n).tobytes()
+    pad = (n + 15) // 16 * 16 + 16
+    buf = seq + bytes(rng.integers(0, 256, pad - n, dtype=np.uint8))   # garbage past the chunk
+    nw = 4096 // 32 + 2
+    want0, want1 = planes(seq, nw)
+    got0, got1 = build_planes_model(buf, n, nw)
+    assert got0 == want0[:nw] and got1 == want1[:nw]
+    rw0, rw1 = planes(O.rc(seq), nw)
+    r0, r1 = rc_planes_model(got0, got1, n, nw)
+    assert r0 == rw0[:nw] and r1 == rw1[:nw]
