@@ -16,6 +16,8 @@ JSON line (rank 0):
   roofline_scan DoOne window checks per second of the scan kernel, with its
                 integer-pipe use from the ncu capture under profiles/
   cpu_baseline  the reference CPU path on this host's cores (bounded sample)
+  other_configs device-resident throughput of the uneven-length batch (20000
+                pairs, FFT 1024..8192) and of 16384-bp chunks at FFT 32768
 
 --impl reference runs the reference's CPU implementation on the host cores
 (the compiled reference when it loads here, else the oracle restatement) and
@@ -402,6 +404,41 @@ def run_ours(args):
     _, p50, p99 = serve_run(xl, items, n_threads=8, req_pairs=16, total=16384, rate=rate, eager_wait=True)
     xl.close()
 
+    # ---- the other configurations, for reference (device-resident batches,
+    #      L2 flushed, median of 3 runs): uneven lengths over FFT buckets
+    #      1024..8192, and 16384-bp chunks at FFT 32768 ----
+    other = {}
+    try:
+        from satsuma2_gb300 import workloads as W
+
+        def device_rate(xc, its, reps=3):
+            b = xc.upload(its)
+            for _ in range(2):
+                b.run(sptr)
+            torch.cuda.synchronize()
+            ts = []
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            for _ in range(reps):
+                flush.zero_()
+                e0.record(stream)
+                b.run(sptr)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            b.free()
+            return len(its) / (float(np.median(ts)) / 1000.0)
+
+        u = W.uneven_batch(20000, seed=SEED + rank)
+        xu = sg.XCorr(fft_len=-1, target_total=float(sum(len(t) for t, _ in u)), device=local)
+        other["uneven_20000_pairs_fft_1024_8192_pairs_per_s"] = device_rate(xu, u)
+        xu.close()
+        lg = W.large_batch(2000, seed=SEED + rank)
+        xg = sg.XCorr(t_chunk=16384, q_chunk=16384, target_total=16384.0 * 2000, device=local)
+        other["large_2000_pairs_16384bp_fft_32768_pairs_per_s"] = device_rate(xg, lg)
+        xg.close()
+    except Exception as exc:   # informational only: never costs the main line
+        other["error"] = str(exc)[:200]
+
     peaks, peak_kind = measured_peaks()
     corr_ms = float(np.mean([s[0] for s in stage]))
     scan_ms = float(np.mean([s[1] for s in stage]))
@@ -458,6 +495,7 @@ def run_ours(args):
         "clocks": clocks,
         "cpu_baseline": cpu,
         "results_per_step": len(res_dev),
+        "other_configs": other,
     }
     print(json.dumps(out_line))
     if world > 1:
