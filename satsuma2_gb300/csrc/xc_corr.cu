@@ -82,9 +82,10 @@ __device__ __forceinline__ void hermitian_pack(float2* __restrict__ buf, const S
 // in increasing i.  Threads t < NT_CORR; warp w of them owns the contiguous
 // range [w*L/16, (w+1)*L/16), lanes stride by one.  Every thread of the CTA
 // calls it (two CTA barriers).
-template <int LOG2L>
+template <int LOG2L, class SY = CtaBarrier>
 __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, uint32_t off_base, int pidx,
-                                         int strand, const float2* __restrict__ buf, int t, int* s_warp) {
+                                         int strand, const float2* __restrict__ buf, int t, int* s_warp,
+                                         SY sync = SY()) {
   constexpr int L = 1 << LOG2L;
   constexpr int N = L >> 1;
   const int lane = t & 31, warp = t >> 5;
@@ -155,7 +156,7 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
     if (P.dbg_xc) P.dbg_xc[(size_t)(pidx * 2 + strand) * L + i] = x;
   }
   if (lane == 0) s_warp[warp] = wcount;
-  __syncthreads();
+  sync();
   if (warp == 0) {
     const int v = lane < NT_CORR / 32 ? s_warp[lane] : 0;
     int w = v;
@@ -167,7 +168,7 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
     if (lane < NT_CORR / 32) s_warp[lane] = w - v;
     if (lane == NT_CORR / 32 - 1) P.off_cnt[pidx * 2 + strand] = w;
   }
-  __syncthreads();
+  sync();
   int run = s_warp[warp];
   int* out = P.off_list + off_base + (size_t)strand * L;
   const unsigned lt = (1u << lane) - 1u;
@@ -752,7 +753,10 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
       v.y = mul_round_f32(E, s_wf[1][k], s_wmo[1][k]);
       vv[which * NWIN + w] = v;
     }
-    __syncthreads();
+    // each half reads only the window values it wrote (target: 0..511, query:
+    // 512..1023), and fills only its own transform buffers
+    const GroupBarrier sb{7 + half, 512};
+    sb();
     // ---- 3b. z (threads 0..511) or w (512..1023) to its even buffer and
     //      times W_L^n to its odd buffer, as corr_kernel builds its z ----
     {
@@ -779,9 +783,12 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
         bO[sn] = cmul(make_float2(x, y), tw2(twLh, twLl, n));   // W_L^n, n < L/2
       }
     }
-    __syncthreads();
-    // ---- 3c. the four N-point transforms, 256 threads each ----
-    fft_forward<LOG2N>(ZE + (tid >> 8) * N, twNh, twNl, tid & 255, 256);
+    sb();
+    // ---- 3c. the four N-point transforms, 256 threads each, each group of
+    //      8 warps on its own named barrier (1..4) between passes ----
+    fft_forward<LOG2N, 0, GroupBarrier>(ZE + (tid >> 8) * N, twNh, twNl, tid & 255, 256,
+                                        GroupBarrier{1 + (tid >> 8), 256});
+    __syncthreads();   // the per-bin step reads across the groups
     // ---- 3d. per-bin step (CrossCorrelation::DoOne, CrossCorr.cc:477-492):
     //      bin 0 is the product of real values; bins N-1 and N keep the
     //      targets' own values, which the reference's loop leaves
@@ -853,11 +860,14 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
                           },
                           twLh, twLl, ht);
   }
-  __syncthreads();
-  fft_inverse<LOG2N>(buf, twNh, twNl, ht, NT_CORR);
+  // each half packs, inverts and scans its own buffer: named barriers 5, 6
+  const GroupBarrier hb{5 + half, NT_CORR};
+  hb();
+  fft_inverse<LOG2N, Plan<LOG2N>, Plan<LOG2N>::n - 1, GroupBarrier>(buf, twNh, twNl, ht, NT_CORR, hb);
 
   // ---- 5. FindTop, one strand per half ----
-  find_top<LOG2L>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, half, buf, ht, s_warp[half]);
+  find_top<LOG2L, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, half, buf, ht, s_warp[half],
+                                hb);
 }
 
 // ---------------------------------------------------------------------------

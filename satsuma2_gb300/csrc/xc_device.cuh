@@ -243,25 +243,37 @@ __host__ __device__ constexpr int plan_used() {   // sum of the log-radices of p
   return u;
 }
 
+// Barriers ending a transform pass: the whole CTA, or a named barrier over
+// a warp-aligned group of n threads that transforms its own buffer.
+struct CtaBarrier {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct GroupBarrier {
+  int id, n;   // id 1..15 (0 is __syncthreads), n a multiple of 32
+  __device__ __forceinline__ void operator()() const { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+};
+
 // Forward transform, natural order in, digit-reversed out (posof).  Every
-// thread of the CTA must call it: each pass ends in __syncthreads.
-template <int LOG2N, int s = 0>
-__device__ __forceinline__ void fft_forward(float2* buf, const float2* h, const float2* l, int t, int nt) {
+// thread of the barrier's group must call it: each pass ends in the barrier.
+template <int LOG2N, int s = 0, class SY = CtaBarrier>
+__device__ __forceinline__ void fft_forward(float2* buf, const float2* h, const float2* l, int t, int nt,
+                                            SY sync = SY()) {
   if constexpr (s < Plan<LOG2N>::n) {
     pass_lr<Plan<LOG2N>::lr(s), (1 << LOG2N), ((1 << LOG2N) >> plan_used<LOG2N, s>()), false>(buf, h, l, t, nt);
-    __syncthreads();
-    fft_forward<LOG2N, s + 1>(buf, h, l, t, nt);
+    sync();
+    fft_forward<LOG2N, s + 1, SY>(buf, h, l, t, nt, sync);
   }
 }
 
 // Inverse (unnormalised), digit-reversed in, natural order out: the forward
 // passes undone in reverse order.
-template <int LOG2N, class PL = Plan<LOG2N>, int s = PL::n - 1>
-__device__ __forceinline__ void fft_inverse(float2* buf, const float2* h, const float2* l, int t, int nt) {
+template <int LOG2N, class PL = Plan<LOG2N>, int s = PL::n - 1, class SY = CtaBarrier>
+__device__ __forceinline__ void fft_inverse(float2* buf, const float2* h, const float2* l, int t, int nt,
+                                            SY sync = SY()) {
   if constexpr (s >= 0) {
     pass_lr<PL::lr(s), (1 << LOG2N), ((1 << LOG2N) >> plan_used<LOG2N, s, PL>()), true>(buf, h, l, t, nt);
-    __syncthreads();
-    fft_inverse<LOG2N, PL, s - 1>(buf, h, l, t, nt);
+    sync();
+    fft_inverse<LOG2N, PL, s - 1, SY>(buf, h, l, t, nt, sync);
   }
 }
 
