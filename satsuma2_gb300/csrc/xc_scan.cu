@@ -704,43 +704,42 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
 // ---------------------------------------------------------------------------
 // Finalize: dense, ordered results
 // ---------------------------------------------------------------------------
-// dense_base[i] = sum_{j<i} min(cnt[j], slots); dense_base[n] = total.  One CTA.
+// dense_base[i] = sum_{j<i} min(cnt[j], slots); dense_base[n] = total.  One
+// CTA: each thread sums a run of ceil(n/1024) consecutive slots, one block
+// scan of the run sums, then each thread writes its run's bases.
 __global__ void __launch_bounds__(1024) count_scan_kernel(const int* __restrict__ cnt, int n, int slots,
                                                           int* __restrict__ base) {
   __shared__ int s_w[32];
-  __shared__ int s_carry;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) s_carry = 0;
+  const int per = (n + 1023) / 1024;
+  const int lo = min(tid * per, n), hi = min(lo + per, n);
+  int sum = 0;
+  for (int i = lo; i < hi; i++) sum += min(cnt[i], slots);
+  int incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) s_w[warp] = incl;
   __syncthreads();
-  for (int c0 = 0; c0 < n; c0 += 1024) {
-    const int i = c0 + tid;
-    const int v = i < n ? min(cnt[i], slots) : 0;
-    int incl = v;
+  if (warp == 0) {
+    const int x = s_w[lane];
+    int y = x;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const int u = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += u;
+      const int u = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y += u;
     }
-    if (lane == 31) s_w[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-      const int x = s_w[lane];
-      int y = x;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int u = __shfl_up_sync(0xffffffffu, y, o);
-        if (lane >= o) y += u;
-      }
-      s_w[lane] = y - x;
-    }
-    __syncthreads();
-    const int carry = s_carry;
-    if (i < n) base[i] = carry + s_w[warp] + incl - v;
-    __syncthreads();
-    if (tid == 1023) s_carry = carry + s_w[warp] + incl;
-    __syncthreads();
+    s_w[lane] = y - x;
   }
-  if (tid == 0) base[n] = s_carry;
+  __syncthreads();
+  int run = s_w[warp] + incl - sum;
+  for (int i = lo; i < hi; i++) {
+    base[i] = run;
+    run += min(cnt[i], slots);
+  }
+  if (tid == 1023) base[n] = run;   // the last thread's run ends at the total
 }
 
 // One warp per pair strand: order its slot records by (offset index, tstart)
