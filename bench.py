@@ -161,72 +161,161 @@ def sampled_window_checks(x, items, n=64):
     return tot / len(samp)
 
 
-def cpu_baseline(items, seconds=12.0, impl_hint=None):
-    """Reference CPU path on a bounded sample, all host threads."""
+def _ref_worker(conn, shard, fft_len, target_total, use_port):
+    """One single-threaded CPU process: the reference's own cross-correlation
+    path (oracle/_ref, compiled from the reference's sources) or, where that
+    library is absent, the oracle's C restatement, over its shard of pairs
+    each time the parent asks."""
     import oracle
-    threads = os.cpu_count() or 1
-    kind = "port"
-    sample = items[: max(threads * 4, 64)]
-    ref = None
-    try:
-        if os.path.exists(oracle.REF_SO):
-            ref = oracle.Reference()
-            kind = "reference"
-    except OSError:
-        ref = None
-    if ref is not None:
-        # reference CPU code, one pair per call across a thread pool
-        from concurrent.futures import ThreadPoolExecutor
+    if use_port:
+        O = oracle.Oracle()
+        P = O.params(target_total=target_total, fft_len=fft_len)
+        pairs = [O.pair(t, q) for t, q in shard]
 
-        def one(tq):
-            ref.align_pair(tq[0], tq[1], 8192, target_total=TARGET_TOTAL)
-            return 1
-        done, t0 = 0, time.time()
-        with ThreadPoolExecutor(threads) as ex:
-            while time.time() - t0 < seconds:
-                done += sum(ex.map(one, sample))
-        dt = time.time() - t0
-        return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": kind,
-                "sample": "%d uniform 4096x4096 pairs (FFT 8192), %d threads, %.1f s" % (done, threads, dt)}
-    O = oracle.Oracle()
-    P = O.params(target_total=TARGET_TOTAL)
-    pairs = [O.pair(t, q) for t, q in sample]
-    done, t0 = 0, time.time()
-    while time.time() - t0 < seconds:
-        O.align_batch(P, pairs, threads)
-        done += len(pairs)
-    dt = time.time() - t0
-    return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": "%d uniform 4096x4096 pairs (FFT 8192) through the C restatement of the reference "
-                      "CPU path, %d threads, %.1f s" % (done, threads, dt)}
+        def run(k):
+            O.align_batch(P, pairs[:k], 1)
+            return k
+    else:
+        ref = oracle.Reference()
+
+        def run(k):
+            for t, q in shard[:k]:
+                ref.align_pair(t, q, fft_len, target_total=target_total)
+            return k
+    conn.send("ready")
+    while True:
+        k = conn.recv()
+        if k is None:
+            return
+        conn.send(run(len(shard) if k < 0 else k))
+
+
+class RefPool:
+    """One single-threaded process per host core, each holding its shard of
+    the workload (round robin), started with spawn.  step(k) has every process
+    run its first k pairs (all of them for k < 0) and returns (pairs, seconds)
+    of wall time."""
+
+    def __init__(self, items, fft_len=8192, target_total=TARGET_TOTAL, procs=None):
+        import multiprocessing as mp
+        import oracle
+        self.use_port = not os.path.exists(oracle.REF_SO)
+        self.kind = "port" if self.use_port else "reference"
+        self.procs = procs or os.cpu_count() or 1
+        ctx = mp.get_context("spawn")
+        self.conns, self.ps = [], []
+        for k in range(self.procs):
+            a, b = ctx.Pipe()
+            pr = ctx.Process(target=_ref_worker, args=(b, items[k::self.procs], fft_len, target_total,
+                                                       self.use_port), daemon=True)
+            pr.start()
+            self.conns.append(a)
+            self.ps.append(pr)
+        for c, pr in zip(self.conns, self.ps):
+            if not c.poll(300) or c.recv() != "ready":
+                self.close()
+                raise RuntimeError("reference worker process %d did not start" % pr.pid)
+
+    def step(self, k=-1):
+        t0 = time.perf_counter()
+        for c in self.conns:
+            c.send(k)
+        done = sum(c.recv() for c in self.conns)
+        return done, time.perf_counter() - t0
+
+    def close(self):
+        for c in self.conns:
+            try:
+                c.send(None)
+            except OSError:
+                pass
+        for pr in self.ps:
+            pr.join(timeout=10)
+            if pr.is_alive():
+                pr.terminate()
+
+
+def host_cpu():
+    """(cores, CPU model) of this host."""
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return os.cpu_count() or 1, model
+
+
+def cpu_baseline(items, seconds=12.0):
+    """The reference CPU path on a bounded sample of the workload: one
+    single-threaded process per host core, repeated passes over 24 pairs per
+    process until about `seconds` have passed."""
+    cores, model = host_cpu()
+    per = 24
+    pool = RefPool(items[:per * cores])
+    try:
+        pool.step(1)   # warm: libraries loaded, tables built
+        done, dt = 0, 0.0
+        while dt < seconds:
+            n, t = pool.step(-1)
+            done += n
+            dt += t
+    finally:
+        pool.close()
+    what = ("the reference's own CPU code (oracle/_ref, compiled from its sources)" if pool.kind == "reference"
+            else "the oracle's C restatement of the reference CPU path (the compiled reference is absent)")
+    return {"value": done / dt, "unit": UNIT, "cores": cores, "kind": pool.kind,
+            "sample": "%d pairs of the uniform 4096x4096 workload (FFT 8192) through %s, one single-threaded "
+                      "process per core on %d cores (%s), %.1f s" % (done, what, cores, model, dt)}
 
 
 def run_reference(args):
+    """--impl reference: the reference's CPU implementation of the path over the
+    same 4096-pair workload, one single-threaded process per host core; each
+    step is one full pass over the batch."""
     rank, world, local = dist_env()
     if rank != 0:
         return 0
     items = workload()
-    vals = []
-    for _ in range(args.warmup):
-        pass
-    info = None
-    # each step a bounded sample; the whole run stays near a minute and a half
-    per_step = max(2.0, min(args.ref_seconds, 90.0 / max(1, args.steps)))
-    for _ in range(args.steps):
-        info = cpu_baseline(items, seconds=per_step)
-        vals.append(info["value"])
-    v = float(np.mean(vals))
+    cores, model = host_cpu()
+    pool = RefPool(items)
+    try:
+        for _ in range(args.warmup):
+            pool.step(-1)
+        ts = []
+        for _ in range(args.steps):
+            n, dt = pool.step(-1)
+            assert n == len(items)
+            ts.append(dt)
+    finally:
+        pool.close()
+    ms = 1000.0 * float(np.mean(ts))
+    v = len(items) / (ms / 1000.0)
+    what = ("the reference's own CPU code (oracle/_ref, compiled from its sources)" if pool.kind == "reference"
+            else "the oracle's C restatement of the reference CPU path (the compiled reference is absent)")
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * N_PAIRS / v,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-           "data": "synthetic (seeded)",
-           "config": {"workload": "batched uniform: %d pairs 4096x4096 bp, FFT 8192, cutoff 1.8, seed %d"
-                                  % (N_PAIRS, SEED), "parallelism": "host threads"},
-           "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": info["kind"],
-                            "sample": info["sample"]},
+           "data": "synthetic (seeded uniform batch, seed %d)" % SEED,
+           "config": bench_config(1),
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": pool.kind,
+                            "sample": "the full %d-pair batch per step through %s, one single-threaded process "
+                                      "per core on %d cores (%s)" % (len(items), what, cores, model)},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
     return 0
+
+
+def bench_config(world):
+    """The workload's config object, the same in both arms."""
+    return {"workload": "batched uniform: %d chunk pairs 4096x4096 bp, both strands, FFT 8192, "
+                        "cutoff 1.8, min_prob 0.99 (slave-faithful), seed %d" % (N_PAIRS, SEED),
+            "pairs_per_step": N_PAIRS, "fft_len": 8192, "target_total": TARGET_TOTAL,
+            "l2": "512 MB buffer written before every timed step (inputs 33.6 MB)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 def serve_run(x, items, n_threads=4, req_pairs=64, total=16384, rate=None, eager_wait=False):
@@ -463,11 +552,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded uniform batch, seed %d)" % SEED,
-        "config": {"workload": "batched uniform: %d chunk pairs 4096x4096 bp, both strands, FFT 8192, "
-                               "cutoff 1.8, min_prob 0.99 (slave-faithful)" % N_PAIRS,
-                   "pairs_per_step": N_PAIRS, "fft_len": 8192, "target_total": TARGET_TOTAL,
-                   "l2": "512 MB buffer written before every timed step",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": bench_config(world),
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "results_match_device_run": bool(same)},
         "plain_pairs_per_s": plain, "served_pairs_per_s": served, "served_vs_plain": served / plain,
@@ -503,6 +588,27 @@ def run_ours(args):
     return 0
 
 
+def profile_case(args):
+    """Fixed device-resident workload for profiler captures: uploads --pairs
+    seeded uniform 4096x4096 chunk pairs (FFT 8192) and runs the batch --runs
+    times without timing, so a profiler's launch list maps one-to-one onto
+    runs (each run: the correlation kernels, the scan kernel and the two
+    finalize kernels)."""
+    import satsuma2_gb300 as sg
+    from satsuma2_gb300 import build, workloads
+    build.build()
+    items = workloads.uniform_batch(args.pairs, seed=SEED)
+    x = sg.XCorr(target_total=TARGET_TOTAL)
+    b = x.upload(items)
+    for _ in range(args.runs):
+        b.run(ctypes.c_void_p(0))
+    res = b.results()
+    print("pairs %d runs %d results %d" % (args.pairs, args.runs, len(res)))
+    b.free()
+    x.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -511,7 +617,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="profiler workload only: upload --pairs pairs and run them --runs times, untimed")
+    ap.add_argument("--pairs", type=int, default=N_PAIRS)
+    ap.add_argument("--runs", type=int, default=3)
     args = ap.parse_args()
+    if args.profile_case:
+        return profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -132,7 +132,9 @@ int xc_transfer_stats(xc_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
 /* Serving: thread-safe submission of chunk pairs from any host thread (the
  * slave's -p workers), continuous batching on the device, and a bounded wait.
  * xc_submit returns XC_ERR_BUSY when admission is refused.  xc_wait returns
- * XC_ERR_TIMEOUT after timeout_ms without results; the ticket stays valid. */
+ * XC_ERR_TIMEOUT after timeout_ms without results, and XC_ERR_CAPACITY with
+ * *n_out > cap when out is too small; in both cases the ticket stays valid.
+ * Any other status (XC_OK included) releases the ticket. */
 int xc_submit(xc_ctx* ctx, const xc_pair* pairs, size_t n, uint64_t* ticket);
 int xc_wait(xc_ctx* ctx, uint64_t ticket, int timeout_ms, xc_result* out, size_t cap,
             size_t* n_out);
@@ -150,22 +152,23 @@ int xc_serving_stats(xc_ctx* ctx, double* p50_ms, double* p99_ms, uint64_t* comp
 int xc_debug_pair(xc_ctx* ctx, const xc_pair* pair, float* sig, float* xc, int* offs,
                   int* n_offs, int* segs, int* n_segs, int seg_cap, int* fft_len_out);
 
-/* One chunk pair, both strands, exactly as xc_align_pairs(ctx, pair, 1, ...)
- * computes it, but without allocating any device or pinned host memory.  No
- * counterpart in the reference: it is for callers that cannot call
- * cudaMalloc -- a process whose device memory belongs to another allocator
- * (a framework's caching allocator or a fixed arena holding the free HBM),
- * and latency-bound callers sharing the GPU, for whom cudaFree's device-wide
- * synchronisation is not acceptable.  The chunks, the kernels' scratch and
- * the results before read-back live in one static device array of 320 KiB
- * that every GPU loading the library holds until exit.  Limits: FFT length
- * at most 16384 (else XC_ERR_UNSUPPORTED) and at most 1024 kept matches per
- * strand (else XC_ERR_CAPACITY, with *n_out the count found).  The first
- * call on a device looks the array up (cudaGetSymbolAddress) with that
- * device current; make that first call before any stream capture.  Calls
- * share the array: each clears what must start at zero, and calls in one
- * process serialise and return only when their results are on the host;
- * calls that overlapped on the GPU would race on the array. */
+/* One chunk pair, both strands, through the same kernels as
+ * xc_align_pairs(ctx, pair, 1, ...) and with the same records, but without
+ * allocating any device or pinned host memory.  No counterpart in the
+ * reference: it is for callers that cannot call cudaMalloc -- a process whose
+ * device memory belongs to another allocator (a framework's caching allocator
+ * or a fixed arena holding the free HBM), and latency-bound callers sharing
+ * the GPU, for whom cudaFree's device-wide synchronisation is not acceptable.
+ * The chunks, the kernels' scratch and the results before read-back live in
+ * one static device array of 320 KiB that every GPU loading the library holds
+ * until exit.  Limits: FFT length at most 16384 (else XC_ERR_UNSUPPORTED) and
+ * at most 1024 kept matches per strand (else XC_ERR_CAPACITY, with *n_out the
+ * number of matches found).  The first call through a context looks the array
+ * up (cudaGetSymbolAddress) with the context's device current; make that
+ * first call before any stream capture.  Calls share the array: each clears
+ * what must start at zero, and calls in one process serialise and return only
+ * when their results are on the host; calls that overlapped on the GPU would
+ * race on the array. */
 int xc_align_pair_noalloc(xc_ctx* ctx, const xc_pair* pair, xc_result* out, size_t cap,
                           size_t* n_out);
 

@@ -5,10 +5,12 @@ Two libraries live here, both loaded through ctypes:
 * ``liboracle.so`` -- ``xcorr_oracle.c``, a plain-C restatement of the
   reference algorithm (FP64 cross-correlation, exact FindTop / DoOne /
   GetMatchProbability / FilterMatches).  It builds anywhere gcc exists.
-* ``_ref/libsatsuma_ref.so`` -- the reference's own sources compiled in place by
-  ``build_ref.sh`` together with ``ref_harness.cc``.  It only exists where the
-  reference tree is present (not on the GPU host); tests that need it skip
-  otherwise.
+* ``_ref/libsatsuma_ref.so`` -- the reference's own sources, unmodified,
+  compiled by ``build_ref.sh`` together with ``ref_harness.cc``.  The sources
+  come from the reference tree, or from the copy ``install_ref.sh`` leaves in
+  ``baseline/_ref/satsuma2`` (git-ignored), so the library can be rebuilt on a
+  machine without the reference tree; tests that need it skip where neither
+  exists.
 
 Only ``tests/``, ``tests/golden/make_golden.py``, ``__graft_entry__.smoke()`` and
 ``bench.py``'s CPU baseline legs may import this package.  The product package
@@ -24,6 +26,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsatsuma_ref.so")
 REF_SLAVE = os.path.join(HERE, "_ref", "HomologyByXCorrSlave")
+# where install_ref.sh puts the reference sources (git-ignored; travels with the tree)
+REF_INSTALL = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "satsuma2")
 
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
@@ -50,12 +54,34 @@ def build(force=False):
     return ORACLE_SO
 
 
-def build_ref(reference_root="/root/reference"):
-    """Builds _ref/ from the reference tree when it is present; else no-op."""
-    if not os.path.isdir(os.path.join(reference_root, "analysis")):
+def install_ref(reference_root=None):
+    """Copies the reference's CPU sources (unmodified) into baseline/_ref/satsuma2
+    with install_ref.sh; no-op where the reference tree is absent.
+    reference_root: None = install_ref.sh's default ($SATSUMA2_REFERENCE or the
+    reference checkout of the build machine)."""
+    args = ["sh", os.path.join(HERE, "install_ref.sh")]
+    if reference_root:
+        args.append(reference_root)
+    subprocess.check_call(args, stdout=subprocess.DEVNULL)
+    return REF_INSTALL if os.path.isdir(os.path.join(REF_INSTALL, "analysis")) else None
+
+
+def build_ref(reference_root=None):
+    """Builds _ref/ from a reference tree: reference_root, else
+    $SATSUMA2_REFERENCE, else the installed copy in baseline/_ref/satsuma2.
+    Returns the library path, or None when no tree is found.  The build is
+    reused while no source is newer than the library."""
+    root = reference_root or os.environ.get("SATSUMA2_REFERENCE") or REF_INSTALL
+    if not os.path.isfile(os.path.join(root, "analysis", "CrossCorr.cc")):
         return None
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), reference_root],
-                          stdout=subprocess.DEVNULL)
+    srcs = [os.path.join(HERE, "ref_harness.cc"), os.path.join(HERE, "build_ref.sh")]
+    for d in ("analysis", "base", "util"):
+        dd = os.path.join(root, d)
+        srcs += [os.path.join(dd, f) for f in os.listdir(dd)]
+    if (os.path.exists(REF_SO) and os.path.exists(REF_SLAVE)
+            and os.path.getmtime(REF_SO) >= max(os.path.getmtime(f) for f in srcs)):
+        return REF_SO
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), root], stdout=subprocess.DEVNULL)
     return REF_SO
 
 
@@ -300,17 +326,20 @@ class Reference:
         L = fft_len
         cap = 1 << 14
         res = np.zeros(cap, RESULT_DTYPE)
-        offs = np.zeros(2 * L, np.int32)
-        noffs = np.zeros(2, np.int32)
         scap = 1 << 16
-        segs = np.zeros(2 * 3 * scap, np.int32)
-        nsegs = np.zeros(2, np.int32)
-        xco = np.zeros(2 * L, np.float32)
         qsz = len(q) if query_size is None else query_size
+        if want_detail:
+            offs = np.zeros(2 * L, np.int32)
+            noffs = np.zeros(2, np.int32)
+            segs = np.zeros(2 * 3 * scap, np.int32)
+            nsegs = np.zeros(2, np.int32)
+            xco = np.zeros(2 * L, np.float32)
+            extra = (_ptr(offs), _ptr(noffs), L, _ptr(segs), _ptr(nsegs), scap, _ptr(xco))
+        else:   # records only: the reference path without stage copies
+            extra = (None, None, 0, None, None, 0, None)
         n = self.lib.ref_align_pair(t, len(t), t_chunk_start, target_id, q, len(q), q_chunk_start,
                                     query_id, qsz, L, cutoff, min_len, min_prob, target_total,
-                                    query_chunk, probtable, _ptr(res), cap, _ptr(offs), _ptr(noffs), L,
-                                    _ptr(segs), _ptr(nsegs), scap, _ptr(xco))
+                                    query_chunk, probtable, _ptr(res), cap, *extra)
         detail = None
         if want_detail:
             detail = {

@@ -187,12 +187,12 @@ struct Slave {
     size_t n = 0;
     for (;;) {
       r = xc_wait(ctx, ticket, 1000, out.data(), out.size(), &n);
-      if (r == XC_ERR_TIMEOUT) continue;
-      if (r == XC_ERR_CAPACITY) {
+      if (r == XC_ERR_TIMEOUT) continue;             // the ticket stays valid
+      if (r == XC_ERR_CAPACITY && n > out.size()) {   // buffer too small: the ticket stays valid
         out.resize(n);
         continue;
       }
-      break;
+      break;   // done, or failed: a failed ticket is released and never waited on again
     }
     if (r != XC_OK) {
       fprintf(stderr, "satsuma2_slave: block failed (%d)\n", r);

@@ -11,9 +11,12 @@
 // slots, counters) live in the file-scope array g_noalloc_scratch below, of
 // fixed size, which every GPU that loads the library holds until exit.
 //
-// Set-up: the first call on a device, with that device current, looks up the
-// array's device address with cudaGetSymbolAddress and keeps it; later calls
-// reuse it.  That first call should come before any stream capture.
+// Set-up: the first call through a context, with the context's device
+// current, looks up the array's device address with cudaGetSymbolAddress and
+// keeps it in the context; later calls through that context reuse it.  That
+// first call should come before any stream capture.  A device reset ends every
+// context of the library on that device (their tables are gone with it); a
+// context created afterwards looks the address up again.
 // Every call shares the array and leaves its contents behind: each call
 // zeroes the counters that must start at zero (offset counts, result counts,
 // the overflow and error words) before its first kernel.  Calls that overlap
@@ -34,7 +37,6 @@ namespace {
 constexpr int NA_MAX_LOG2L = 14;          // largest FFT length: 16384
 constexpr int NA_MAX_L = 1 << NA_MAX_LOG2L;
 constexpr int NA_SLOTS = 1024;              // kept matches per strand
-constexpr int NA_MAX_DEVICES = 64;
 
 // Byte layout of the scratch array (256-byte aligned pieces).
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -49,10 +51,15 @@ constexpr size_t NA_BYTES = NA_DENSE + align256((size_t)2 * NA_SLOTS * sizeof(De
 constexpr int C_OFFCNT = 0;   // [2] FindTop offsets per strand
 constexpr int C_FLAGS = 2;    // [1] pair flags
 constexpr int C_RESCNT = 4;   // [2] kept matches per strand
-constexpr int C_MISC = 8;     // [4] overflow count, error bits, debug count
+constexpr int C_MISC = 8;     // [4] overflow count, error bits, debug count, pairs handed back
 constexpr int C_BASE = 12;    // [3] dense result bases
+constexpr int C_FB = 15;      // [1] the pair index the both-strands kernel may hand back
 
 static_assert(NA_BYTES <= 320 * 1024, "scratch layout exceeds the stated 320 KiB maximum");
+// Every length accepted here keeps the correlation kernel's channel sums in
+// shared memory; longer ones would need the global scratch (CorrParams::acc)
+// that this entry point does not provide.
+static_assert(NA_MAX_LOG2L <= MAX_SMEM_LOG2L, "FFT lengths beyond one SM need a channel-sum scratch");
 
 }  // namespace
 
@@ -62,21 +69,20 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[320 * 1024];
 namespace {
 
 std::mutex g_noalloc_mu;                          // one call at a time per process
-unsigned char* g_noalloc_ptr[NA_MAX_DEVICES];     // device address per device, set once
 
-// Device address of the scratch array on the current device (looked up once).
-int noalloc_scratch(int device, unsigned char** out) {
-  if (device < 0 || device >= NA_MAX_DEVICES) return XC_ERR_ARG;
-  if (!g_noalloc_ptr[device]) {
+// Device address of the scratch array for this context's device, looked up
+// at the context's first call with that device current.
+int noalloc_scratch(Ctx* c, unsigned char** out) {
+  if (!c->noalloc_base) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) {
       fprintf(stderr, "satsuma2_gb300: cudaGetSymbolAddress(g_noalloc_scratch): %s\n", cudaGetErrorString(e));
       return XC_ERR_CUDA;
     }
-    g_noalloc_ptr[device] = static_cast<unsigned char*>(p);
+    c->noalloc_base = static_cast<unsigned char*>(p);
   }
-  *out = g_noalloc_ptr[device];
+  *out = c->noalloc_base;
   return XC_OK;
 }
 
@@ -103,7 +109,7 @@ int align_pair_noalloc(Ctx* c, const xc_pair& p, xc_result* out, size_t cap, siz
   if (p.tlen > (1 << lg) / 2 || p.qlen > (1 << lg) / 2) return XC_ERR_INPUT;
 
   unsigned char* base = nullptr;
-  int r = noalloc_scratch(c->device, &base);
+  int r = noalloc_scratch(c, &base);
   if (r != XC_OK) return r;
   PairDesc* d_desc = reinterpret_cast<PairDesc*>(base + NA_DESC);
   int* cnt = reinterpret_cast<int*>(base + NA_CNT);
@@ -146,6 +152,12 @@ int align_pair_noalloc(Ctx* c, const xc_pair& p, xc_result* out, size_t cap, siz
   cp.off_list = offl;
   cp.off_cnt = cnt + C_OFFCNT;
   cp.pair_flags = reinterpret_cast<uint32_t*>(cnt + C_FLAGS);
+  if (lg == PAIR_LOG2L && c->pair_kernel) {
+    // the same correlation kernels as xc_align_pairs: both strands in one
+    // CTA, or the per-strand kernel for a pair it hands back
+    cp.fb_list = cnt + C_FB;
+    cp.fb_cnt = cnt + C_MISC + 3;
+  }
   NA_CHECK(launch_corr(lg, cp, 1, s));
 
   ScanParams sp{};
@@ -181,16 +193,19 @@ int align_pair_noalloc(Ctx* c, const xc_pair& p, xc_result* out, size_t cap, siz
   NA_CHECK(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s));
   NA_CHECK(cudaStreamSynchronize(s));
   if (h[C_FLAGS] & PF_INVALID) return XC_ERR_INPUT;
-  if (h[C_MISC + 1] & 4) {
-    fprintf(stderr, "satsuma2_gb300: scan kernel: inconsistent segment bounds\n");
+  // error bits of the scan: bit 0 (records beyond the slots, no overflow pool
+  // here) is reported below as XC_ERR_CAPACITY; any other bit is a failure
+  if (h[C_MISC + 1] & ~1) {
+    fprintf(stderr, "satsuma2_gb300: xc_align_pair_noalloc: scan kernel error bits 0x%x\n", h[C_MISC + 1]);
     return XC_ERR_CUDA;
   }
   const int total = h[C_BASE + 2];
   const size_t need = (size_t)total + (size_t)h[C_MISC + 0];   // kept + beyond the slots
   if (n_out) *n_out = need;
   if (h[C_MISC + 0] > 0) {
-    fprintf(stderr, "satsuma2_gb300: xc_align_pair_noalloc: %zu kept matches on a strand exceed %d\n", need,
-            NA_SLOTS);
+    fprintf(stderr,
+            "satsuma2_gb300: xc_align_pair_noalloc: %zu matches found; a strand exceeds its %d kept slots\n",
+            need, NA_SLOTS);
     return XC_ERR_CAPACITY;
   }
   if (need > cap || (!out && need)) return XC_ERR_CAPACITY;

@@ -605,7 +605,7 @@ int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, 
   const int err = b->h_misc[1];
   uint64_t d2h = (uint64_t)(nslots + 1) * sizeof(int) + 4 * sizeof(int) + (uint64_t)n * sizeof(uint32_t) +
                  (uint64_t)b->pre_dense * sizeof(DevResult);
-  if (err & 1) return XC_ERR_CAPACITY;   // caller re-runs with a bigger overflow pool
+  if (err & 1) return XC_INTERNAL_OVERFLOW;   // the caller grows the pool and runs the batch again
   if (err & 4) {
     fprintf(stderr, "satsuma2_gb300: scan kernel: inconsistent segment bounds\n");
     return XC_ERR_CUDA;
@@ -704,19 +704,23 @@ int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, 
   return XC_OK;
 }
 
-int ctx_run_pairs(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, xc_result* out, size_t cap,
-                  size_t* n_out, size_t* pair_counts) {
-  int r = batch_pack(c, b, pairs, n, c->stream);
-  if (r != XC_OK) return r;
+int batch_rerun_overflow(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, size_t* n_out,
+                         size_t* pair_counts) {
   for (int attempt = 0; attempt < 3; attempt++) {
-    if ((r = batch_run(c, b, c->stream, false)) != XC_OK) return r;
-    r = batch_collect(c, b, c->stream, out, cap, n_out, pair_counts);
-    if (r != XC_ERR_CAPACITY || b->h_misc[1] == 0) return r;
-    // device overflow pool was too small: grow to what was asked and re-run
+    // the scan kernel counts every record it could not place, so the pool
+    // grows to at least what this run asked for; the captured graphs hold the
+    // old pool and capacity in their launch parameters
     b->ovf_cap = std::max(b->ovf_cap * 4, b->h_misc[0] + 1024);
-    if ((r = dev_grow(b->d_ovf, b->cap_ovf, (size_t)b->ovf_cap)) != XC_OK) return r;
+    b->graph_valid = false;
+    b->graph_timed_valid = false;
+    int r = dev_grow(b->d_ovf, b->cap_ovf, (size_t)b->ovf_cap);
+    if (r != XC_OK) return r;
+    if ((r = batch_run(c, b, s, false)) != XC_OK) return r;
+    r = batch_collect(c, b, s, out, cap, n_out, pair_counts);
+    if (r != XC_INTERNAL_OVERFLOW) return r;
   }
-  return XC_ERR_CAPACITY;
+  fprintf(stderr, "satsuma2_gb300: result overflow pool still full after three runs\n");
+  return XC_ERR_NOMEM;
 }
 
 // xc_align_pairs: the pairs run as sub-batches alternating between two
@@ -754,14 +758,14 @@ int ctx_align_pipelined(Ctx* c, const xc_pair* pairs, size_t n, xc_result* out, 
     return r;
   };
   auto finish = [&](size_t k) -> int {
-    const size_t lo = bound[k], m = bound[k + 1] - lo;
+    const size_t lo = bound[k];
     Batch* b = c->work[k & 1];
     xc_result* o = (full || !out) ? nullptr : out + written;
     const size_t cp = full ? 0 : (cap >= written ? cap - written : 0);
     size_t got = 0;
     int r = batch_collect(c, b, c->work_stream[k & 1], o, cp, &got, pair_counts ? pair_counts + lo : nullptr);
-    if (r == XC_ERR_CAPACITY && b->h_misc[1] != 0)   // device overflow pool too small: run it again alone
-      r = ctx_run_pairs(c, b, pairs + lo, m, o, cp, &got, pair_counts ? pair_counts + lo : nullptr);
+    if (r == XC_INTERNAL_OVERFLOW)   // device overflow pool too small: grow it, run the sub-batch again
+      r = batch_rerun_overflow(c, b, c->work_stream[k & 1], o, cp, &got, pair_counts ? pair_counts + lo : nullptr);
     need += got;
     h2d += c->last_h2d;
     d2h += c->last_d2h;
@@ -904,7 +908,9 @@ int xc_batch_results(xc_ctx* c, xc_batch* b, xc_result* out, size_t cap, size_t*
   if (!c || !b) return XC_ERR_ARG;
   cudaSetDevice(c->device);
   XC_CHECK(cudaDeviceSynchronize());
-  return batch_collect(c, b, c->stream, out, cap, n_out, pair_counts);
+  int r = batch_collect(c, b, c->stream, out, cap, n_out, pair_counts);
+  if (r == XC_INTERNAL_OVERFLOW) r = batch_rerun_overflow(c, b, c->stream, out, cap, n_out, pair_counts);
+  return r;
 }
 
 int xc_batch_free(xc_ctx* c, xc_batch* b) {

@@ -100,9 +100,17 @@ struct Ctx {
   uint64_t last_h2d = 0, last_d2h = 0;
   int sms = 152;               // multiprocessors of the device (sub-batch sizing)
   bool pair_kernel = false;    // both-strands correlation kernel usable (entropy table complement-symmetric)
+  unsigned char* noalloc_base = nullptr;   // xc_align_pair_noalloc's static array on this device (set at first use)
 };
 
 
+
+// batch_collect's status when the batch's device overflow pool filled during
+// the run (records were dropped on the device).  Internal only: every caller
+// grows the pool and runs the batch again (batch_rerun_overflow), so it never
+// reaches the C ABI, and it is never confused with XC_ERR_CAPACITY (the
+// caller's output buffer is too small).
+constexpr int XC_INTERNAL_OVERFLOW = -100;
 
 int pair_log2L(const xc_params& p, const xc_pair& q);
 Batch* new_batch(Ctx* c);
@@ -113,11 +121,14 @@ int batch_run(Ctx* c, Batch* b, cudaStream_t s, bool use_graph, bool timed = fal
 int batch_readback_async(Ctx* c, Batch* b, cudaStream_t s);
 int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, size_t* n_out,
                   size_t* pair_counts);
+// After batch_collect returned XC_INTERNAL_OVERFLOW: grows the overflow pool to
+// what the run asked for and runs the batch again on s (the pairs are still on
+// the device), then collects; XC_ERR_NOMEM if three runs still overflow.
+int batch_rerun_overflow(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, size_t* n_out,
+                         size_t* pair_counts);
 int batch_launch_count(const Ctx* c, const Batch* b);
 // z-score threshold of the scan kernel's FP32 probability screen.
 float screen_z(double min_prob, double target_total);
-int ctx_run_pairs(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, xc_result* out, size_t cap,
-                  size_t* n_out, size_t* pair_counts);
 int ctx_align_pipelined(Ctx* c, const xc_pair* pairs, size_t n, xc_result* out, size_t cap, size_t* n_out,
                         size_t* pair_counts);
 void server_stop(Ctx* c);

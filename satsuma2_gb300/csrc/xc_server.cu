@@ -11,12 +11,20 @@
 // (measured with cudaMemGetInfo when the server starts); xc_submit answers
 // XC_ERR_BUSY beyond it.  xc_wait is bounded: it returns XC_ERR_TIMEOUT and
 // keeps the ticket.  No device code waits on the host or on other kernels.
+//
+// What overlaps on the device: a slot's host packing and host-to-device copy
+// run while the previous slot's kernels run, and its read-back while the next
+// slot's kernels run; the kernels of successive slots themselves run one batch
+// after another (see the scheduler).  A batch whose result overflow pool fills
+// is grown and run again by the scheduler, so one request's yield never fails
+// the requests batched with it.
 #include "satsuma2_xcorr.h"
 #include "xc_runtime.h"
 
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -43,7 +51,10 @@ struct Request {
   Clock::time_point t_submit, t_done;
 };
 
+struct Server;
+
 struct Slot {
+  Server* S = nullptr;
   Batch* b = nullptr;
   cudaStream_t s = nullptr;
   cudaEvent_t ev = nullptr;
@@ -55,6 +66,7 @@ struct Slot {
 };
 
 constexpr int NSLOTS = 3;
+constexpr size_t LAT_RING = 1 << 16;   // latencies kept for the percentiles: the last 65536 requests
 
 struct Server {
   Ctx* ctx = nullptr;
@@ -70,7 +82,9 @@ struct Server {
   Slot slots[NSLOTS];
   uint64_t launch_seq = 0;
   cudaEvent_t last_kend = nullptr;   // kernels of the last launched batch done
-  std::vector<double> lat_ms;
+  std::vector<double> lat_ms;        // ring of the last LAT_RING request latencies
+  size_t lat_next = 0;
+  uint64_t slots_done = 0;           // bumped by the stream callback of each finished slot
   uint64_t completed = 0, pairs_done = 0;
   int device = 0;
   size_t max_batch = 4096;
@@ -87,6 +101,23 @@ static size_t pair_footprint(const Ctx* c, const xc_pair& p, int slots) {
          2 * acc_stride(lg > 0 ? lg : 13) * sizeof(float2);
 }
 
+// Stream callback queued behind each slot's read-back: wakes the scheduler
+// (no CUDA call here, as host functions on a stream require).
+static void CUDART_CB slot_finished(void* arg) {
+  Slot* sl = static_cast<Slot*>(arg);
+  {
+    std::lock_guard<std::mutex> lk(sl->S->mu);
+    sl->S->slots_done++;
+  }
+  sl->S->cv_work.notify_all();
+}
+
+static void record_latency(Server* S, double ms) {
+  if (S->lat_ms.size() < LAT_RING) S->lat_ms.push_back(ms);
+  else S->lat_ms[S->lat_next] = ms;
+  S->lat_next = (S->lat_next + 1) % LAT_RING;
+}
+
 static void complete_slot(Server* S, Slot& sl) {
   const size_t n = sl.items.size();
   std::vector<size_t> counts(n);
@@ -95,7 +126,10 @@ static void complete_slot(Server* S, Slot& sl) {
   // only when it was too small
   std::vector<xc_result> res(std::max<size_t>(S->res_per_pair * n + 1024, 4096));
   int r = batch_collect(S->ctx, sl.b, sl.s, res.data(), res.size(), &need, counts.data());
-  if (r == XC_ERR_CAPACITY && need > res.size() && sl.b->h_misc[1] == 0) {
+  // the batch's device overflow pool filled: grow it and run the batch again,
+  // so every request in it gets its full results
+  if (r == XC_INTERNAL_OVERFLOW) r = batch_rerun_overflow(S->ctx, sl.b, sl.s, res.data(), res.size(), &need, counts.data());
+  if (r == XC_ERR_CAPACITY && need > res.size()) {
     res.resize(need);
     r = batch_collect(S->ctx, sl.b, sl.s, res.data(), res.size(), &need, counts.data());
   }
@@ -119,7 +153,7 @@ static void complete_slot(Server* S, Slot& sl) {
     if (q->done == q->pairs.size() && !q->complete) {
       q->complete = true;
       q->t_done = now;
-      S->lat_ms.push_back(std::chrono::duration<double, std::milli>(now - q->t_submit).count());
+      record_latency(S, std::chrono::duration<double, std::milli>(now - q->t_submit).count());
       S->completed++;
       S->pairs_done += q->pairs.size();
       S->queued_bytes -= std::min(S->queued_bytes, q->footprint);
@@ -190,6 +224,7 @@ static void scheduler(Server* S) {
         if (r == XC_OK) S->last_kend = free_slot->kend;
         if (r == XC_OK) r = batch_readback_async(S->ctx, free_slot->b, free_slot->s);
         if (r == XC_OK && cudaEventRecord(free_slot->ev, free_slot->s) != cudaSuccess) r = XC_ERR_CUDA;
+        if (r == XC_OK && cudaLaunchHostFunc(free_slot->s, slot_finished, free_slot) != cudaSuccess) r = XC_ERR_CUDA;
         free_slot->busy = true;
         free_slot->seq = ++S->launch_seq;
         if (r != XC_OK) {
@@ -210,22 +245,22 @@ static void scheduler(Server* S) {
       }
     }
     if (launched) continue;
-    // 3. idle: wait for the oldest slot or new work
-    Slot* oldest = nullptr;
-    for (auto& sl : S->slots)
-      if (sl.busy && (!oldest || sl.seq < oldest->seq)) oldest = &sl;
-    if (oldest) {
+    // 3. idle: sleep until a slot's stream callback reports it finished, new
+    //    work arrives for a free slot, or a held batch's wait runs out
+    {
       std::unique_lock<std::mutex> lk(S->mu);
-      const bool have_work = !S->queue.empty() && free_slot != nullptr && !holding;
-      lk.unlock();
-      if (!have_work) {
-        // short polling keeps new arrivals flowing into free slots
-        if (cudaEventQuery(oldest->ev) != cudaSuccess) std::this_thread::sleep_for(std::chrono::microseconds(50));
+      if (S->stop && S->queue.empty() && busy == 0) return;
+      const uint64_t seen = S->slots_done;
+      auto limit = std::chrono::milliseconds(5);   // a bound only: every wake-up has a cause above
+      if (holding && !S->queue.empty()) {
+        const double left = S->max_wait_ms -
+            std::chrono::duration<double, std::milli>(Clock::now() - S->queue.front()->t_submit).count();
+        limit = std::min(limit, std::chrono::milliseconds((long)std::max(0.0, std::ceil(left))));
       }
-    } else {
-      std::unique_lock<std::mutex> lk(S->mu);
-      S->cv_work.wait_for(lk, std::chrono::milliseconds(5), [S] { return S->stop || !S->queue.empty(); });
-      if (S->stop && S->queue.empty()) return;
+      const bool can_take = free_slot != nullptr && !holding;
+      S->cv_work.wait_for(lk, limit, [&] {
+        return S->stop || S->slots_done != seen || (can_take && !S->queue.empty());
+      });
     }
   }
 }
@@ -246,6 +281,7 @@ static int server_start(Ctx* c) {
   S->max_pairs = 64 * S->max_batch;
   S->min_batch = std::min<size_t>(S->max_batch, 1024);
   for (auto& sl : S->slots) {
+    sl.S = S;
     sl.b = new_batch(c);
     if (cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess ||
@@ -385,18 +421,21 @@ int xc_serving_stats(xc_ctx* c, double* p50, double* p99, uint64_t* completed, u
     return XC_OK;
   }
   Server* S = c->server;
-  std::lock_guard<std::mutex> lk(S->mu);
-  std::vector<double> v = S->lat_ms;
-  std::sort(v.begin(), v.end());
+  std::vector<double> v;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    v = S->lat_ms;
+    if (completed) *completed = S->completed;
+    if (pairs_done) *pairs_done = S->pairs_done;
+  }
   auto pct = [&](double p) {
     if (v.empty()) return 0.0;
-    size_t i = (size_t)std::min<double>((double)v.size() - 1, std::floor(p * (double)(v.size() - 1) + 0.5));
+    const size_t i = (size_t)std::min<double>((double)v.size() - 1, std::floor(p * (double)(v.size() - 1) + 0.5));
+    std::nth_element(v.begin(), v.begin() + i, v.end());
     return v[i];
   };
   if (p50) *p50 = pct(0.50);
   if (p99) *p99 = pct(0.99);
-  if (completed) *completed = S->completed;
-  if (pairs_done) *pairs_done = S->pairs_done;
   return XC_OK;
 }
 
