@@ -125,6 +125,25 @@ int xc_batch_launches(xc_ctx* ctx, xc_batch* batch);
  * stage_ms[0] = correlation + FindTop kernels, [1] = scan kernels,
  * [2] = result ordering/packing kernels (all buckets of each stage). */
 int xc_batch_run_timed(xc_ctx* ctx, xc_batch* batch, void* stream, float* stage_ms);
+/* FindTop offsets the last run of a device batch kept: counts[2*i + s] for
+ * caller pair i and strand s (0 forward, 1 reverse-complemented query) if
+ * counts is not NULL, and the offsets (lag index j into the FFT-length
+ * correlation: query index - target index = j - L/2), packed in that order
+ * into offs.  *n_out gets the total; XC_ERR_CAPACITY when it exceeds cap.
+ * SeqAnalyzer::FindTop's output (CrossCorr.cc:878-944), for inspection. */
+int xc_batch_offsets(xc_ctx* ctx, xc_batch* batch, int* offs, size_t cap, size_t* n_out, int* counts);
+/* Near-threshold lags of the last run of a device batch: lags whose FP32
+ * correlation lies within XC_STRADDLE_REL (XC_STRADDLE_REL_L32768 at FFT
+ * 32768) times max(1, max|xc|) of FindTop's FP32 threshold, where the
+ * reference's FP32 FFT and this one can decide differently (the compare of
+ * CrossCorr.cc:932).  counts[2*i + s] gets their number for caller pair i,
+ * strand s; lags (if not NULL, XC_STRAD_CAP ints per pair strand) the first
+ * XC_STRAD_CAP of them in increasing order, -1 after the last.  Every lag
+ * outside this list is kept or dropped as an exact computation would. */
+#define XC_STRAD_CAP 16
+#define XC_STRADDLE_REL 2e-5
+#define XC_STRADDLE_REL_L32768 3e-4
+int xc_batch_straddles(xc_ctx* ctx, xc_batch* batch, int* counts, int* lags);
 /* Bytes the last xc_align_pairs call (or batch upload / readback) moved:
  * host-to-device and device-to-host. */
 int xc_transfer_stats(xc_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes);

@@ -33,7 +33,9 @@ assert RESULT_DTYPE.itemsize == 72
 EXPORTS = ("xc_create", "xc_destroy", "xc_align_pairs", "xc_batch_upload", "xc_batch_run",
            "xc_batch_results", "xc_batch_free", "xc_batch_launches", "xc_batch_run_timed",
            "xc_transfer_stats", "xc_submit", "xc_wait", "xc_serving_stats", "xc_debug_pair",
-           "xc_version", "xc_device_name", "xc_align_pair_noalloc")
+           "xc_version", "xc_device_name", "xc_align_pair_noalloc", "xc_batch_offsets",
+           "xc_batch_straddles")
+STRAD_CAP = 16   # XC_STRAD_CAP: near-threshold lags listed per pair strand
 
 
 class XCError(RuntimeError):
@@ -82,6 +84,8 @@ def load(path=LIB_PATH):
     lib.xc_batch_free.argtypes = [vp, vp]
     lib.xc_batch_launches.argtypes = [vp, vp]
     lib.xc_batch_run_timed.argtypes = [vp, vp, vp, vp]
+    lib.xc_batch_offsets.argtypes = [vp, vp, vp, sz, ctypes.POINTER(sz), vp]
+    lib.xc_batch_straddles.argtypes = [vp, vp, vp, vp]
     lib.xc_transfer_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
     lib.xc_submit.argtypes = [vp, vp, sz, ctypes.POINTER(ctypes.c_uint64)]
     lib.xc_wait.argtypes = [vp, ctypes.c_uint64, i, vp, sz, ctypes.POINTER(sz)]
@@ -277,6 +281,32 @@ class Batch:
             _check(r, "xc_batch_results")
             res = out[:n_out.value].copy()
             return (res, counts) if with_counts else res
+
+    def offsets(self):
+        """FindTop offsets of the last run: list over pairs of [forward, reverse] int32 arrays."""
+        counts = np.zeros(2 * self.n, np.int32)
+        n_out = ctypes.c_size_t()
+        _check(self.x.lib.xc_batch_offsets(self.x.ctx, self.h, None, 0, ctypes.byref(n_out), counts.ctypes.data),
+               "xc_batch_offsets")
+        offs = np.zeros(max(1, n_out.value), np.int32)
+        _check(self.x.lib.xc_batch_offsets(self.x.ctx, self.h, offs.ctypes.data, len(offs), ctypes.byref(n_out),
+                                           counts.ctypes.data), "xc_batch_offsets")
+        out, o = [], 0
+        for i in range(self.n):
+            a = offs[o:o + counts[2 * i]].copy()
+            o += counts[2 * i]
+            b = offs[o:o + counts[2 * i + 1]].copy()
+            o += counts[2 * i + 1]
+            out.append([a, b])
+        return out
+
+    def straddles(self):
+        """Near-threshold lags of the last run: (counts [n, 2], lags [n, 2, STRAD_CAP], -1 padded)."""
+        counts = np.zeros(2 * self.n, np.int32)
+        lags = np.zeros(2 * self.n * STRAD_CAP, np.int32)
+        _check(self.x.lib.xc_batch_straddles(self.x.ctx, self.h, counts.ctypes.data, lags.ctypes.data),
+               "xc_batch_straddles")
+        return counts.reshape(self.n, 2), lags.reshape(self.n, 2, STRAD_CAP)
 
     def free(self):
         if self.h:

@@ -81,7 +81,13 @@ __device__ __forceinline__ void hermitian_pack(float2* __restrict__ buf, const S
 // over 256-sample blocks when L/256 > 8; keep i with xc[i] > env*cutoff + 1
 // in increasing i.  Threads t < NT_CORR; warp w of them owns the contiguous
 // range [w*L/16, (w+1)*L/16), lanes stride by one.  Every thread of the CTA
-// calls it (two CTA barriers).
+// calls it (two CTA barriers).  s_warp holds 2 * NT_CORR/32 ints.
+//
+// Near-threshold lags: with P.strad_cnt set, every lag whose FP32 value lies
+// within straddle_rel(L) * max(1, max|xc|) of its FP32 threshold is counted
+// in strad_cnt[pair*2+strand] and the first STRAD_CAP of them are listed.
+// There the reference's FP32 FFT and this one may decide differently; every
+// other lag's decision is the same for both.
 template <int LOG2L, class SY = CtaBarrier>
 __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, uint32_t off_base, int pidx,
                                          int strand, const float2* __restrict__ buf, int t, int* s_warp,
@@ -145,6 +151,7 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
     thrb[0] = 1.0f;
   }
   int wcount = 0;
+  float amax = 0.f;   // max |xc| of the lane's lags (for the near-threshold band)
   unsigned msk[KEEP ? ITER : 1];
 #pragma unroll(KEEP ? ITER : 4)
   for (int e = 0; e < ITER; e++) {
@@ -153,7 +160,13 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
     const unsigned m = __ballot_sync(0xffffffffu, x > thrb[(L / 256 > 8) ? (e >> 3) : 0]);
     if constexpr (KEEP) msk[e] = m;
     wcount += __popc(m);
+    amax = fmaxf(amax, fabsf(x));
     if (P.dbg_xc) P.dbg_xc[(size_t)(pidx * 2 + strand) * L + i] = x;
+  }
+  int* s_max = s_warp + NT_CORR / 32;   // max |xc| bits per warp (non-negative floats order as ints)
+  if (P.strad_cnt) {
+    const unsigned mb = __reduce_max_sync(0xffffffffu, __float_as_uint(amax));
+    if (lane == 0) s_max[warp] = (int)mb;
   }
   if (lane == 0) s_warp[warp] = wcount;
   sync();
@@ -170,16 +183,34 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
   }
   sync();
   int run = s_warp[warp];
+  float band = -1.f;   // no near-threshold lags without a list
+  if (P.strad_cnt) {
+    unsigned mb = 0u;
+#pragma unroll
+    for (int k = 0; k < NT_CORR / 32; k++) mb = max(mb, (unsigned)s_max[k]);
+    band = straddle_rel(LOG2L) * fmaxf(1.0f, __uint_as_float(mb));
+  }
   int* out = P.off_list + off_base + (size_t)strand * L;
   const unsigned lt = (1u << lane) - 1u;
 #pragma unroll(KEEP ? ITER : 4)
   for (int e = 0; e < ITER; e++) {
     const int i = wbase + e * 32 + lane;
+    const float thr = thrb[(L / 256 > 8) ? (e >> 3) : 0];
     unsigned m;
     if constexpr (KEEP) m = msk[e];
-    else m = __ballot_sync(0xffffffffu, xat(e) > thrb[(L / 256 > 8) ? (e >> 3) : 0]);
+    else m = __ballot_sync(0xffffffffu, xat(e) > thr);
     if ((m >> lane) & 1u) out[run + __popc(m & lt)] = i;
     run += __popc(m);
+    if (P.strad_cnt) {
+      const unsigned nm = __ballot_sync(0xffffffffu, fabsf(xat(e) - thr) <= band);
+      if (nm) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&P.strad_cnt[pidx * 2 + strand], __popc(nm));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int k = base + __popc(nm & lt);
+        if (((nm >> lane) & 1u) && k < STRAD_CAP) P.strad_list[(size_t)(pidx * 2 + strand) * STRAD_CAP + k] = i;
+      }
+    }
   }
 }
 
@@ -214,7 +245,7 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
   __shared__ double s_off[8];
   __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
   __shared__ Split3 s_wf[2][8];    // the same as three floats each
-  __shared__ int s_warp[NT_CORR / 32];
+  __shared__ int s_warp[2 * NT_CORR / 32];
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -614,7 +645,7 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
   __shared__ int s_cnt4[8];
   __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
   __shared__ Split3 s_wf[2][8];    // the same as three floats each
-  __shared__ int s_warp[2][NT_CORR / 32];
+  __shared__ int s_warp[2][2 * NT_CORR / 32];
 
   const int tid = threadIdx.x;
   const int half = tid >> 9;       // steps 3b-5: 0 target / forward strand, 1 query / reverse strand

@@ -18,6 +18,17 @@ constexpr int SCAN_CTAS_PER_SM = 8;   // scan register budget: 64 per thread (8 
 constexpr int WINDOW = 46;       // DoOne window: m_minLen + 1 positions (CrossCorr.cc:701-705)
 constexpr int MIN_HITS = 19;     // ACGT windows pass when 100*hits > 1889 (CrossCorr.cc:675)
 
+// Near-threshold band of FindTop: lags whose FP32 correlation lies within
+// straddle_rel(L) * max(1, max|xc|) of the FP32 threshold.  The reference's
+// FP32 FFT (FFTReal) and this one each differ from the exact correlation by
+// ~2e-7 of the peak (measured), so only there can their keep/drop decisions
+// part; the band is about 60x that.  At L = 32768 FFTReal rotates its
+// twiddles with a float oscillator beyond its 12th pass and its own error
+// grows to ~1.5e-4 of the peak, hence the wider band.  The parity tests use
+// the same band around the FP64 threshold.
+constexpr int STRAD_CAP = 16;    // near-threshold lags listed per pair strand (all are counted)
+__host__ __device__ constexpr float straddle_rel(int log2L) { return log2L > 14 ? 3e-4f : 2e-5f; }
+
 // Pair flags written by the correlation kernel, read by the scan kernel.
 enum : uint32_t {
   PF_FAST = 1u,        // use cutoff_fast
@@ -79,6 +90,8 @@ struct CorrParams {
   float2* acc;              // L > 2^MAX_SMEM_LOG2L: channel sums, [pair*2+strand][acc_stride(log2L)]
   int* fb_list;             // log2L == PAIR_LOG2L: both-strands kernel first; the pairs it
   int* fb_cnt;              //   hands back ([*fb_cnt], zeroed before) go to corr_kernel
+  int* strad_cnt;           // optional: near-threshold lags per [pair*2 + strand] (zeroed before)
+  int* strad_list;          //   and the first STRAD_CAP of them, [pair*2 + strand][STRAD_CAP]
 };
 
 // Global channel-sum scratch of one pair strand for FFT lengths beyond one

@@ -349,6 +349,7 @@ Batch::~Batch() {
   cudaFree(d_pool); cudaFree(d_desc); cudaFree(d_off); cudaFree(d_offcnt); cudaFree(d_flags);
   cudaFree(d_res); cudaFree(d_rescnt); cudaFree(d_ovf); cudaFree(d_misc); cudaFree(d_base);
   cudaFree(d_dense); cudaFree(d_dbg); cudaFree(d_dbg_sig); cudaFree(d_dbg_xc); cudaFree(d_acc); cudaFree(d_fb);
+  cudaFree(d_stradcnt); cudaFree(d_strad);
   cudaFreeHost(h_pool); cudaFreeHost(h_desc); cudaFreeHost(h_base); cudaFreeHost(h_dense);
   cudaFreeHost(h_misc); cudaFreeHost(h_ovf); cudaFreeHost(h_flags);
 }
@@ -420,6 +421,8 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   if ((r = dev_grow(b->d_ovf, b->cap_ovf, (size_t)b->ovf_cap)) != XC_OK) return r;
   if ((r = dev_grow(b->d_misc, b->cap_misc, 4)) != XC_OK) return r;
   if ((r = dev_grow(b->d_fb, b->cap_fb, n)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_stradcnt, b->cap_stradcnt, nslots)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_strad, b->cap_strad, nslots * STRAD_CAP)) != XC_OK) return r;
   if ((r = dev_grow(b->d_base, b->cap_base, nslots + 1)) != XC_OK) return r;
   if ((r = dev_grow(b->d_dense, b->cap_dense, nslots * slots)) != XC_OK) return r;
   size_t acc = 0;
@@ -475,6 +478,7 @@ float screen_z(double min_prob, double target_total) {
 static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
   const int nslots = 2 * b->n;
   XC_CHECK(cudaMemsetAsync(b->d_misc, 0, 4 * sizeof(int), s));
+  XC_CHECK(cudaMemsetAsync(b->d_stradcnt, 0, nslots * sizeof(int), s));
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[0], s, cudaEventRecordExternal));
   for (const Bucket& bk : b->buckets) {
     const DevTables& t = c->tab[bk.log2L];
@@ -501,6 +505,8 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
       cp.fb_list = b->d_fb;
       cp.fb_cnt = b->d_misc + 3;   // zeroed above
     }
+    cp.strad_cnt = b->d_stradcnt;
+    cp.strad_list = b->d_strad;
     XC_CHECK(launch_corr(bk.log2L, cp, bk.count, s));
   }
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[1], s, cudaEventRecordExternal));
@@ -911,6 +917,65 @@ int xc_batch_results(xc_ctx* c, xc_batch* b, xc_result* out, size_t cap, size_t*
   int r = batch_collect(c, b, c->stream, out, cap, n_out, pair_counts);
   if (r == XC_INTERNAL_OVERFLOW) r = batch_rerun_overflow(c, b, c->stream, out, cap, n_out, pair_counts);
   return r;
+}
+
+int xc_batch_offsets(xc_ctx* c, xc_batch* b, int* offs, size_t cap, size_t* n_out, int* counts) {
+  if (!c || !b) return XC_ERR_ARG;
+  cudaSetDevice(c->device);
+  XC_CHECK(cudaDeviceSynchronize());
+  const int n = b->n;
+  std::vector<int> cnt(2 * (size_t)n);
+  XC_CHECK(cudaMemcpy(cnt.data(), b->d_offcnt, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<int> dev_of(n);
+  for (int d = 0; d < n; d++) dev_of[b->order[d]] = d;
+  size_t need = 0;
+  for (int i = 0; i < n; i++)
+    for (int s2 = 0; s2 < 2; s2++) {
+      const int k = cnt[2 * dev_of[i] + s2];
+      if (counts) counts[2 * i + s2] = k;
+      need += (size_t)k;
+    }
+  if (n_out) *n_out = need;
+  if (!offs) return XC_OK;
+  if (need > cap) return XC_ERR_CAPACITY;
+  size_t o = 0;
+  for (int i = 0; i < n; i++) {
+    const int d = dev_of[i];
+    const PairDesc& D = b->desc_host[d];
+    for (int s2 = 0; s2 < 2; s2++) {
+      const int k = cnt[2 * d + s2];
+      if (k) XC_CHECK(cudaMemcpy(offs + o, b->d_off + D.off_base + ((size_t)s2 << D.log2L), k * sizeof(int),
+                                 cudaMemcpyDeviceToHost));
+      o += (size_t)k;
+    }
+  }
+  return XC_OK;
+}
+
+int xc_batch_straddles(xc_ctx* c, xc_batch* b, int* counts, int* lags) {
+  if (!c || !b) return XC_ERR_ARG;
+  cudaSetDevice(c->device);
+  XC_CHECK(cudaDeviceSynchronize());
+  const int n = b->n;
+  std::vector<int> cnt(2 * (size_t)n), lst(2 * (size_t)n * STRAD_CAP);
+  XC_CHECK(cudaMemcpy(cnt.data(), b->d_stradcnt, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  if (lags) XC_CHECK(cudaMemcpy(lst.data(), b->d_strad, lst.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  for (int d = 0; d < n; d++) {
+    const int i = b->order[d];
+    for (int s2 = 0; s2 < 2; s2++) {
+      const int k = cnt[2 * d + s2];
+      if (counts) counts[2 * i + s2] = k;
+      if (lags) {
+        int* dst = lags + (size_t)(2 * i + s2) * STRAD_CAP;
+        const int* src = lst.data() + (size_t)(2 * d + s2) * STRAD_CAP;
+        const int m = std::min(k, STRAD_CAP);
+        std::copy(src, src + m, dst);
+        std::sort(dst, dst + m);
+        std::fill(dst + m, dst + STRAD_CAP, -1);
+      }
+    }
+  }
+  return XC_OK;
 }
 
 int xc_batch_free(xc_ctx* c, xc_batch* b) {

@@ -43,6 +43,8 @@ struct Batch {
   int* d_misc = nullptr;          size_t cap_misc = 0;   // [0] ovf count [1] err [2] dbg count
                                                          // [3] pairs corr_pair_kernel handed back
   int* d_fb = nullptr;            size_t cap_fb = 0;     // those pairs' indices
+  int* d_stradcnt = nullptr;      size_t cap_stradcnt = 0;   // near-threshold lags per pair strand
+  int* d_strad = nullptr;         size_t cap_strad = 0;      // the first STRAD_CAP of them
   int* d_base = nullptr;          size_t cap_base = 0;
   DevResult* d_dense = nullptr;   size_t cap_dense = 0;
   float2* d_acc = nullptr;        size_t cap_acc = 0;     // channel sums of FFT lengths beyond one SM

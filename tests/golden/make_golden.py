@@ -15,8 +15,14 @@ reference itself (run in a container that has the reference tree).
   slave binary (oracle/_ref/HomologyByXCorrSlave) over a small genome pair,
   driven through its TCP protocol (analysis/WorkQueue.cc:93-166 master side)
   by a fake master in this script.
+* ``slave_e2e_probtable.npz`` -- the same genome pair with the slave's
+  ``-prob_table -min_prob 0.9999`` (ProbTable lookups instead of erf/exp,
+  HomologyByXCorrSlave.cc:186-199, 413-421) over the first two blocks of
+  ``slave_e2e.npz`` (``n_blocks``): the records only; the sequences and blocks
+  are those of ``slave_e2e.npz``.
 
-Usage: python tests/golden/make_golden.py   (needs oracle/build_ref.sh first)
+Usage: python tests/golden/make_golden.py [cases|slave|probtable ...]
+(all three by default; builds oracle/_ref first)
 """
 import hashlib
 import json
@@ -192,7 +198,7 @@ def recv_exact(conn, n):
     return buf
 
 
-def slave_e2e():
+def slave_e2e(prob_table=False):
     rng = np.random.default_rng(SEED + 1)
     tg = [W.random_bases(rng, 20000), W.random_bases(rng, 9000)]
     qg = [W.mutate(rng, tg[0][2000:15000], 0.85),
@@ -218,6 +224,10 @@ def slave_e2e():
     for qf in range(0, n_q_real, 3):
         for tf in range(0, n_t_real, 4):
             blocks.append((tf, min(tf + 3, n_t_real - 1), qf, min(qf + 2, n_q_real - 1), False))
+    # -prob_table keeps thousands of records per pair here: the first two
+    # blocks (homologous chunks) keep that fixture small
+    n_blocks = 2 if prob_table else len(blocks)
+    blocks = blocks[:n_blocks]
     blocks.append((sent_t, sent_t, sent_q, sent_q, False))
     tmp = tempfile.mkdtemp(prefix="satsuma_e2e_")
     write_fasta(os.path.join(tmp, "t.fa"), targets)
@@ -227,8 +237,9 @@ def slave_e2e():
     srv.bind(("127.0.0.1", 0))
     srv.listen(16)
     port = srv.getsockname()[1]
+    extra = ["-prob_table", "-min_prob", "0.9999"] if prob_table else []
     proc = subprocess.Popen([oracle.REF_SLAVE, "-master", "127.0.0.1", "-port", str(port),
-                             "-sid", "1", "-p", "1", "-q", "q.fa", "-t", "t.fa"], cwd=tmp,
+                             "-sid", "1", "-p", "1", "-q", "q.fa", "-t", "t.fa"] + extra, cwd=tmp,
                             stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     results = []
     pending = list(blocks)
@@ -263,6 +274,13 @@ def slave_e2e():
     allres = np.concatenate(results) if results else np.zeros(0, oracle.RESULT_DTYPE)
     allres = allres[allres["target_id"] < len(tg)]
     target_total = float(sum(len(s) for _, s in targets))
+    if prob_table:
+        print("slave e2e, -prob_table: %d blocks, %d results" % (len(blocks), len(allres)))
+        return {"results": allres,
+                "meta": np.array(json.dumps(dict(target_total=target_total, t_chunk=4096, q_chunk=4096,
+                                                 cutoff=1.8, min_prob_effective=0.99, prob_table=1,
+                                                 prob_table_cutoff=0.9999, n_blocks=n_blocks,
+                                                 n_real_targets=len(tg), n_real_queries=len(qg))))}
     out = {
         "tg0": tg[0], "tg1": tg[1], "qg0": qg[0], "qg1": qg[1], "qg2": qg[2],
         "sentinel": sentinel,
@@ -278,11 +296,17 @@ def slave_e2e():
 
 
 def main():
+    what = set(sys.argv[1:]) or {"cases", "slave", "probtable"}
+    oracle.install_ref()
     oracle.build_ref()
     R = oracle.Reference()
     O = oracle.Oracle()
-    np.savez_compressed(os.path.join(HERE, "cases.npz"), **run_cases(R, O))
-    np.savez_compressed(os.path.join(HERE, "slave_e2e.npz"), **slave_e2e())
+    if "cases" in what:
+        np.savez_compressed(os.path.join(HERE, "cases.npz"), **run_cases(R, O))
+    if "slave" in what:
+        np.savez_compressed(os.path.join(HERE, "slave_e2e.npz"), **slave_e2e())
+    if "probtable" in what:
+        np.savez_compressed(os.path.join(HERE, "slave_e2e_probtable.npz"), **slave_e2e(prob_table=True))
 
 
 if __name__ == "__main__":

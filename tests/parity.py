@@ -47,6 +47,35 @@ def load_slave_e2e():
     return d
 
 
+def load_slave_e2e_probtable():
+    """The reference slave's records with -prob_table over the first
+    meta["n_blocks"] blocks of slave_e2e.npz (sequences and blocks from there)."""
+    d = load_slave_e2e()
+    z = np.load(os.path.join(GOLDEN, "slave_e2e_probtable.npz"), allow_pickle=False)
+    meta = json.loads(str(z["meta"]))
+    d["results"] = z["results"]
+    d["meta"] = meta
+    d["blocks"] = np.concatenate([d["blocks"][:meta["n_blocks"]], d["blocks"][-1:]])
+    return d
+
+
+def slave_items(d):
+    """The chunk pairs of the golden run's real blocks, block by block
+    (query-major, target-minor, as align_target loops)."""
+    tseqs = [d["tg0"].tobytes(), d["tg1"].tobytes(), d["sentinel"].tobytes()]
+    qseqs = [d["qg0"].tobytes(), d["qg1"].tobytes(), d["qg2"].tobytes(), d["sentinel"].tobytes()]
+    items = []
+    for (tf, tt, qf, qt) in d["blocks"][:-1]:
+        for qi in range(qf, qt + 1):
+            for ti in range(tf, tt + 1):
+                ts, tst, ten = d["tchunks"][ti]
+                qs, qst, qen = d["qchunks"][qi]
+                items.append(dict(t=tseqs[ts][tst:ten], q=qseqs[qs][qst:qen], t_chunk_start=int(tst),
+                                  target_id=int(ts), q_chunk_start=int(qst), query_id=int(qs),
+                                  query_size=len(qseqs[qs])))
+    return items
+
+
 def result_offsets(res, case):
     """(strand, FindTop index) of each t_result record of one chunk pair."""
     L = case["L"]

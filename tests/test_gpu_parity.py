@@ -198,31 +198,23 @@ def test_device_batch_replay_is_stable():
     x.close()
 
 
-def test_slave_end_to_end(O):
+def _slave_stream_check(O, d, prob_table):
     """The CUDA path reproduces the unmodified reference slave's output stream.
 
     The oracle reproduces that stream exactly on the CPU (test_oracle), so it
     splits the stream per chunk pair; records from offsets where the GPU's
     FP32 FindTop and the FP64 oracle disagree inside the straddle band are set
-    aside on both sides."""
+    aside on both sides.  Returns the number of (strand, offset) set aside."""
     import satsuma2_gb300 as sg
-    d = parity.load_slave_e2e()
     m = d["meta"]
-    tseqs = [d["tg0"].tobytes(), d["tg1"].tobytes(), d["sentinel"].tobytes()]
-    qseqs = [d["qg0"].tobytes(), d["qg1"].tobytes(), d["qg2"].tobytes(), d["sentinel"].tobytes()]
+    pt = O.probtable(m["target_total"], m["prob_table_cutoff"]) if prob_table else None
     x = sg.XCorr(cutoff=m["cutoff"], min_prob=m["min_prob_effective"], target_total=m["target_total"],
-                 t_chunk=m["t_chunk"], q_chunk=m["q_chunk"])
+                 t_chunk=m["t_chunk"], q_chunk=m["q_chunk"], prob_table=prob_table,
+                 prob_table_cutoff=m.get("prob_table_cutoff", 0.9999))
     P = O.params(cutoff=m["cutoff"], min_prob=m["min_prob_effective"], target_total=m["target_total"],
-                 t_chunk=m["t_chunk"], q_chunk=m["q_chunk"])
-    items = []
-    for (tf, tt, qf, qt) in d["blocks"][:-1]:
-        for qi in range(qf, qt + 1):
-            for ti in range(tf, tt + 1):
-                ts, tst, ten = d["tchunks"][ti]
-                qs, qst, qen = d["qchunks"][qi]
-                items.append(dict(t=tseqs[ts][tst:ten], q=qseqs[qs][qst:qen], t_chunk_start=int(tst),
-                                  target_id=int(ts), q_chunk_start=int(qst), query_id=int(qs),
-                                  query_size=len(qseqs[qs])))
+                 t_chunk=m["t_chunk"], q_chunk=m["q_chunk"], probtable=pt,
+                 probtable_cutoff=m.get("prob_table_cutoff", 0.0))
+    items = parity.slave_items(d)
     got, counts = x.align(items, with_counts=True)
     slave = d["results"]
     og = os_ = 0
@@ -251,6 +243,82 @@ def test_slave_end_to_end(O):
             k, a[["qstart", "tstart", "len", "reverse", "prob", "ident"]],
             b[["qstart", "tstart", "len", "reverse", "prob", "ident"]])
     assert og == len(got) and os_ == len(slave)
+    x.close()
+    return n_dropped, len(items)
+
+
+def test_slave_end_to_end(O):
+    n_dropped, n_pairs = _slave_stream_check(O, parity.load_slave_e2e(), prob_table=False)
+    assert n_dropped <= max(2, n_pairs // 10)   # straddling offsets are rare
+
+
+def test_slave_end_to_end_probtable(O):
+    """-prob_table: thousands of records per pair (a small targetTotal makes
+    most DoOne segments pass the table), far past the result slots."""
+    n_dropped, n_pairs = _slave_stream_check(O, parity.load_slave_e2e_probtable(), prob_table=True)
+    assert n_dropped <= max(2, n_pairs // 10)
+
+
+def _block_items(tchunks, qchunks, tf, qf, n=24):
+    """One n x n grid block of chunk pairs, query-major as align_target loops."""
+    return [dict(t=tchunks[ti], q=qchunks[qi], t_chunk_start=3072 * ti, target_id=0,
+                 q_chunk_start=4096 * qi, query_id=0, query_size=4096 * len(qchunks))
+            for qi in range(qf, qf + n) for ti in range(tf, tf + n)]
+
+
+def test_serving_probtable_blocks_overflow_vs_oracle(O):
+    """Serving in -prob_table mode: three 576-pair grid blocks plus a batch of
+    tandem-repeat pairs, submitted together.  At hundreds of records per pair
+    the slot batches overflow their device result pool; the scheduler grows
+    it and runs the batch again.  Every request's records equal
+    xc_align_pairs', and the oracle's over the GPU's own offsets."""
+    import satsuma2_gb300 as sg
+    from concurrent.futures import ThreadPoolExecutor
+    rng = np.random.default_rng(61)
+    genome = W.random_bases(rng, 3072 * 40 + 1024)
+    tchunks = [genome[3072 * i:3072 * i + 4096].tobytes() for i in range(40)]
+    qg = W.mutate(rng, genome[:4096 * 30], 0.85)
+    qchunks = [qg[4096 * i:4096 * i + 4096].tobytes() for i in range(len(qg) // 4096)]
+    blocks = [_block_items(tchunks, qchunks, 0, 0), _block_items(tchunks, qchunks, 8, 2),
+              _block_items(tchunks, qchunks, 16, 4)]
+    reps = []
+    for k in range(64):
+        t = W.random_bases(rng, 4096)
+        rep = W.tandem_repeat(rng, int(rng.integers(200, 1200)), 1, 6)
+        p = int(rng.integers(0, 4096 - len(rep)))
+        t[p:p + len(rep)] = rep
+        q = W.random_bases(rng, 4096)
+        p2 = int(rng.integers(0, 4096 - len(rep)))
+        q[p2:p2 + len(rep)] = W.mutate(rng, rep, 0.97, indel_every=0)
+        reps.append((t.tobytes(), q.tobytes()))
+    reqs = blocks + [reps]
+    TT = 4096.0 * 64
+    x = sg.XCorr(target_total=TT, prob_table=True, prob_table_cutoff=0.9999, max_batch=4096)
+    tickets = [x.submit(r) for r in reqs]
+    served = [x.wait(tk, timeout_ms=300000) for tk in tickets]
+    pt = O.probtable(TT, 0.9999)
+    P = O.params(target_total=TT, probtable=pt, probtable_cutoff=0.9999)
+    total = 0
+    for r, got in zip(reqs, served):
+        want, counts = x.align(r, with_counts=True)
+        assert parity.same_results(got, want, target_total=TT)
+        total += len(got)
+        offs = [x.debug_pair(signals=False, **(it if isinstance(it, dict) else dict(t=it[0], q=it[1])))["offsets"]
+                for it in r]
+
+        def one(k):
+            it = r[k] if isinstance(r[k], dict) else dict(t=r[k][0], q=r[k][1])
+            pr = O.pair(it["t"], it["q"], t_chunk_start=it.get("t_chunk_start", 0),
+                        q_chunk_start=it.get("q_chunk_start", 0), query_size=it.get("query_size"))
+            return O.align_pair(P, pr, offsets_in=offs[k])[0]
+        with ThreadPoolExecutor(16) as ex:
+            oracle_recs = list(ex.map(one, range(len(r))))
+        o = 0
+        for k in range(len(r)):
+            mine = want[o:o + int(counts[k])]
+            o += int(counts[k])
+            assert parity.same_results(mine, oracle_recs[k], target_total=TT), k
+    assert total > 3 * 65536   # well past one batch's initial overflow pool
     x.close()
 
 

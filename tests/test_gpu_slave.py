@@ -48,7 +48,7 @@ def recv_exact(conn, n):
     return buf
 
 
-def run_slave(d, threads, expected):
+def run_slave(d, threads, expected, extra=()):
     """Serves every golden block to the slave; returns its records (sentinel
     records removed) in arrival order."""
     tg = [d["tg0"], d["tg1"], d["sentinel"]]
@@ -63,7 +63,7 @@ def run_slave(d, threads, expected):
     srv.settimeout(60)
     port = srv.getsockname()[1]
     proc = subprocess.Popen([SLAVE, "-master", "127.0.0.1", "-port", str(port), "-sid", "7", "-p", str(threads),
-                             "-q", "q.fa", "-t", "t.fa"], cwd=tmp, stdout=subprocess.PIPE,
+                             "-q", "q.fa", "-t", "t.fa"] + list(extra), cwd=tmp, stdout=subprocess.PIPE,
                             stderr=subprocess.STDOUT)
     n_real_t = d["meta"]["n_real_targets"]
     pending = [tuple(int(v) for v in b) for b in d["blocks"]]
@@ -101,23 +101,13 @@ def run_slave(d, threads, expected):
     return np.concatenate(got) if got else np.zeros(0, sg.RESULT_DTYPE)
 
 
-def expected_stream(d):
+def expected_stream(d, prob_table=False):
     """xc_align_pairs over every chunk pair of the blocks, block by block."""
     m = d["meta"]
-    tseqs = [d["tg0"].tobytes(), d["tg1"].tobytes(), d["sentinel"].tobytes()]
-    qseqs = [d["qg0"].tobytes(), d["qg1"].tobytes(), d["qg2"].tobytes(), d["sentinel"].tobytes()]
-    items = []
-    for (tf, tt, qf, qt) in d["blocks"][:-1]:
-        for qi in range(qf, qt + 1):
-            for ti in range(tf, tt + 1):
-                ts, tst, ten = d["tchunks"][ti]
-                qs, qst, qen = d["qchunks"][qi]
-                items.append(dict(t=tseqs[ts][tst:ten], q=qseqs[qs][qst:qen], t_chunk_start=int(tst),
-                                  target_id=int(ts), q_chunk_start=int(qst), query_id=int(qs),
-                                  query_size=len(qseqs[qs])))
     x = sg.XCorr(cutoff=m["cutoff"], min_prob=m["min_prob_effective"], target_total=m["target_total"],
-                 t_chunk=m["t_chunk"], q_chunk=m["q_chunk"])
-    want = x.align(items)
+                 t_chunk=m["t_chunk"], q_chunk=m["q_chunk"], prob_table=prob_table,
+                 prob_table_cutoff=m.get("prob_table_cutoff", 0.9999))
+    want = x.align(parity.slave_items(d))
     x.close()
     return want, m["target_total"]
 
@@ -145,4 +135,17 @@ def test_slave_stream_one_worker(golden):
 def test_slave_three_workers(golden):
     d, want, tt = golden
     got = run_slave(d, 3, len(want))
+    assert parity.same_results(got[sort_key(got)], want[sort_key(want)], target_total=tt)
+
+
+def test_slave_stream_probtable():
+    """-prob_table -min_prob 0.9999: the table replaces erf/exp and thousands
+    of records per pair come back (tests/golden/slave_e2e_probtable.npz holds
+    the reference slave's records for the same blocks; test_gpu_parity holds
+    xc_align_pairs to them)."""
+    build.build()
+    d = parity.load_slave_e2e_probtable()
+    want, tt = expected_stream(d, prob_table=True)
+    assert len(want) > 50000
+    got = run_slave(d, 2, len(want), extra=("-prob_table", "-min_prob", "0.9999"))
     assert parity.same_results(got[sort_key(got)], want[sort_key(want)], target_total=tt)

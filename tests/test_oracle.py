@@ -116,6 +116,25 @@ def test_slave_end_to_end(O):
     assert parity.same_results(got, d["results"], prob_rtol=1e-12)
 
 
+def test_slave_end_to_end_probtable(O):
+    """The oracle reproduces the reference slave's -prob_table stream."""
+    d = parity.load_slave_e2e_probtable()
+    m = d["meta"]
+    pt = O.probtable(m["target_total"], m["prob_table_cutoff"])
+    P = O.params(cutoff=m["cutoff"], min_prob=m["min_prob_effective"], target_total=m["target_total"],
+                 t_chunk=m["t_chunk"], q_chunk=m["q_chunk"], probtable=pt,
+                 probtable_cutoff=m["prob_table_cutoff"])
+    out = []
+    for it in parity.slave_items(d):
+        pr = O.pair(it["t"], it["q"], t_chunk_start=it["t_chunk_start"], target_id=it["target_id"],
+                    q_chunk_start=it["q_chunk_start"], query_id=it["query_id"], query_size=it["query_size"])
+        res, _ = O.align_pair(P, pr)
+        out.append(res)
+    got = np.concatenate(out)
+    assert len(got) > 50000
+    assert parity.same_results(got, d["results"], prob_rtol=0.0)
+
+
 def test_workloads_deterministic():
     a = W.uniform_batch(4, seed=3)
     b = W.uniform_batch(4, seed=3)
