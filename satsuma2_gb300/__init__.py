@@ -62,6 +62,13 @@ class Pair(ctypes.Structure):
                 ("query_size", ctypes.c_ulong), ("fast", ctypes.c_int)]
 
 
+# xc_pair as a numpy record (LP64 layout of the ctypes Pair above, 64 bytes):
+# arrays of chunk pairs that point into caller-owned sequence buffers.
+PAIR_DTYPE = np.dtype({"names": ["tseq", "tlen", "t_chunk_start", "target_id", "qseq", "qlen", "q_chunk_start",
+                                 "query_id", "query_size", "fast"],
+                       "formats": ["<u8", "<i4", "<i4", "<u8", "<u8", "<i4", "<i4", "<u8", "<u8", "<i4"],
+                       "offsets": [0, 8, 12, 16, 24, 32, 36, 40, 48, 56], "itemsize": 64})
+
 _lib = None
 
 
@@ -122,6 +129,32 @@ def make_pairs(items):
     return arr, keep
 
 
+def block_pairs(tbuf, tchunks, qbuf, qchunks, tf, tt, qf, qt, target_id=0, query_id=0, fast=0):
+    """The chunk pairs of one t_pair block (inclusive chunk ranges), query-major
+    as HomologyByXCorr::align_target loops (HomologyByXCorrSlave.cc:281-299),
+    as a PAIR_DTYPE array pointing into tbuf / qbuf (numpy uint8 arrays the
+    caller keeps alive).  tchunks / qchunks: int arrays of (start, end) per
+    chunk of one target and one query sequence."""
+    tchunks = np.asarray(tchunks, np.int64)
+    qchunks = np.asarray(qchunks, np.int64)
+    ti = np.arange(tf, tt + 1)
+    qi = np.arange(qf, qt + 1)
+    T, Qg = np.meshgrid(ti, qi)          # query outer, target inner
+    T, Qg = T.ravel(), Qg.ravel()
+    out = np.zeros(len(T), PAIR_DTYPE)
+    out["tseq"] = tbuf.ctypes.data + tchunks[T, 0]
+    out["tlen"] = tchunks[T, 1] - tchunks[T, 0]
+    out["t_chunk_start"] = tchunks[T, 0]
+    out["target_id"] = target_id
+    out["qseq"] = qbuf.ctypes.data + qchunks[Qg, 0]
+    out["qlen"] = qchunks[Qg, 1] - qchunks[Qg, 0]
+    out["q_chunk_start"] = qchunks[Qg, 0]
+    out["query_id"] = query_id
+    out["query_size"] = len(qbuf)
+    out["fast"] = fast
+    return out
+
+
 class XCorr:
     """One GPU context of the chunk-pair cross-correlation path.
 
@@ -160,9 +193,13 @@ class XCorr:
         return buf.value.decode()
 
     def align(self, items, with_counts=False):
-        """Runs chunk pairs (both strands) -> structured array of t_result records."""
-        arr, keep = make_pairs(items)
-        n = len(arr)
+        """Runs chunk pairs (both strands) -> structured array of t_result
+        records.  items as for make_pairs, or a PAIR_DTYPE array."""
+        if isinstance(items, np.ndarray) and items.dtype == PAIR_DTYPE:
+            arr, n = ctypes.c_void_p(items.ctypes.data), len(items)
+        else:
+            arr, keep = make_pairs(items)
+            n = len(arr)
         cap = max(64, 16 * n)
         counts = np.zeros(n, np.uint64)
         while True:
@@ -215,14 +252,19 @@ class XCorr:
 
     # serving -------------------------------------------------------------------
     def submit(self, items):
-        """Queues chunk pairs for the GPU; items as for align, or the (array,
-        keepalive) pair make_pairs returns (built ahead of time)."""
-        if isinstance(items, tuple) and len(items) == 2 and isinstance(items[0], ctypes.Array):
-            arr, keep = items
+        """Queues chunk pairs for the GPU; items as for align, the (array,
+        keepalive) pair make_pairs returns (built ahead of time), or a
+        PAIR_DTYPE array (block_pairs).  The library copies the sequences."""
+        if isinstance(items, np.ndarray) and items.dtype == PAIR_DTYPE:
+            arr, n = ctypes.c_void_p(items.ctypes.data), len(items)
         else:
-            arr, keep = make_pairs(items)
+            if isinstance(items, tuple) and len(items) == 2 and isinstance(items[0], ctypes.Array):
+                arr, keep = items
+            else:
+                arr, keep = make_pairs(items)
+            n = len(arr)
         t = ctypes.c_uint64()
-        _check(self.lib.xc_submit(self.ctx, arr, len(arr), ctypes.byref(t)), "xc_submit")
+        _check(self.lib.xc_submit(self.ctx, arr, n, ctypes.byref(t)), "xc_submit")
         return t.value
 
     def wait(self, ticket, timeout_ms=10000, cap=4096):

@@ -45,31 +45,33 @@ size_t corr_smem_bytes(int log2L) {
 // k = 0..N of the L-point spectrum, N = L/2, given by S(k)), ready for the
 // N-point inverse: Z(k) = E(k) + i O(k), E = (S(k) + conj S(N-k))/2,
 // O = (S(k) - conj S(N-k)) conj(W_L^k)/2; the inverse then holds
-// z[m] = r[2m] + i r[2m+1].  Threads t < NT_CORR.
-template <int LOG2L, class SF>
+// z[m] = r[2m] + i r[2m+1].  Threads t < NTF.  HALF = 0.5f as written; the
+// both-strands pair kernel passes 1.0f (its inverse then carries a power of
+// two, which FindTop's scale removes exactly).
+template <int LOG2L, int NTF = NT_CORR, class SF>
 __device__ __forceinline__ void hermitian_pack(float2* __restrict__ buf, const SF& S, const float2* twLh,
-                                               const float2* twLl, int t) {
+                                               const float2* twLl, int t, float HALF = 0.5f) {
   constexpr int N = 1 << (LOG2L - 1);
   constexpr int LOG2N = LOG2L - 1;
   const int la = lp<LOG2N>(t);
-  const int lb = lp<LOG2N>((NT_CORR - t) & (NT_CORR - 1));
+  const int lb = lp<LOG2N>((NTF - t) & (NTF - 1));
 #pragma unroll
-  for (int it = 0; it <= N / (2 * NT_CORR); it++) {
-    const int k = t + NT_CORR * it;
+  for (int it = 0; it <= N / (2 * NTF); it++) {
+    const int k = t + NTF * it;
     if (k > N / 2) break;
     const float2 Sk = S(k);
     const float2 Sn = S(N - k);
     {
-      const float2 Ev = make_float2(0.5f * (Sk.x + Sn.x), 0.5f * (Sk.y - Sn.y));
-      const float2 Dv = make_float2(0.5f * (Sk.x - Sn.x), 0.5f * (Sk.y + Sn.y));
+      const float2 Ev = make_float2(HALF * (Sk.x + Sn.x), HALF * (Sk.y - Sn.y));
+      const float2 Dv = make_float2(HALF * (Sk.x - Sn.x), HALF * (Sk.y + Sn.y));
       const float2 Ov = cmulc(Dv, tw2(twLh, twLl, k));
-      buf[la ^ lp<LOG2N>(NT_CORR * it)] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
+      buf[la ^ lp<LOG2N>(NTF * it)] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
     }
     if (k != 0 && k != N / 2) {
-      // N-k = (N - NT_CORR(it+1)) | (NT_CORR - t) for t >= 1
-      const int pb = t ? (lb ^ lp<LOG2N>(N - NT_CORR * (it + 1))) : lp<LOG2N>(N - NT_CORR * it);
-      const float2 Ev = make_float2(0.5f * (Sn.x + Sk.x), 0.5f * (Sn.y - Sk.y));
-      const float2 Dv = make_float2(0.5f * (Sn.x - Sk.x), 0.5f * (Sn.y + Sk.y));
+      // N-k = (N - NTF(it+1)) | (NTF - t) for t >= 1
+      const int pb = t ? (lb ^ lp<LOG2N>(N - NTF * (it + 1))) : lp<LOG2N>(N - NTF * it);
+      const float2 Ev = make_float2(HALF * (Sn.x + Sk.x), HALF * (Sn.y - Sk.y));
+      const float2 Dv = make_float2(HALF * (Sn.x - Sk.x), HALF * (Sn.y + Sk.y));
       const float2 Ov = cmulc(Dv, tw2(twLh, twLl, N - k));
       buf[pb] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
     }
@@ -79,34 +81,37 @@ __device__ __forceinline__ void hermitian_pack(float2* __restrict__ buf, const S
 // Step 5: FindTop (SeqAnalyzer::FindTop, CrossCorr.cc:878-944) over the
 // inverse in buf, for one strand: xc[i] = r[(i + N) mod L] / N; envelope
 // over 256-sample blocks when L/256 > 8; keep i with xc[i] > env*cutoff + 1
-// in increasing i.  Threads t < NT_CORR; warp w of them owns the contiguous
-// range [w*L/16, (w+1)*L/16), lanes stride by one.  Every thread of the CTA
-// calls it (two CTA barriers).  s_warp holds 2 * NT_CORR/32 ints.
+// in increasing i.  Threads t < NTF; warp w of them owns the contiguous
+// range [w*L/(NTF/32), (w+1)*L/(NTF/32)), lanes stride by one.  Every thread
+// of the barrier's group calls it (two barriers).  s_warp holds 2 * NTF/32
+// ints.  scale is 1/N for an inverse of the spectrum itself (a power of two
+// smaller when the inverse carries a power-of-two factor).
 //
 // Near-threshold lags: with P.strad_cnt set, every lag whose FP32 value lies
 // within straddle_rel(L) * max(1, max|xc|) of its FP32 threshold is counted
 // in strad_cnt[pair*2+strand] and the first STRAD_CAP of them are listed.
 // There the reference's FP32 FFT and this one may decide differently; every
 // other lag's decision is the same for both.
-template <int LOG2L, class SY = CtaBarrier>
+template <int LOG2L, int NTF = NT_CORR, class SY = CtaBarrier>
 __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, uint32_t off_base, int pidx,
                                          int strand, const float2* __restrict__ buf, int t, int* s_warp,
-                                         SY sync = SY()) {
+                                         SY sync = SY(), float scale = 1.0f / (float)(1 << (LOG2L - 1))) {
   constexpr int L = 1 << LOG2L;
   constexpr int N = L >> 1;
+  constexpr int NW = NTF / 32;   // warps of the group
   const int lane = t & 31, warp = t >> 5;
-  constexpr int PER_WARP = L / (NT_CORR / 32);
+  constexpr int PER_WARP = L / NW;
   constexpr int ITER = PER_WARP / 32;
   const int wbase = warp * PER_WARP;
-  const float scale = 1.0f / (float)N;
   auto xval = [&](int i) -> float {
     const int n = (i + N) & (L - 1);
     const float2 z = buf[swz(n >> 1)];
     return ((n & 1) ? z.y : z.x) * scale;
   };
-  // Up to L = 8192 a lane's 16 values stay in registers across the three
-  // passes (envelope, count, compaction); longer transforms re-read them.
-  constexpr bool KEEP = ITER <= 16;
+  // Up to L = 8192 a lane's values stay in registers across the three passes
+  // (envelope, count, compaction): 16 on 512 threads, 32 on 256; longer
+  // transforms re-read them.
+  constexpr bool KEEP = ITER <= (NTF <= 256 ? 32 : 16);
   float xs[KEEP ? ITER : 1];
   if constexpr (KEEP) {
 #pragma unroll
@@ -152,18 +157,19 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
   }
   int wcount = 0;
   float amax = 0.f;   // max |xc| of the lane's lags (for the near-threshold band)
-  unsigned msk[KEEP ? ITER : 1];
+  constexpr bool KEEPM = KEEP && ITER <= 16;   // ballots kept too (registers allowing)
+  unsigned msk[KEEPM ? ITER : 1];
 #pragma unroll(KEEP ? ITER : 4)
   for (int e = 0; e < ITER; e++) {
     const int i = wbase + e * 32 + lane;
     const float x = xat(e);
     const unsigned m = __ballot_sync(0xffffffffu, x > thrb[(L / 256 > 8) ? (e >> 3) : 0]);
-    if constexpr (KEEP) msk[e] = m;
+    if constexpr (KEEPM) msk[e] = m;
     wcount += __popc(m);
     amax = fmaxf(amax, fabsf(x));
     if (P.dbg_xc) P.dbg_xc[(size_t)(pidx * 2 + strand) * L + i] = x;
   }
-  int* s_max = s_warp + NT_CORR / 32;   // max |xc| bits per warp (non-negative floats order as ints)
+  int* s_max = s_warp + NW;   // max |xc| bits per warp (non-negative floats order as ints)
   if (P.strad_cnt) {
     const unsigned mb = __reduce_max_sync(0xffffffffu, __float_as_uint(amax));
     if (lane == 0) s_max[warp] = (int)mb;
@@ -171,15 +177,15 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
   if (lane == 0) s_warp[warp] = wcount;
   sync();
   if (warp == 0) {
-    const int v = lane < NT_CORR / 32 ? s_warp[lane] : 0;
+    const int v = lane < NW ? s_warp[lane] : 0;
     int w = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int u = __shfl_up_sync(0xffffffffu, w, o);
       if (lane >= o) w += u;
     }
-    if (lane < NT_CORR / 32) s_warp[lane] = w - v;
-    if (lane == NT_CORR / 32 - 1) P.off_cnt[pidx * 2 + strand] = w;
+    if (lane < NW) s_warp[lane] = w - v;
+    if (lane == NW - 1) P.off_cnt[pidx * 2 + strand] = w;
   }
   sync();
   int run = s_warp[warp];
@@ -187,7 +193,7 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
   if (P.strad_cnt) {
     unsigned mb = 0u;
 #pragma unroll
-    for (int k = 0; k < NT_CORR / 32; k++) mb = max(mb, (unsigned)s_max[k]);
+    for (int k = 0; k < NW; k++) mb = max(mb, (unsigned)s_max[k]);
     band = straddle_rel(LOG2L) * fmaxf(1.0f, __uint_as_float(mb));
   }
   int* out = P.off_list + off_base + (size_t)strand * L;
@@ -197,7 +203,7 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
     const int i = wbase + e * 32 + lane;
     const float thr = thrb[(L / 256 > 8) ? (e >> 3) : 0];
     unsigned m;
-    if constexpr (KEEP) m = msk[e];
+    if constexpr (KEEPM) m = msk[e];
     else m = __ballot_sync(0xffffffffu, xat(e) > thr);
     if ((m >> lane) & 1u) out[run + __popc(m & lt)] = i;
     run += __popc(m);
@@ -877,10 +883,10 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
   //      target-only bins are the same for both strands ----
   float2* buf = half ? WE : ZE;
   if (half == 0) {
-    hermitian_pack<LOG2L>(ZE, [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; }, twLh, twLl,
+    hermitian_pack<LOG2L, NT_CORR>(ZE, [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; }, twLh, twLl,
                           ht);
   } else {
-    hermitian_pack<LOG2L>(WE,
+    hermitian_pack<LOG2L, NT_CORR>(WE,
                           [&](int k) -> float2 {
                             if (k >= N - 1) return (k & 1) ? aFO[k >> 1] : aFE[k >> 1];
                             const float2 r = (k & 1) ? aRO[k >> 1] : aRE[k >> 1];
@@ -897,8 +903,356 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
   fft_inverse<LOG2N, Plan<LOG2N>, Plan<LOG2N>::n - 1, GroupBarrier>(buf, twNh, twNl, ht, NT_CORR, hb);
 
   // ---- 5. FindTop, one strand per half ----
-  find_top<LOG2L, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, half, buf, ht, s_warp[half],
+  find_top<LOG2L, NT_CORR, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, half, buf, ht, s_warp[half],
                                 hb);
+}
+
+// ---------------------------------------------------------------------------
+// corr_pair2_kernel<13>: the persistent both-strands form.  One CTA of 512
+// threads per SM strides over the FFT-8192 pairs of a launch; the next pair's
+// chunk bytes arrive by cp.async while the current one is transformed.  Each
+// thread carries two butterflies per pass (the even-bin and odd-bin
+// transforms of one packed signal) and generates their twiddles once.  The
+// same premise as corr_pair_kernel (reverse strand from the forward spectra),
+// with these changes to the work per pair:
+//  - the transform input is built in registers inside the first pass: thread
+//    g of a group takes positions g + 256 r (r < 16) from one word of 2-bit
+//    codes and the windows' channel values, so no input buffer is written;
+//  - the per-bin step forms the sums without separating the channels:
+//    with A = Zt(m), B = Zt(N-m), C = Zq(m), D = Zq(N-m) (Zt, Zq the
+//    transforms of t_c0 + i t_c1 and q_c0 + i q_c1),
+//      2 sum_c conj(T_c) Q_c = conj(A) C + B conj(D)
+//      2i (T_c0 Q_c1 + T_c1 Q_c0) = A C - conj(B D),
+//    and the reverse strand's sum W_L^((Q-1)k) conj(R) becomes
+//    W_L^((Q-1)k) (i conj(2i R)) / 2, i conj(x + iy) = y + ix;
+//  - the factors of two are left in (exact powers of two) and removed by
+//    FindTop's scale 1/(4N).
+// Pairs outside the premise go on P.fb_list for corr_kernel, as there.
+// ---------------------------------------------------------------------------
+size_t corr_pair2_smem_bytes() {
+  constexpr size_t N = 4096, NH = N / 64;
+  return (6 * N + 16 + 2 * (NH + 64)) * sizeof(float2)   // 4 transforms, F and R sums, twiddles
+         + 2 * N                                           // chunk bytes (target, query)
+         + 2 * 256 * sizeof(float)                         // entropy weight per window
+         + 2 * 256 * sizeof(float4)                        // window values of a channel pair
+         + 2 * 256 * sizeof(uint32_t);                     // 2-bit codes of positions g + 256 r
+}
+
+// Issues the cp.async copies of pair pidx's chunk bytes into st / sq: thread
+// t takes 16-byte piece t & 255 of the target (t < 256) or the query; bytes
+// past the chunk end are zero-filled (pool chunks are 16-byte aligned).
+__device__ __forceinline__ void pair2_prefetch(const CorrParams& P, int pidx, uint8_t* st, uint8_t* sq, int tid) {
+  const PairDesc& D = P.pairs[pidx];
+  const int which = tid >> 8, c = tid & 255;
+  const int len = which ? D.qlen : D.tlen;
+  const uint8_t* src = P.pool + (which ? D.q_off : D.t_off);
+  const int valid = min(max(len - 16 * c, 0), 16);
+  if (valid > 0) src += 16 * c;   // else: nothing is read; the chunk start stays a valid address
+  const uint32_t dst = (uint32_t)__cvta_generic_to_shared((which ? sq : st) + 16 * c);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid) : "memory");
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+template <int LOG2L>
+__global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParams P) {
+  constexpr int L = 1 << LOG2L;
+  constexpr int N = L >> 1;
+  constexpr int LOG2N = LOG2L - 1;
+  constexpr int WIN = L / 512;
+  constexpr int NWIN = 256;
+  constexpr int NH = N / 64;
+  static_assert(N == 16 * NWIN && N == 4096, "thread g of a group owns positions g + 256 r, r < 16");
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* ZE = reinterpret_cast<float2*>(smem);   // z = t_c0 + i t_c1, even-bin transform
+  float2* ZO = ZE + N;                            // z * W_L^n, odd-bin transform
+  float2* WE = ZO + N;                            // w = q_c0 + i q_c1
+  float2* WO = WE + N;
+  float2* aFE = WO + N;                           // 2 x forward-strand sum, bins 2m, m <= N/2
+  float2* aFO = aFE + (N / 2 + 8);                // bins 2m+1
+  float2* aRE = aFO + N / 2;                      // 2i x R, bins 2m (m < N/2)
+  float2* aRO = aRE + (N / 2 + 8);                // bins 2m+1
+  float2* twNh = aRO + N / 2;
+  float2* twNl = twNh + NH;
+  float2* twLh = twNl + 64;
+  float2* twLl = twLh + NH;
+  uint8_t* st = reinterpret_cast<uint8_t*>(twLl + 64);
+  uint8_t* sq = st + N;
+  float* Et = reinterpret_cast<float*>(sq + N);
+  float* Eq = Et + NWIN;
+  float4* vv = reinterpret_cast<float4*>(Eq + NWIN);   // [sequence][window]: c0 (w=0, w=1), c1 (w=0, w=1)
+  uint32_t* cw = reinterpret_cast<uint32_t*>(vv + 2 * NWIN);   // [sequence][g]
+  __shared__ int s_cnt4[8];
+  __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
+  __shared__ Split3 s_wf[2][8];    // the same as three floats each
+  __shared__ int s_warp[2][2 * 256 / 32];
+
+  const int tid = threadIdx.x;
+  const int G = tid >> 8;          // 0: target transforms / forward strand, 1: query / reverse strand
+  const int g = tid & 255;
+  const GroupBarrier gb{1 + G, 256};
+
+  for (int i = tid; i < NH; i += NT_PAIR2) {
+    twNh[i] = P.tab.twN_hi[i];
+    twLh[i] = P.tab.twL_hi[i];
+  }
+  if (tid < 64) {
+    twNl[tid] = P.tab.twN_lo[tid];
+    twLl[tid] = P.tab.twL_lo[tid];
+  }
+  if ((int)blockIdx.x < P.count) pair2_prefetch(P, P.first + blockIdx.x, st, sq, tid);
+
+  for (int p = blockIdx.x; p < P.count; p += gridDim.x) {
+    const int pidx = P.first + p;
+    const int next = p + (int)gridDim.x < P.count ? P.first + p + (int)gridDim.x : -1;
+    const int T = P.pairs[pidx].tlen, Q = P.pairs[pidx].qlen;
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    if (tid < 8) s_cnt4[tid] = 0;
+    __syncthreads();
+
+    // ---- 1. byte checks on this thread's 16-byte piece (zero past the end):
+    //      per byte, exactly, (y & 0x7f) + 0x7f | y has bit 7 clear iff y == 0 ----
+    int high = 0, nonacgt = 0;
+    {
+      const int which = tid >> 8, c = tid & 255;
+      const int valid = (which ? Q : T) - 16 * c;
+      const uint4 v = *reinterpret_cast<const uint4*>((which ? sq : st) + 16 * c);
+      const uint32_t x[4] = {v.x, v.y, v.z, v.w};
+      auto nz = [](uint32_t y) { return (((y & 0x7f7f7f7fu) + 0x7f7f7f7fu) | y) & 0x80808080u; };
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int vk = min(max(valid - 4 * k, 0), 4);
+        const uint32_t m = vk >= 4 ? 0xffffffffu : (1u << (8 * vk)) - 1u;
+        high |= (x[k] & m & 0x80808080u) != 0u;
+        const uint32_t bad = nz(x[k] ^ 0x41414141u) & nz(x[k] ^ 0x43434343u) & nz(x[k] ^ 0x47474747u) &
+                             nz(x[k] ^ 0x54545454u);   // bit 7: byte is not A, C, G or T
+        nonacgt |= (bad & m & 0x80808080u) != 0u;
+      }
+    }
+    const int any_high = __syncthreads_or(high);
+    const int generic = __syncthreads_or(nonacgt);
+    if (any_high || generic || (Q >= 1024 && Q % WIN != 0) || P.dbg_sig) {
+      if (tid == 0) {
+        if (any_high) {
+          P.off_cnt[pidx * 2] = 0;
+          P.off_cnt[pidx * 2 + 1] = 0;
+          P.pair_flags[pidx] = PF_INVALID;
+        } else {
+          P.fb_list[atomicAdd(P.fb_cnt, 1)] = pidx;   // the per-strand kernel takes it
+        }
+      }
+      if (next >= 0) pair2_prefetch(P, next, st, sq, tid);   // the bytes were read before the barriers above
+      continue;
+    }
+    if (tid == 0) P.pair_flags[pidx] = P.pairs[pidx].flags & PF_FAST;
+
+    // ---- 2a. entropy weight per window (CCSignal::ComputeEntropy,
+    //      CrossCorr.cc:35-93): group 0 target windows, group 1 query ----
+    {
+      const uint8_t* sb = G ? sq : st;
+      const int len = G ? Q : T;
+      float E = 0.f;
+      if (len < 1024) {
+        E = 1.f;
+      } else if (g * WIN + WIN <= len) {
+        const int i0 = g * WIN;
+        uint32_t cnt = 0;
+        for (int j = 0; j < WIN; j++) cnt += 1u << (8 * code_of(sb[i0 + j]));
+        const int a = cnt & 255u, c = (cnt >> 8) & 255u, gg = (cnt >> 16) & 255u;
+        E = __ldg(&P.tab.ent_acgt[(a * (WIN + 1) + c) * (WIN + 1) + gg]);
+      } else if (g * WIN < len) {
+        const int i0 = g * WIN;
+        const int k = len - i0;
+        int a4 = 0, c4 = 0, g4 = 0, t4 = 0;
+        for (int j = 0; j < k; j++) {
+          const uchar4 q = c_w4q[sb[i0 + j]];
+          a4 += q.x; c4 += q.y; g4 += q.z; t4 += q.w;
+        }
+        const double* et = P.tab.ent + k * (4 * WIN + 1);
+        const double sv =
+            __dadd_rn(__dadd_rn(__dadd_rn(__ldg(et + a4), __ldg(et + c4)), __ldg(et + g4)), __ldg(et + t4));
+        E = __double2float_rn(-sv);
+        if (E < 0.f) E = 0.f;
+      }
+      (G ? Eq : Et)[g] = E;
+    }
+    // ---- 2b. base counts for the channel means (SeqToPCM, CrossCorr.cc:108-116),
+    //      and the 2-bit codes of positions g + 256 r in one word per thread ----
+    {
+      uint32_t ct = 0, cq = 0;   // one 8-bit count field per base, at most N / 512 each
+      for (int i = tid; i < N; i += NT_PAIR2) {
+        if (i < T) ct += 1u << (8 * code_of(st[i]));
+        if (i < Q) cq += 1u << (8 * code_of(sq[i]));
+      }
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int vt = __reduce_add_sync(0xffffffffu, 4 * (int)((ct >> (8 * k)) & 255u));
+        const int vq = __reduce_add_sync(0xffffffffu, 4 * (int)((cq >> (8 * k)) & 255u));
+        if ((tid & 31) == 0) {
+          if (vt) atomicAdd(&s_cnt4[k], vt);
+          if (vq) atomicAdd(&s_cnt4[4 + k], vq);
+        }
+      }
+      const uint8_t* sb = G ? sq : st;
+      uint32_t w = 0;
+#pragma unroll
+      for (int r = 0; r < 16; r++) w |= code_of(sb[g + 256 * r]) << (2 * r);
+      cw[tid] = w;
+    }
+    __syncthreads();   // the chunk bytes are no longer read: the next pair's may come in
+    if (next >= 0) pair2_prefetch(P, next, st, sq, tid);
+    if (tid < 8) {
+      const int len = (tid >> 2) ? Q : T;
+      const double off = len > 0 ? __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len) : 0.0;
+      s_wmo[0][tid] = __dsub_rn(0.0, off);
+      s_wmo[1][tid] = __dsub_rn(1.0, off);
+      s_wf[0][tid] = split3(s_wmo[0][tid]);
+      s_wf[1][tid] = split3(s_wmo[1][tid]);
+    }
+    __syncthreads();
+
+    // one stage per channel pair, (A, T) then (C, G); a loop the compiler
+    // keeps rolled, so nothing of one stage stays live into the other
+#pragma unroll 1
+    for (int stg = 0; stg < 2; stg++) {
+      const int c0 = stg ? 1 : 0, c1 = stg ? 2 : 3;
+      const bool first = stg == 0;
+      // ---- 3a. per-window channel values float(entropy * (weight - mean))
+      //      (CrossCorr.cc:123), weight 0 or 1; group G writes sequence G's ----
+      {
+        const float E = (G ? Eq : Et)[g];
+        const int k0 = G * 4 + c0, k1 = G * 4 + c1;
+        vv[G * NWIN + g] = make_float4(mul_round_f32(E, s_wf[0][k0], s_wmo[0][k0]),
+                                       mul_round_f32(E, s_wf[1][k0], s_wmo[1][k0]),
+                                       mul_round_f32(E, s_wf[0][k1], s_wmo[0][k1]),
+                                       mul_round_f32(E, s_wf[1][k1], s_wmo[1][k1]));
+      }
+      gb();
+      // ---- 3b. first forward pass with its input built in registers:
+      //      x_E[r] = z[g + 256 r], x_O[r] = z[g + 256 r] W_L^(g + 256 r),
+      //      W_L^(256 r) = exp(-i pi r / 16); then the radix-16 butterflies
+      //      of span N and their twiddles W_N^(g r), shared by both ----
+      {
+        const uint32_t codes = cw[tid];
+        const int len = G ? Q : T;
+        const float4* vw = vv + G * NWIN + (g >> 4);   // window of position g + 256 r: (g >> 4) + 16 r
+        const float2 wg = tw2(twLh, twLl, g);
+        float2 xe[16], xo[16];
+#pragma unroll
+        for (int r = 0; r < 16; r++) {
+          const float4 v = vw[16 * r];
+          const uint32_t code = (codes >> (2 * r)) & 3u;
+          float2 z = make_float2(0.f, 0.f);
+          if (g + 256 * r < len) z = make_float2(code == (uint32_t)c0 ? v.y : v.x, code == (uint32_t)c1 ? v.w : v.z);
+          xe[r] = z;
+          xo[r] = cmul(cmul(z, wg), make_float2(cos_pi16(r), -sin_pi16(r)));
+        }
+        DFT<16, -1>::run(xe);
+        DFT<16, -1>::run(xo);
+        const Tw16 tw = tw16(twNh, twNl, g);
+#pragma unroll
+        for (int r = 1; r < 16; r++) {
+          const float2 w = tw16_r(tw, r);
+          xe[r] = cmul(xe[r], w);
+          xo[r] = cmul(xo[r], w);
+        }
+        float2* bE = G ? WE : ZE;
+        float2* bO = bE + N;
+        const int sb = swz(g);
+#pragma unroll
+        for (int r = 0; r < 16; r++) {
+          bE[sb ^ swz(256 * r)] = xe[r];
+          bO[sb ^ swz(256 * r)] = xo[r];
+        }
+      }
+      gb();
+      // ---- 3c. the other two passes, both transforms of the group at once ----
+      {
+        float2* bE = G ? WE : ZE;
+        fft_pass16_x2<N, N / 16>(bE, bE + N, twNh, twNl, g);
+        gb();
+        fft_pass16_x2<N, N / 256>(bE, bE + N, twNh, twNl, g);
+      }
+      __syncthreads();   // the per-bin step reads both groups' spectra
+      // ---- 3d. per-bin step (CrossCorrelation::DoOne, CrossCorr.cc:477-492):
+      //      bin 0 is the product of real values (the general formula with
+      //      B = A, D = C); bins N-1 and N keep the targets' own values, which
+      //      the reference's loop leaves unmultiplied, for both strands.
+      //      Group 0: even bins, group 1: odd bins. ----
+      if (G == 0) {
+        const int la = lp<LOG2N>(g);
+        const int lb = lp<LOG2N>((256 - g) & 255);
+#pragma unroll
+        for (int it = 0; it <= N / 512; it++) {
+          const int m = g + 256 * it;
+          if (m > N / 2) break;
+          const int pa = la ^ lp<LOG2N>(256 * it);
+          // partner N-m = (N - 256(it+1)) | (256 - g) for g >= 1
+          const int pb = g ? (lb ^ lp<LOG2N>(N - 256 * (it + 1))) : lp<LOG2N>((N - 256 * it) & (N - 1));
+          const float2 A = ZE[pa], B = ZE[pb], C = WE[pa], D = WE[pb];
+          if (m == N / 2) {   // Nyquist: 2 (T_c0 + T_c1), both real
+            const float2 f = make_float2(2.f * (A.x + A.y), 0.f);
+            aFE[m] = first ? f : cadd(aFE[m], f);
+          } else {
+            const float2 f = cadd(cmulc(C, A), cmulc(B, D));
+            const float2 ac = cmul(A, C), bd = cmul(B, D);
+            const float2 r = make_float2(ac.x - bd.x, ac.y + bd.y);
+            aFE[m] = first ? f : cadd(aFE[m], f);
+            aRE[m] = first ? r : cadd(aRE[m], r);
+          }
+        }
+      } else {
+        const int la = lp<LOG2N>(g);
+#pragma unroll
+        for (int it = 0; it < N / 512; it++) {
+          const int m = g + 256 * it;
+          const int pa = la ^ lp<LOG2N>(256 * it);
+          const int pb = pa ^ lp<LOG2N>(N - 1);   // N-1-m = m ^ (N-1)
+          const float2 A = ZO[pa], B = ZO[pb], C = WO[pa], D = WO[pb];
+          if (m == N / 2 - 1) {   // bin N-1: 2 (T_c0 + T_c1) = (A + conj B) - i (A - conj B)
+            const float2 f = make_float2((A.x + B.x) + (A.y + B.y), (A.y - B.y) - (A.x - B.x));
+            aFO[m] = first ? f : cadd(aFO[m], f);
+          } else {
+            const float2 f = cadd(cmulc(C, A), cmulc(B, D));
+            const float2 ac = cmul(A, C), bd = cmul(B, D);
+            const float2 r = make_float2(ac.x - bd.x, ac.y + bd.y);
+            aFO[m] = first ? f : cadd(aFO[m], f);
+            aRO[m] = first ? r : cadd(aRO[m], r);
+          }
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- 4. inverses: group 0 the forward strand into ZE, group 1 the
+    //      reverse strand S_r(k) = W_L^((Q-1)k) i conj(2i R(k)) into WE; the two
+    //      target-only bins are the same for both strands.  Sums and the pack
+    //      carry factors 2 and 2: FindTop scales by 1/(4N). ----
+    float2* buf = G ? WE : ZE;
+    if (G == 0) {
+      hermitian_pack<LOG2L, 256>(ZE, [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; }, twLh,
+                                 twLl, g, 1.0f);
+    } else {
+      hermitian_pack<LOG2L, 256>(WE,
+                                 [&](int k) -> float2 {
+                                   if (k >= N - 1) return (k & 1) ? aFO[k >> 1] : aFE[k >> 1];
+                                   const float2 r = (k & 1) ? aRO[k >> 1] : aRE[k >> 1];
+                                   const int j = ((Q - 1) * k) & (L - 1);
+                                   float2 w = tw2(twLh, twLl, j & (N - 1));   // W_L^j, j < L/2
+                                   if (j & N) w = make_float2(-w.x, -w.y);   // W_L^(j + L/2) = -W_L^j
+                                   return cmul(w, make_float2(r.y, r.x));
+                                 },
+                                 twLh, twLl, g, 1.0f);
+    }
+    gb();
+    fft_inverse<LOG2N, Plan<LOG2N>, Plan<LOG2N>::n - 1, GroupBarrier>(buf, twNh, twNl, g, 256, gb);
+
+    // ---- 5. FindTop, one strand per group ----
+    find_top<LOG2L, 256, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, G, buf, g, s_warp[G], gb,
+                                       1.0f / (float)(4 * N));
+    __syncthreads();   // buffers and per-pair words are reused by the next pair
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -917,6 +1271,9 @@ cudaError_t prepare_kernels() {
   cudaError_t e = cudaFuncSetAttribute(corr_pair_kernel<PAIR_LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)corr_pair_smem_bytes(PAIR_LOG2L));
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(corr_pair2_kernel<PAIR_LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)corr_pair2_smem_bytes());
+  if (e != cudaSuccess) return e;
   if ((e = set_corr_attrs<10>()) != cudaSuccess) return e;
   if ((e = set_corr_attrs<11>()) != cudaSuccess) return e;
   if ((e = set_corr_attrs<12>()) != cudaSuccess) return e;
@@ -934,12 +1291,17 @@ cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t
     // both strands per CTA, then corr_kernel over the pairs handed back:
     // one wave of CTAs striding over the list (*fb_cnt starts at zero)
     if (log2L != PAIR_LOG2L) return cudaErrorInvalidValue;
-    corr_pair_kernel<PAIR_LOG2L><<<npairs, NT_PAIR, corr_pair_smem_bytes(PAIR_LOG2L), s>>>(p);
     static const int sms = [] {
       int dev = 0, n = 152;
       if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
       return n;
     }();
+    CorrParams q = p;
+    q.count = npairs;
+    if (p.pair_form == 2)   // persistent: one CTA per SM strides over the pairs
+      corr_pair2_kernel<PAIR_LOG2L><<<std::min(npairs, sms), NT_PAIR2, corr_pair2_smem_bytes(), s>>>(q);
+    else
+      corr_pair_kernel<PAIR_LOG2L><<<npairs, NT_PAIR, corr_pair_smem_bytes(PAIR_LOG2L), s>>>(q);
     grid.x = std::min(npairs, sms);
   }
   switch (log2L) {

@@ -181,6 +181,63 @@ template <int DIR> struct DFT<16, DIR> {
   }
 };
 
+// Twiddles W^(j r), r = 1..15, of a radix-16 pass: W^m and W^(4m) from the
+// two-level tables (m = j * N/S), the others by products; about 4 ulp each.
+struct Tw16 {
+  float2 w1, w2, w3, w4, w8, w12;
+};
+__device__ __forceinline__ Tw16 tw16(const float2* twh, const float2* twl, int m1) {
+  Tw16 t;
+  t.w1 = tw2(twh, twl, m1);
+  t.w4 = tw2(twh, twl, 4 * m1);
+  t.w2 = cmul(t.w1, t.w1);
+  t.w3 = cmul(t.w2, t.w1);
+  t.w8 = cmul(t.w4, t.w4);
+  t.w12 = cmul(t.w8, t.w4);
+  return t;
+}
+// W^(j r) for a compile-time r = 4a + b.
+__device__ __forceinline__ float2 tw16_r(const Tw16& t, int r) {
+  const int a = r >> 2, bb = r & 3;
+  const float2 wa = a == 1 ? t.w4 : a == 2 ? t.w8 : t.w12;
+  const float2 wb = bb == 1 ? t.w1 : bb == 2 ? t.w2 : t.w3;
+  return a == 0 ? wb : bb == 0 ? wa : cmul(wa, wb);
+}
+
+// One forward radix-16 pass of span S over two N-point buffers at once
+// (butterfly b of each): the twiddles are generated once for both.  Same
+// arithmetic per buffer as fft_pass<16, N, S, false>.
+template <int N, int S>
+__device__ __forceinline__ void fft_pass16_x2(float2* __restrict__ bufA, float2* __restrict__ bufB,
+                                              const float2* __restrict__ twh, const float2* __restrict__ twl,
+                                              int b) {
+  constexpr int d = S / 16;
+  const int j = b & (d - 1);
+  const int sb = swz((b - j) * 16 + j);
+  float2 xa[16], xb[16];
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    xa[r] = bufA[sb ^ swz(r * d)];
+    xb[r] = bufB[sb ^ swz(r * d)];
+  }
+  DFT<16, -1>::run(xa);
+  DFT<16, -1>::run(xb);
+  if constexpr (d > 1) {
+    const Tw16 t = tw16(twh, twl, j * (N / S));
+#pragma unroll
+    for (int r = 1; r < 16; r++) {
+      const float2 w = tw16_r(t, r);
+      xa[r] = cmul(xa[r], w);
+      xb[r] = cmul(xb[r], w);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    bufA[sb ^ swz(r * d)] = xa[r];
+    bufB[sb ^ swz(r * d)] = xb[r];
+  }
+}
+
 // One in-place pass of span S and radix R over an N-point buffer.
 // Forward (decimation in frequency): butterfly, then twiddle W_S^(j r').
 // Inverse (decimation in time, the exact reverse): conjugate twiddle, then

@@ -10,7 +10,8 @@ constexpr int MIN_LOG2L = 10;    // FFT length 1024
 constexpr int MAX_LOG2L = 15;    // FFT length 32768
 constexpr int MAX_SMEM_LOG2L = 14;  // longest FFT whose two transforms and channel sums fit one SM
 constexpr int NT_CORR = 512;     // threads of the correlation kernel (one pair strand)
-constexpr int NT_PAIR = 1024;    // threads of the both-strands correlation kernel
+constexpr int NT_PAIR = 1024;    // threads of the both-strands correlation kernel (first form)
+constexpr int NT_PAIR2 = 512;    // threads of the persistent both-strands correlation kernel
 constexpr int PAIR_LOG2L = 13;   // FFT length of the both-strands kernel (its buffers fill one SM)
 constexpr int NT_SCAN = 128;     // threads of the scan kernel
 constexpr int OFF_CHUNK = 256;   // offsets staged per scan chunk
@@ -92,6 +93,8 @@ struct CorrParams {
   int* fb_cnt;              //   hands back ([*fb_cnt], zeroed before) go to corr_kernel
   int* strad_cnt;           // optional: near-threshold lags per [pair*2 + strand] (zeroed before)
   int* strad_list;          //   and the first STRAD_CAP of them, [pair*2 + strand][STRAD_CAP]
+  int count;                // pairs of this launch (set by launch_corr)
+  int pair_form;            // with fb_list: 2 = persistent 512-thread kernel, 1 = 1024-thread form
 };
 
 // Global channel-sum scratch of one pair strand for FFT lengths beyond one

@@ -157,6 +157,7 @@ int align_pair_noalloc(Ctx* c, const xc_pair& p, xc_result* out, size_t cap, siz
     // CTA, or the per-strand kernel for a pair it hands back
     cp.fb_list = cnt + C_FB;
     cp.fb_cnt = cnt + C_MISC + 3;
+    cp.pair_form = c->pair_form;
   }
   NA_CHECK(launch_corr(lg, cp, 1, s));
 

@@ -138,8 +138,12 @@ static int build_tables(Ctx* c) {
             const int tt = win - a - cc - g;
             sym = sym && eacgt[((size_t)a * W1 + cc) * W1 + g] == eacgt[((size_t)tt * W1 + g) * W1 + cc];
           }
-      const char* env = getenv("SATSUMA2_GB300_PAIR_KERNEL");   // "0": one corr_kernel CTA per strand
+      // SATSUMA2_GB300_PAIR_KERNEL: "0" one corr_kernel CTA per strand for
+      // every pair, "1" the 1024-thread both-strands kernel, else (default)
+      // the persistent 512-thread one
+      const char* env = getenv("SATSUMA2_GB300_PAIR_KERNEL");
       c->pair_kernel = sym && !(env && env[0] == '0');
+      c->pair_form = (env && env[0] == '1') ? 1 : 2;
     }
     DevTables& t = c->tab[lg];
     XC_CHECK(cudaMalloc(&t.tw, tw.size() * sizeof(float2)));
@@ -504,6 +508,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     if (bk.log2L == PAIR_LOG2L && c->pair_kernel) {
       cp.fb_list = b->d_fb;
       cp.fb_cnt = b->d_misc + 3;   // zeroed above
+      cp.pair_form = c->pair_form;
     }
     cp.strad_cnt = b->d_stradcnt;
     cp.strad_list = b->d_strad;

@@ -102,6 +102,7 @@ struct Ctx {
   uint64_t last_h2d = 0, last_d2h = 0;
   int sms = 152;               // multiprocessors of the device (sub-batch sizing)
   bool pair_kernel = false;    // both-strands correlation kernel usable (entropy table complement-symmetric)
+  int pair_form = 2;           // its form: 2 persistent 512-thread kernel, 1 the 1024-thread one
   unsigned char* noalloc_base = nullptr;   // xc_align_pair_noalloc's static array on this device (set at first use)
 };
 

@@ -15,7 +15,9 @@ the cross-correlation path:
                        both sides; FFT length nextpow2(2*max(tLen,qLen)).
 * ``serving_genomes`` -- a target genome (GC 41%) and an 80% identity query
                        derived from it with inversions, segmental duplications
-                       and 10% novel insertions, chunked as the slave does.
+                       and 10% novel insertions, chunked as the slave does;
+                       ``grid_search_blocks`` orders its 24x24 chunk blocks as
+                       a grid search would submit them.
 * ``large_batch``   -- 16384x16384 pairs (FFT length 32768), 30% of the
                        sequence low-complexity microsatellites, GC U[25,70]%.
 """
@@ -192,24 +194,39 @@ def large_batch(n=2000, seed=42, length=16384):
 
 
 def serving_genomes(seed=42, size=20_000_000, n_inv=30, inv_range=(10_000, 200_000),
-                    n_dup=20, dup_range=(5_000, 50_000), novel_frac=0.10, identity=0.80):
+                    n_dup=20, dup_range=(5_000, 50_000), novel_frac=0.10, identity=0.80, with_map=False):
     """Target genome (GC 41%) and a derived query: 80% identity, inversions,
-    segmental duplications and novel insertions (about novel_frac of the length)."""
+    segmental duplications and novel insertions (about novel_frac of the length).
+
+    with_map: also returns (src, rev), for every query base the target
+    position it derives from (-1 for novel bases) and whether it is
+    reverse-complemented."""
     rng = np.random.default_rng(seed)
     target = random_bases(rng, size, 0.41)
     q = target.copy()
+    src = np.arange(size, dtype=np.int32) if with_map else None
+    rev = np.zeros(size, bool) if with_map else None
     for _ in range(n_inv):
         ln = int(rng.integers(*inv_range))
         ln = min(ln, size // 4)
         p = int(rng.integers(0, size - ln))
         q[p:p + ln] = revcomp(q[p:p + ln])
-    pieces = [q]
+        if with_map:
+            src[p:p + ln] = src[p:p + ln][::-1].copy()
+            rev[p:p + ln] = ~rev[p:p + ln][::-1]
+    pieces, spieces, rpieces = [q], [src], [rev]
     for _ in range(n_dup):
         ln = int(rng.integers(*dup_range))
         ln = min(ln, size // 8)
         p = int(rng.integers(0, size - ln))
         pieces.append(q[p:p + ln].copy())
+        if with_map:
+            spieces.append(src[p:p + ln].copy())
+            rpieces.append(rev[p:p + ln].copy())
     q = np.concatenate(pieces)
+    if with_map:
+        src = np.concatenate(spieces)
+        rev = np.concatenate(rpieces)
     sub = rng.random(len(q)) > identity
     shift = rng.integers(1, 4, size=int(sub.sum()))
     idx = np.clip(np.searchsorted(ACGT, q[sub]), 0, 3)
@@ -218,14 +235,70 @@ def serving_genomes(seed=42, size=20_000_000, n_inv=30, inv_range=(10_000, 200_0
     total_ins = int(novel_frac * size)
     cuts = np.sort(rng.integers(0, len(q), size=n_ins))
     lens = rng.multinomial(total_ins, np.ones(n_ins) / n_ins)
-    out, prev = [], 0
+    out, so, ro, prev = [], [], [], 0
     for c, ln in zip(cuts, lens):
         out.append(q[prev:c])
         out.append(random_bases(rng, int(ln), 0.41))
+        if with_map:
+            so += [src[prev:c], np.full(int(ln), -1, np.int32)]
+            ro += [rev[prev:c], np.zeros(int(ln), bool)]
         prev = c
     out.append(q[prev:])
     query = np.concatenate(out)
+    if with_map:
+        so.append(src[prev:])
+        ro.append(rev[prev:])
+        return target.tobytes(), query.tobytes(), (np.concatenate(so), np.concatenate(ro))
     return target.tobytes(), query.tobytes()
+
+
+def grid_search_blocks(src, n_tchunks, n_qchunks, t_step=3072, q_step=4096, block=24, seed_every=8,
+                       per_round=64, probes=4):
+    """Blocks of block x block chunk pairs in the order a grid search over the
+    chunk matrix would submit them (GridSearch::CollectTargets,
+    analysis/GridSearch.cc:354-411): blocks holding homology (found from the
+    query-to-target map src, probes positions per query chunk) are the hits;
+    every seed_every-th hit in query order seeds the search; each round then
+    takes up to per_round unknown blocks next to processed hits, ordered by
+    the number of processed hits around them (descending), then by target and
+    query block, as CollectTargets sorts GridTarget.  Returns [(tf, tt, qf,
+    qt)] inclusive chunk ranges, query blocks of one target block row-major
+    in submission order."""
+    ntb = (n_tchunks + block - 1) // block
+    nqb = (n_qchunks + block - 1) // block
+    hits = set()
+    for j in range(n_qchunks):
+        for k in range(probes):
+            pos = j * q_step + (k * q_step) // probes + q_step // (2 * probes)
+            if pos >= len(src) or src[pos] < 0:
+                continue
+            i = min(int(src[pos]) // t_step, n_tchunks - 1)
+            hits.add((i // block, j // block))
+    known = {}
+    order = []
+    seeds = sorted(hits, key=lambda b: (b[1], b[0]))[::seed_every]
+    count = {}
+
+    def take(b):
+        known[b] = True
+        order.append(b)
+        if b in hits:
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    nb = (b[0] + dx, b[1] + dy)
+                    if (dx or dy) and 0 <= nb[0] < ntb and 0 <= nb[1] < nqb and nb not in known:
+                        count[nb] = count.get(nb, 0) + 1
+
+    for b in seeds:
+        take(b)
+    while True:
+        cand = sorted((b for b in count if b not in known), key=lambda b: (-count[b], b[0], b[1]))[:per_round]
+        if not cand:
+            break
+        for b in cand:
+            take(b)
+    return [(x * block, min((x + 1) * block, n_tchunks) - 1, y * block, min((y + 1) * block, n_qchunks) - 1)
+            for x, y in order]
 
 
 def chunk_starts(length, size, overlap):
