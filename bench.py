@@ -575,7 +575,10 @@ def run_ours(args):
 
     # ---- the other configurations, for reference (device-resident batches,
     #      L2 flushed, median of 3 runs): uneven lengths over FFT buckets
-    #      1024..8192, and 16384-bp chunks at FFT 32768 ----
+    #      1024..8192, 16384-bp chunks at FFT 32768, and the benchmark batch
+    #      at min_prob 0.99999.  After the timed runs each batch's records are
+    #      read back (the call fails on any device error word) and its
+    #      near-threshold FindTop lags counted. ----
     other = {}
     try:
         from satsuma2_gb300 import workloads as W
@@ -585,6 +588,7 @@ def run_ours(args):
             for _ in range(2):
                 b.run(sptr)
             torch.cuda.synchronize()
+            first = len(b.results())
             ts = []
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             for _ in range(reps):
@@ -594,19 +598,33 @@ def run_ours(args):
                 e1.record(stream)
                 torch.cuda.synchronize()
                 ts.append(e0.elapsed_time(e1))
+            recs = len(b.results())
+            near, _ = b.straddles()
             b.free()
-            return len(its) / (float(np.median(ts)) / 1000.0)
+            return {"pairs": len(its), "pairs_per_s": len(its) / (float(np.median(ts)) / 1000.0),
+                    "records": recs, "records_stable": recs == first, "near_threshold_lags": int(near.sum())}
 
         u = W.uneven_batch(20000, seed=SEED + rank)
         xu = sg.XCorr(fft_len=-1, target_total=float(sum(len(t) for t, _ in u)), device=local)
-        other["uneven_20000_pairs_fft_1024_8192_pairs_per_s"] = device_rate(xu, u)
+        other["uneven_20000_fft_1024_8192"] = device_rate(xu, u)
         xu.close()
         lg = W.large_batch(2000, seed=SEED + rank)
         xg = sg.XCorr(t_chunk=16384, q_chunk=16384, target_total=16384.0 * 2000, device=local)
-        other["large_2000_pairs_16384bp_fft_32768_pairs_per_s"] = device_rate(xg, lg)
+        other["large_2000_16384bp_fft_32768"] = device_rate(xg, lg)
         xg.close()
+        x5 = sg.XCorr(min_prob=0.99999, target_total=TARGET_TOTAL, device=local)
+        other["uniform_4096_min_prob_0.99999"] = device_rate(x5, items)
+        x5.close()
+        nb, _ = batch.straddles()
+        other["uniform_4096_min_prob_0.99_near_threshold_lags"] = int(nb.sum())
     except Exception as exc:   # informational only: never costs the main line
         other["error"] = str(exc)[:200]
+    parity_path = os.path.join(ROOT, "profiles", "parity_bench_configs.json")
+    parity = None
+    if os.path.exists(parity_path):
+        with open(parity_path) as f:
+            parity = {"source": "tests/test_gpu_bench_scale.py on a GB300 (profiles/parity_bench_configs.json): "
+                                "whole batches against the FP64 oracle", "configs": json.load(f)}
 
     peaks, peak_kind = measured_peaks()
     corr_ms = float(np.mean([s[0] for s in stage]))
@@ -661,6 +679,7 @@ def run_ours(args):
         "clocks": clocks,
         "cpu_baseline": cpu,
         "results_per_step": len(res_dev),
+        "parity": parity,
         "other_configs": other,
     }
     print(json.dumps(out_line))

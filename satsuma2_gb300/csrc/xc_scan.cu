@@ -432,10 +432,30 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
       s_hist[lane + 32] = tot0 + i1 - v1;
     }
     __syncthreads();
-    for (int k = tid; k < nc; k += NT_SCAN) {
-      const int b = 63 - (int)(((long long)diag_len(offs[k] - N, T, Q) * 64) / N);
-      const int p = atomicAdd(&s_hist[b], 1);
-      order[p] = (uint16_t)k;
+    // Stable placement, in offset-index order within a length bucket: when a
+    // strand is split over several CTAs each builds this order itself, and
+    // they must agree on it (an atomic placement order may differ between
+    // CTAs, so a diagonal could fall to two CTAs' rounds or to none).  Groups
+    // of NT_SCAN indices in order; within a group, warp by warp; within a
+    // warp, lanes with the same bucket ranked by lane.
+    for (int kb = 0; kb < nc; kb += NT_SCAN) {
+      const int k = kb + tid;
+      const bool have = k < nc;
+      const int b = have ? 63 - (int)(((long long)diag_len(offs[k] - N, T, Q) * 64) / N) : -1;
+      const unsigned peers = __match_any_sync(FULL, b);
+      const unsigned below = peers & ((1u << lane) - 1u);
+      const bool leader = (32 - __clz((int)peers)) - 1 == lane;   // highest lane of the peers
+#pragma unroll
+      for (int w = 0; w < NWARP; w++) {
+        int p = 0;
+        if (warp == w && have) {
+          p = s_hist[b] + __popc(below);
+          order[p] = (uint16_t)k;
+        }
+        __syncwarp();
+        if (warp == w && have && leader) s_hist[b] += __popc(peers);
+        __syncthreads();
+      }
     }
     if (tid == 0) s_next = 0;
     __syncthreads();

@@ -168,6 +168,38 @@ def test_batch_equals_single_pairs(O):
     x.close()
 
 
+def test_split_scan_small_batch_vs_oracle(O):
+    """Batches smaller than a wave split each strand's scan over several CTAs
+    that each order the strand's diagonals by length themselves.  With the
+    envelope off (FFT 2048) a pair keeps hundreds of offsets, many per length
+    bucket, so the CTAs must agree on that order exactly: every pair's records
+    equal the oracle's over the GPU's offsets, on three runs of the batch."""
+    import satsuma2_gb300 as sg
+    items = [it for it in W.uneven_batch(400, seed=23) if W.uneven_fft_len(len(it[0]), len(it[1])) == 2048][:40]
+    assert len(items) >= 20
+    TT = float(sum(len(t) for t, _ in items))
+    x = sg.XCorr(fft_len=-1, target_total=TT)
+    P = O.params(target_total=TT, fft_len=2048)
+    b = x.upload(items)
+    want = None
+    for run in range(3):
+        b.run()
+        res, counts = b.results(with_counts=True)
+        if want is None:
+            offs = b.offsets()
+            o = 0
+            for k, (t, q) in enumerate(items):
+                got = res[o:o + int(counts[k])]
+                o += int(counts[k])
+                ref, _ = O.align_pair(P, O.pair(t, q), offsets_in=offs[k])
+                assert parity.same_results(got, ref, target_total=TT), k
+            want = res
+        else:
+            assert parity.same_results(res, want, target_total=TT), run
+    b.free()
+    x.close()
+
+
 def test_uniform_batch_vs_oracle(O):
     import satsuma2_gb300 as sg
     items = W.uniform_batch(32, seed=5)
