@@ -400,6 +400,23 @@ def serve_run(x, items, n_threads=4, req_pairs=64, total=16384, rate=None, eager
     return len(reqs) * req_pairs / dt, p50, p99
 
 
+_GENOME = {}
+
+
+def genome_workload(seed=SEED):
+    """The genome workload (config 3): target and query as uint8 arrays, their
+    chunk tables (4096 bp; target overlap 1024) and the 24x24 blocks in
+    grid-search order; built once per process."""
+    if seed not in _GENOME:
+        from satsuma2_gb300 import workloads as W
+        t, q, (src, _) = W.serving_genomes(seed=seed, with_map=True)
+        tb, qb = np.frombuffer(t, np.uint8), np.frombuffer(q, np.uint8)
+        tc = np.array(W.chunk_starts(len(t), 4096, 1024), np.int64)
+        qc = np.array(W.chunk_starts(len(q), 4096, 0), np.int64)
+        _GENOME[seed] = (tb, qb, tc, qc, W.grid_search_blocks(src, len(tc), len(qc)))
+    return _GENOME[seed]
+
+
 def genome_serving(local, rates=(5000.0, 50000.0, 200000.0, 1000000.0), seconds=3.0, seed=SEED):
     """Serving on the genome workload: a 20 Mb target (GC 41%) and a query
     derived from it at 80% identity with 30 inversions, 20 segmental
@@ -411,21 +428,16 @@ def genome_serving(local, rates=(5000.0, 50000.0, 200000.0, 1000000.0), seconds=
     it is ready.  Per rate: requests, p50/p99 latency (submit to results in
     hand) and the pairs/s completed."""
     import satsuma2_gb300 as sg
-    from satsuma2_gb300 import workloads as W
-    t, q, (src, _) = W.serving_genomes(seed=seed, with_map=True)
-    tb, qb = np.frombuffer(t, np.uint8), np.frombuffer(q, np.uint8)
-    tc = np.array(W.chunk_starts(len(t), 4096, 1024), np.int64)
-    qc = np.array(W.chunk_starts(len(q), 4096, 0), np.int64)
-    blocks = W.grid_search_blocks(src, len(tc), len(qc))
-    x = sg.XCorr(target_total=float(len(t)), max_batch=4096, device=local)
+    tb, qb, tc, qc, blocks = genome_workload(seed)
+    x = sg.XCorr(target_total=float(len(tb)), max_batch=4096, device=local)
     warm = sg.block_pairs(tb, tc, qb, qc, *blocks[0])
     x.wait(x.submit(warm), timeout_ms=120000)
     out = {"workload": "20 Mb target, 80%% identity query (%d bp) with inversions, duplications, insertions; "
                        "%d target x %d query chunks; requests = 24x24 grid blocks in grid-search order "
-                       "(%d blocks, %d pairs), Poisson arrivals" % (len(q), len(tc), len(qc), len(blocks),
+                       "(%d blocks, %d pairs), Poisson arrivals" % (len(qb), len(tc), len(qc), len(blocks),
                                                                     sum((b[1] - b[0] + 1) * (b[3] - b[2] + 1)
                                                                         for b in blocks)),
-           "target_total": float(len(t)), "rates": {}}
+           "target_total": float(len(tb)), "rates": {}}
     k0 = 0
     for rate in rates:
         n_req = max(16, int(rate * seconds / 576))
@@ -612,6 +624,28 @@ def run_ours(args):
         xg = sg.XCorr(t_chunk=16384, q_chunk=16384, target_total=16384.0 * 2000, device=local)
         other["large_2000_16384bp_fft_32768"] = device_rate(xg, lg)
         xg.close()
+        # 24x24 grid blocks of the genome workload as one device batch (7
+        # blocks, 4032 pairs of 336 distinct chunks), correlation stage with
+        # the spectra path (each chunk transformed once) and without it
+        tb, qb, tc, qc, gblocks = genome_workload()
+        gb_items = np.concatenate([sg.block_pairs(tb, tc, qb, qc, *bl) for bl in gblocks[:7]])
+        for name, env in (("grid_blocks_4032_spectra_on", "1"), ("grid_blocks_4032_spectra_off", "0")):
+            os.environ["SATSUMA2_GB300_SPECTRA"] = env
+            xs = sg.XCorr(target_total=float(len(tb)), device=local)
+            os.environ.pop("SATSUMA2_GB300_SPECTRA")
+            rr = device_rate(xs, gb_items)
+            bs = xs.upload(gb_items)
+            for _ in range(2):
+                bs.run(sptr)
+            st_ms = []
+            for _ in range(5):
+                flush.zero_()
+                st_ms.append(bs.run_timed(sptr))
+            bs.free()
+            rr["stage_ms"] = {"corr_findtop": float(np.median([v[0] for v in st_ms])),
+                              "scan_filter": float(np.median([v[1] for v in st_ms]))}
+            other[name] = rr
+            xs.close()
         x5 = sg.XCorr(min_prob=0.99999, target_total=TARGET_TOTAL, device=local)
         other["uniform_4096_min_prob_0.99999"] = device_rate(x5, items)
         x5.close()

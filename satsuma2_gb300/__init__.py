@@ -245,10 +245,16 @@ class XCorr:
 
     # device-resident batches -------------------------------------------------
     def upload(self, items):
-        arr, keep = make_pairs(items)
+        """Packs and uploads chunk pairs (items as for align, or a PAIR_DTYPE
+        array) as a device-resident batch."""
+        if isinstance(items, np.ndarray) and items.dtype == PAIR_DTYPE:
+            arr, n = ctypes.c_void_p(items.ctypes.data), len(items)
+        else:
+            arr, keep = make_pairs(items)
+            n = len(arr)
         b = ctypes.c_void_p()
-        _check(self.lib.xc_batch_upload(self.ctx, arr, len(arr), ctypes.byref(b)), "xc_batch_upload")
-        return Batch(self, b, len(arr))
+        _check(self.lib.xc_batch_upload(self.ctx, arr, n, ctypes.byref(b)), "xc_batch_upload")
+        return Batch(self, b, n)
 
     # serving -------------------------------------------------------------------
     def submit(self, items):

@@ -938,6 +938,72 @@ size_t corr_pair2_smem_bytes() {
          + 2 * 256 * sizeof(uint32_t);                     // 2-bit codes of positions g + 256 r
 }
 
+// Per-bin step of the both-strands kernels at a general bin, from the packed
+// spectra A = Zt(m), B = Zt(N-m), C = Zq(m), D = Zq(N-m) of one channel pair:
+// f = conj(A) C + B conj(D) = 2 sum_c conj(T_c) Q_c and
+// r = A C - conj(B D) = 2i (T_c0 Q_c1 + T_c1 Q_c0).
+__device__ __forceinline__ void pair_bin(float2 A, float2 B, float2 C, float2 D, float2& f, float2& r) {
+  f = cadd(cmulc(C, A), cmulc(B, D));
+  const float2 ac = cmul(A, C), bd = cmul(B, D);
+  r = make_float2(ac.x - bd.x, ac.y + bd.y);
+}
+// Target-only bins, which the reference's loop leaves unmultiplied: Nyquist
+// (bin N: A = Zt(N/2) of the even-bin transform) 2 (T_c0 + T_c1), real; bin
+// N-1 (A = Zt(N/2-1), B = Zt(N/2) of the odd-bin transform)
+// 2 (T_c0 + T_c1) = (A + conj B) - i (A - conj B).
+__device__ __forceinline__ float2 pair_bin_nyquist(float2 A) { return make_float2(2.f * (A.x + A.y), 0.f); }
+__device__ __forceinline__ float2 pair_bin_nm1(float2 A, float2 B) {
+  return make_float2((A.x + B.x) + (A.y + B.y), (A.y - B.y) - (A.x - B.x));
+}
+
+// First forward pass of one sequence's packed signal z = s_c0 + i s_c1 at
+// FFT 8192 (N = 4096), its input built in registers: thread g takes
+// x_E[r] = z[g + 256 r] and x_O[r] = z[g + 256 r] W_L^(g + 256 r),
+// W_L^(256 r) = exp(-i pi r / 16), from the word of 2-bit codes of those
+// positions and the windows' channel values vw[16 r] (window (g >> 4) + 16 r:
+// c0 at weight 0, 1, then c1), then the radix-16 butterflies of span N with
+// their twiddles W_N^(g r), generated once for both transforms.
+__device__ __forceinline__ void first_pass_from_codes(uint32_t codes, int len, const float4* __restrict__ vw, int g,
+                                                      int c0, int c1, const float2* twLh, const float2* twLl,
+                                                      const float2* twNh, const float2* twNl,
+                                                      float2* __restrict__ bE, float2* __restrict__ bO) {
+  const float2 wg = tw2(twLh, twLl, g);
+  float2 xe[16], xo[16];
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    const float4 v = vw[16 * r];
+    const uint32_t code = (codes >> (2 * r)) & 3u;
+    float2 z = make_float2(0.f, 0.f);
+    if (g + 256 * r < len) z = make_float2(code == (uint32_t)c0 ? v.y : v.x, code == (uint32_t)c1 ? v.w : v.z);
+    xe[r] = z;
+    xo[r] = cmul(cmul(z, wg), make_float2(cos_pi16(r), -sin_pi16(r)));
+  }
+  DFT<16, -1>::run(xe);
+  DFT<16, -1>::run(xo);
+  const Tw16 tw = tw16(twNh, twNl, g);
+#pragma unroll
+  for (int r = 1; r < 16; r++) {
+    const float2 w = tw16_r(tw, r);
+    xe[r] = cmul(xe[r], w);
+    xo[r] = cmul(xo[r], w);
+  }
+  const int sb = swz(g);
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    bE[sb ^ swz(256 * r)] = xe[r];
+    bO[sb ^ swz(256 * r)] = xo[r];
+  }
+}
+
+// Per-window channel values float(entropy * (weight - mean)) (CrossCorr.cc:123)
+// of channels c0 and c1 at weights 0 and 1, from the sequence's means held
+// as (0 - mean, 1 - mean) in double and as three floats each (k = channel).
+__device__ __forceinline__ float4 window_values(float E, const Split3 (*wf)[8], const double (*wmo)[8], int k0,
+                                                int k1) {
+  return make_float4(mul_round_f32(E, wf[0][k0], wmo[0][k0]), mul_round_f32(E, wf[1][k0], wmo[1][k0]),
+                     mul_round_f32(E, wf[0][k1], wmo[0][k1]), mul_round_f32(E, wf[1][k1], wmo[1][k1]));
+}
+
 // Issues the cp.async copies of pair pidx's chunk bytes into st / sq: thread
 // t takes 16-byte piece t & 255 of the target (t < 256) or the query; bytes
 // past the chunk end are zero-filled (pool chunks are 16-byte aligned).
@@ -1119,52 +1185,11 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
       const bool first = stg == 0;
       // ---- 3a. per-window channel values float(entropy * (weight - mean))
       //      (CrossCorr.cc:123), weight 0 or 1; group G writes sequence G's ----
-      {
-        const float E = (G ? Eq : Et)[g];
-        const int k0 = G * 4 + c0, k1 = G * 4 + c1;
-        vv[G * NWIN + g] = make_float4(mul_round_f32(E, s_wf[0][k0], s_wmo[0][k0]),
-                                       mul_round_f32(E, s_wf[1][k0], s_wmo[1][k0]),
-                                       mul_round_f32(E, s_wf[0][k1], s_wmo[0][k1]),
-                                       mul_round_f32(E, s_wf[1][k1], s_wmo[1][k1]));
-      }
+      vv[G * NWIN + g] = window_values((G ? Eq : Et)[g], s_wf, s_wmo, G * 4 + c0, G * 4 + c1);
       gb();
-      // ---- 3b. first forward pass with its input built in registers:
-      //      x_E[r] = z[g + 256 r], x_O[r] = z[g + 256 r] W_L^(g + 256 r),
-      //      W_L^(256 r) = exp(-i pi r / 16); then the radix-16 butterflies
-      //      of span N and their twiddles W_N^(g r), shared by both ----
-      {
-        const uint32_t codes = cw[tid];
-        const int len = G ? Q : T;
-        const float4* vw = vv + G * NWIN + (g >> 4);   // window of position g + 256 r: (g >> 4) + 16 r
-        const float2 wg = tw2(twLh, twLl, g);
-        float2 xe[16], xo[16];
-#pragma unroll
-        for (int r = 0; r < 16; r++) {
-          const float4 v = vw[16 * r];
-          const uint32_t code = (codes >> (2 * r)) & 3u;
-          float2 z = make_float2(0.f, 0.f);
-          if (g + 256 * r < len) z = make_float2(code == (uint32_t)c0 ? v.y : v.x, code == (uint32_t)c1 ? v.w : v.z);
-          xe[r] = z;
-          xo[r] = cmul(cmul(z, wg), make_float2(cos_pi16(r), -sin_pi16(r)));
-        }
-        DFT<16, -1>::run(xe);
-        DFT<16, -1>::run(xo);
-        const Tw16 tw = tw16(twNh, twNl, g);
-#pragma unroll
-        for (int r = 1; r < 16; r++) {
-          const float2 w = tw16_r(tw, r);
-          xe[r] = cmul(xe[r], w);
-          xo[r] = cmul(xo[r], w);
-        }
-        float2* bE = G ? WE : ZE;
-        float2* bO = bE + N;
-        const int sb = swz(g);
-#pragma unroll
-        for (int r = 0; r < 16; r++) {
-          bE[sb ^ swz(256 * r)] = xe[r];
-          bO[sb ^ swz(256 * r)] = xo[r];
-        }
-      }
+      // ---- 3b. first forward pass with its input built in registers ----
+      first_pass_from_codes(cw[tid], G ? Q : T, vv + G * NWIN + (g >> 4), g, c0, c1, twLh, twLl, twNh, twNl,
+                            G ? WE : ZE, (G ? WE : ZE) + N);
       gb();
       // ---- 3c. the other two passes, both transforms of the group at once ----
       {
@@ -1190,13 +1215,12 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
           // partner N-m = (N - 256(it+1)) | (256 - g) for g >= 1
           const int pb = g ? (lb ^ lp<LOG2N>(N - 256 * (it + 1))) : lp<LOG2N>((N - 256 * it) & (N - 1));
           const float2 A = ZE[pa], B = ZE[pb], C = WE[pa], D = WE[pb];
-          if (m == N / 2) {   // Nyquist: 2 (T_c0 + T_c1), both real
-            const float2 f = make_float2(2.f * (A.x + A.y), 0.f);
+          if (m == N / 2) {
+            const float2 f = pair_bin_nyquist(A);
             aFE[m] = first ? f : cadd(aFE[m], f);
           } else {
-            const float2 f = cadd(cmulc(C, A), cmulc(B, D));
-            const float2 ac = cmul(A, C), bd = cmul(B, D);
-            const float2 r = make_float2(ac.x - bd.x, ac.y + bd.y);
+            float2 f, r;
+            pair_bin(A, B, C, D, f, r);
             aFE[m] = first ? f : cadd(aFE[m], f);
             aRE[m] = first ? r : cadd(aRE[m], r);
           }
@@ -1209,13 +1233,12 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
           const int pa = la ^ lp<LOG2N>(256 * it);
           const int pb = pa ^ lp<LOG2N>(N - 1);   // N-1-m = m ^ (N-1)
           const float2 A = ZO[pa], B = ZO[pb], C = WO[pa], D = WO[pb];
-          if (m == N / 2 - 1) {   // bin N-1: 2 (T_c0 + T_c1) = (A + conj B) - i (A - conj B)
-            const float2 f = make_float2((A.x + B.x) + (A.y + B.y), (A.y - B.y) - (A.x - B.x));
+          if (m == N / 2 - 1) {
+            const float2 f = pair_bin_nm1(A, B);
             aFO[m] = first ? f : cadd(aFO[m], f);
           } else {
-            const float2 f = cadd(cmulc(C, A), cmulc(B, D));
-            const float2 ac = cmul(A, C), bd = cmul(B, D);
-            const float2 r = make_float2(ac.x - bd.x, ac.y + bd.y);
+            float2 f, r;
+            pair_bin(A, B, C, D, f, r);
             aFO[m] = first ? f : cadd(aFO[m], f);
             aRO[m] = first ? r : cadd(aRO[m], r);
           }
@@ -1256,6 +1279,307 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
 }
 
 // ---------------------------------------------------------------------------
+// The spectra path at FFT 8192.  In a block of chunk pairs (a t_pair block of
+// 24 x 24 chunks is 576 pairs of 48 distinct chunks) every chunk takes part in
+// many pairs; the reference builds each chunk's signals once per block
+// (HomologyByXCorrSlave.cc:284-299).  spec_kernel transforms each distinct
+// chunk once -- both channel pairs, even-bin and odd-bin transforms, exactly
+// as corr_pair2_kernel transforms a sequence -- and stores the spectra in bin
+// order (128 KB per chunk, L2-resident for a batch of blocks);
+// corr_spec_kernel then forms each pair's sums from the two chunks' spectra,
+// in the same operations and order as corr_pair2_kernel, so its results are
+// the same bit for bit, and runs the inverses and FindTop.
+// ---------------------------------------------------------------------------
+size_t spec_bytes_per_chunk() { return (size_t)4 * 4096 * sizeof(float2); }
+
+static size_t spec_smem_bytes() {
+  constexpr size_t N = 4096, NH = N / 64;
+  return (4 * N + 2 * (NH + 64)) * sizeof(float2)   // 4 transforms, twiddles
+         + N                                        // chunk bytes
+         + 256 * sizeof(float)                      // entropy weight per window
+         + 2 * 256 * sizeof(float4)                 // window values per channel pair
+         + 256 * sizeof(uint32_t);                  // 2-bit codes of positions g + 256 r
+}
+
+__device__ __forceinline__ void spec_prefetch(const SpecParams& S, int u, uint8_t* sb, int tid) {
+  if (tid >= 256) return;   // 256 pieces of 16 bytes
+  const ChunkDesc c = S.chunks[u];
+  const int valid = min(max(c.len - 16 * tid, 0), 16);
+  const uint8_t* src = S.pool + c.off + (valid > 0 ? 16 * tid : 0);
+  const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sb + 16 * tid);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid) : "memory");
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+template <int LOG2L>
+__global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
+  constexpr int L = 1 << LOG2L;
+  constexpr int N = L >> 1;
+  constexpr int WIN = L / 512;
+  constexpr int NWIN = 256;
+  constexpr int NH = N / 64;
+  static_assert(N == 4096, "thread g of a group owns positions g + 256 r, r < 16");
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* buf = reinterpret_cast<float2*>(smem);   // [channel pair][even, odd][N]
+  float2* twNh = buf + 4 * N;
+  float2* twNl = twNh + NH;
+  float2* twLh = twNl + 64;
+  float2* twLl = twLh + NH;
+  uint8_t* sb = reinterpret_cast<uint8_t*>(twLl + 64);
+  float* Es = reinterpret_cast<float*>(sb + N);
+  float4* vv = reinterpret_cast<float4*>(Es + NWIN);     // [channel pair][window]
+  uint32_t* cw = reinterpret_cast<uint32_t*>(vv + 2 * NWIN);
+  __shared__ int s_cnt4[4];
+  __shared__ double s_wmo[2][8];
+  __shared__ Split3 s_wf[2][8];
+
+  const int tid = threadIdx.x;
+  const int G = tid >> 8;   // channel pair: 0 (A, T), 1 (C, G)
+  const int g = tid & 255;
+  const GroupBarrier gb{1 + G, 256};
+  for (int i = tid; i < NH; i += NT_PAIR2) {
+    twNh[i] = S.tab.twN_hi[i];
+    twLh[i] = S.tab.twL_hi[i];
+  }
+  if (tid < 64) {
+    twNl[tid] = S.tab.twN_lo[tid];
+    twLl[tid] = S.tab.twL_lo[tid];
+  }
+  if ((int)blockIdx.x < S.count) spec_prefetch(S, blockIdx.x, sb, tid);
+  for (int u = blockIdx.x; u < S.count; u += gridDim.x) {
+    const int next = u + (int)gridDim.x < S.count ? u + (int)gridDim.x : -1;
+    const int len = S.chunks[u].len;
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    if (tid < 4) s_cnt4[tid] = 0;
+    __syncthreads();
+    // byte checks of the 16-byte pieces (zero past the end)
+    int high = 0, nonacgt = 0;
+    if (tid < 256) {
+      const int valid = len - 16 * tid;
+      const uint4 v = *reinterpret_cast<const uint4*>(sb + 16 * tid);
+      const uint32_t x[4] = {v.x, v.y, v.z, v.w};
+      auto nz = [](uint32_t y) { return (((y & 0x7f7f7f7fu) + 0x7f7f7f7fu) | y) & 0x80808080u; };
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int vk = min(max(valid - 4 * k, 0), 4);
+        const uint32_t m = vk >= 4 ? 0xffffffffu : (1u << (8 * vk)) - 1u;
+        high |= (x[k] & m & 0x80808080u) != 0u;
+        const uint32_t bad = nz(x[k] ^ 0x41414141u) & nz(x[k] ^ 0x43434343u) & nz(x[k] ^ 0x47474747u) &
+                             nz(x[k] ^ 0x54545454u);
+        nonacgt |= (bad & m & 0x80808080u) != 0u;
+      }
+    }
+    const int any_high = __syncthreads_or(high);
+    const int generic = __syncthreads_or(nonacgt);
+    if (any_high || generic) {
+      if (tid == 0) S.chunk_flags[u] = (any_high ? CF_HIGH : 0u) | CF_GENERIC;
+      if (next >= 0) spec_prefetch(S, next, sb, tid);
+      continue;
+    }
+    // entropy weights (group 0), 2-bit codes (group 1), base counts (all)
+    if (G == 0) {
+      float E = 0.f;
+      if (len < 1024) {
+        E = 1.f;
+      } else if (g * WIN + WIN <= len) {
+        const int i0 = g * WIN;
+        uint32_t cnt = 0;
+        for (int j = 0; j < WIN; j++) cnt += 1u << (8 * code_of(sb[i0 + j]));
+        const int a = cnt & 255u, c = (cnt >> 8) & 255u, gg = (cnt >> 16) & 255u;
+        E = __ldg(&S.tab.ent_acgt[(a * (WIN + 1) + c) * (WIN + 1) + gg]);
+      } else if (g * WIN < len) {
+        const int i0 = g * WIN;
+        const int k = len - i0;
+        int a4 = 0, c4 = 0, g4 = 0, t4 = 0;
+        for (int j = 0; j < k; j++) {
+          const uchar4 q = c_w4q[sb[i0 + j]];
+          a4 += q.x; c4 += q.y; g4 += q.z; t4 += q.w;
+        }
+        const double* et = S.tab.ent + k * (4 * WIN + 1);
+        const double sv =
+            __dadd_rn(__dadd_rn(__dadd_rn(__ldg(et + a4), __ldg(et + c4)), __ldg(et + g4)), __ldg(et + t4));
+        E = __double2float_rn(-sv);
+        if (E < 0.f) E = 0.f;
+      }
+      Es[g] = E;
+    } else {
+      uint32_t w = 0;
+#pragma unroll
+      for (int r = 0; r < 16; r++) w |= code_of(sb[g + 256 * r]) << (2 * r);
+      cw[g] = w;
+    }
+    {
+      uint32_t ct = 0;
+      for (int i = tid; i < N; i += NT_PAIR2)
+        if (i < len) ct += 1u << (8 * code_of(sb[i]));
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int v = __reduce_add_sync(0xffffffffu, 4 * (int)((ct >> (8 * k)) & 255u));
+        if ((tid & 31) == 0 && v) atomicAdd(&s_cnt4[k], v);
+      }
+    }
+    __syncthreads();   // the chunk bytes are no longer read
+    if (next >= 0) spec_prefetch(S, next, sb, tid);
+    if (tid < 4) {
+      const double off = len > 0 ? __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len) : 0.0;
+      s_wmo[0][tid] = __dsub_rn(0.0, off);
+      s_wmo[1][tid] = __dsub_rn(1.0, off);
+      s_wf[0][tid] = split3(s_wmo[0][tid]);
+      s_wf[1][tid] = split3(s_wmo[1][tid]);
+    }
+    __syncthreads();
+    // group G transforms channel pair G: (A, T) or (C, G)
+    const int c0 = G ? 1 : 0, c1 = G ? 2 : 3;
+    float2* bE = buf + 2 * G * N;
+    float2* bO = bE + N;
+    vv[G * NWIN + g] = window_values(Es[g], s_wf, s_wmo, c0, c1);
+    gb();
+    first_pass_from_codes(cw[g], len, vv + G * NWIN + (g >> 4), g, c0, c1, twLh, twLl, twNh, twNl, bE, bO);
+    gb();
+    fft_pass16_x2<N, N / 16>(bE, bO, twNh, twNl, g);
+    gb();
+    fft_pass16_x2<N, N / 256>(bE, bO, twNh, twNl, g);
+    gb();
+    // out in bin order: bin m of the even-bin transform at [2G][m], odd at [2G + 1][m]
+    float2* out = S.spec + ((size_t)u * 4 + 2 * G) * N;
+    const int la = lp<LOG2L - 1>(g);
+#pragma unroll 4
+    for (int it = 0; it < N / 256; it++) {
+      const int pa = la ^ lp<LOG2L - 1>(256 * it);
+      out[g + 256 * it] = bE[pa];
+      out[N + g + 256 * it] = bO[pa];
+    }
+    if (tid == 0) S.chunk_flags[u] = 0u;
+    __syncthreads();
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+static size_t corr_spec_smem_bytes() {
+  constexpr size_t N = 4096, NH = N / 64;
+  return (2 * N + 2 * N + 16 + 2 * (NH + 64)) * sizeof(float2);   // 2 inverses, F and R sums, twiddles
+}
+
+template <int LOG2L>
+__global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams P) {
+  constexpr int L = 1 << LOG2L;
+  constexpr int N = L >> 1;
+  constexpr int LOG2N = LOG2L - 1;
+  constexpr int WIN = L / 512;
+  constexpr int NH = N / 64;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* ZE = reinterpret_cast<float2*>(smem);   // forward-strand inverse
+  float2* WE = ZE + N;                            // reverse-strand inverse
+  float2* aFE = WE + N;
+  float2* aFO = aFE + (N / 2 + 8);
+  float2* aRE = aFO + N / 2;
+  float2* aRO = aRE + (N / 2 + 8);
+  float2* twNh = aRO + N / 2;
+  float2* twNl = twNh + NH;
+  float2* twLh = twNl + 64;
+  float2* twLl = twLh + NH;
+  __shared__ int s_warp[2][2 * 256 / 32];
+
+  const int tid = threadIdx.x;
+  const int G = tid >> 8;   // product: 0 even bins, 1 odd bins; then 0 forward strand, 1 reverse
+  const int g = tid & 255;
+  const GroupBarrier gb{1 + G, 256};
+  for (int i = tid; i < NH; i += NT_PAIR2) {
+    twNh[i] = P.tab.twN_hi[i];
+    twLh[i] = P.tab.twL_hi[i];
+  }
+  if (tid < 64) {
+    twNl[tid] = P.tab.twN_lo[tid];
+    twLl[tid] = P.tab.twL_lo[tid];
+  }
+  __syncthreads();
+  for (int p = blockIdx.x; p < P.count; p += gridDim.x) {
+    const int pidx = P.first + p;
+    const int tc = P.pair_chunk[2 * pidx], qc = P.pair_chunk[2 * pidx + 1];
+    const int Q = P.pairs[pidx].qlen;
+    const uint32_t fl = P.chunk_flags[tc] | P.chunk_flags[qc];
+    if (fl || (Q >= 1024 && Q % WIN != 0) || P.dbg_sig) {   // the same for every thread
+      if (tid == 0) {
+        if (fl & CF_HIGH) {
+          P.off_cnt[pidx * 2] = 0;
+          P.off_cnt[pidx * 2 + 1] = 0;
+          P.pair_flags[pidx] = PF_INVALID;
+        } else {
+          P.fb_list[atomicAdd(P.fb_cnt, 1)] = pidx;
+        }
+      }
+      continue;
+    }
+    if (tid == 0) P.pair_flags[pidx] = P.pairs[pidx].flags & PF_FAST;
+    // ---- per-bin step from the stored spectra, both channel pairs summed in
+    //      the order corr_pair2_kernel accumulates them ----
+    const float2* __restrict__ Ts = P.spec + (size_t)tc * 4 * N;
+    const float2* __restrict__ Qs = P.spec + (size_t)qc * 4 * N;
+    if (G == 0) {
+#pragma unroll 3
+      for (int it = 0; it <= N / 512; it++) {
+        const int m = g + 256 * it;
+        if (m > N / 2) break;
+        const int mb = (N - m) & (N - 1);
+        const float2 A0 = __ldg(Ts + m), B0 = __ldg(Ts + mb), C0 = __ldg(Qs + m), D0 = __ldg(Qs + mb);
+        const float2 A1 = __ldg(Ts + 2 * N + m), B1 = __ldg(Ts + 2 * N + mb);
+        const float2 C1 = __ldg(Qs + 2 * N + m), D1 = __ldg(Qs + 2 * N + mb);
+        if (m == N / 2) {
+          aFE[m] = cadd(pair_bin_nyquist(A0), pair_bin_nyquist(A1));
+        } else {
+          float2 f0, r0, f1, r1;
+          pair_bin(A0, B0, C0, D0, f0, r0);
+          pair_bin(A1, B1, C1, D1, f1, r1);
+          aFE[m] = cadd(f0, f1);
+          aRE[m] = cadd(r0, r1);
+        }
+      }
+    } else {
+#pragma unroll 4
+      for (int it = 0; it < N / 512; it++) {
+        const int m = g + 256 * it;
+        const int mb = N - 1 - m;
+        const float2 A0 = __ldg(Ts + N + m), B0 = __ldg(Ts + N + mb), C0 = __ldg(Qs + N + m), D0 = __ldg(Qs + N + mb);
+        const float2 A1 = __ldg(Ts + 3 * N + m), B1 = __ldg(Ts + 3 * N + mb);
+        const float2 C1 = __ldg(Qs + 3 * N + m), D1 = __ldg(Qs + 3 * N + mb);
+        if (m == N / 2 - 1) {
+          aFO[m] = cadd(pair_bin_nm1(A0, B0), pair_bin_nm1(A1, B1));
+        } else {
+          float2 f0, r0, f1, r1;
+          pair_bin(A0, B0, C0, D0, f0, r0);
+          pair_bin(A1, B1, C1, D1, f1, r1);
+          aFO[m] = cadd(f0, f1);
+          aRO[m] = cadd(r0, r1);
+        }
+      }
+    }
+    __syncthreads();
+    // ---- inverses and FindTop, as corr_pair2_kernel ----
+    float2* buf = G ? WE : ZE;
+    if (G == 0) {
+      hermitian_pack<LOG2L, 256>(ZE, [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; }, twLh,
+                                 twLl, g, 1.0f);
+    } else {
+      hermitian_pack<LOG2L, 256>(WE,
+                                 [&](int k) -> float2 {
+                                   if (k >= N - 1) return (k & 1) ? aFO[k >> 1] : aFE[k >> 1];
+                                   const float2 r = (k & 1) ? aRO[k >> 1] : aRE[k >> 1];
+                                   const int j = ((Q - 1) * k) & (L - 1);
+                                   float2 w = tw2(twLh, twLl, j & (N - 1));
+                                   if (j & N) w = make_float2(-w.x, -w.y);
+                                   return cmul(w, make_float2(r.y, r.x));
+                                 },
+                                 twLh, twLl, g, 1.0f);
+    }
+    gb();
+    fft_inverse<LOG2N, Plan<LOG2N>, Plan<LOG2N>::n - 1, GroupBarrier>(buf, twNh, twNl, g, 256, gb);
+    find_top<LOG2L, 256, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, G, buf, g, s_warp[G], gb,
+                                       1.0f / (float)(4 * N));
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
 cudaError_t prepare_scan_kernels();
@@ -1273,6 +1597,12 @@ cudaError_t prepare_kernels() {
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(corr_pair2_kernel<PAIR_LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)corr_pair2_smem_bytes());
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(spec_kernel<PAIR_LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)spec_smem_bytes());
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(corr_spec_kernel<PAIR_LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)corr_spec_smem_bytes());
   if (e != cudaSuccess) return e;
   if ((e = set_corr_attrs<10>()) != cudaSuccess) return e;
   if ((e = set_corr_attrs<11>()) != cudaSuccess) return e;
@@ -1313,6 +1643,25 @@ cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t
     case 15: corr_kernel<15><<<grid, NT_CORR, sm, s>>>(p); break;
     default: return cudaErrorInvalidValue;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_corr_spec(const SpecParams& sp, const CorrParams& p, int npairs, cudaStream_t s) {
+  if (npairs <= 0) return cudaSuccess;
+  static const int sms = [] {
+    int dev = 0, n = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n;
+  }();
+  if (!p.fb_list || !p.pair_chunk) return cudaErrorInvalidValue;
+  if (sp.count > 0) spec_kernel<PAIR_LOG2L><<<std::min(sp.count, sms), NT_PAIR2, spec_smem_bytes(), s>>>(sp);
+  CorrParams q = p;
+  q.count = npairs;
+  corr_spec_kernel<PAIR_LOG2L><<<std::min(npairs, sms), NT_PAIR2, corr_spec_smem_bytes(), s>>>(q);
+  // the pairs handed back: one wave of per-strand CTAs striding over the list
+  CorrParams h = p;
+  h.pair_chunk = nullptr;
+  corr_kernel<PAIR_LOG2L><<<dim3(std::min(npairs, sms), 2), NT_CORR, corr_smem_bytes(PAIR_LOG2L), s>>>(h);
   return cudaGetLastError();
 }
 

@@ -95,6 +95,32 @@ struct CorrParams {
   int* strad_list;          //   and the first STRAD_CAP of them, [pair*2 + strand][STRAD_CAP]
   int count;                // pairs of this launch (set by launch_corr)
   int pair_form;            // with fb_list: 2 = persistent 512-thread kernel, 1 = 1024-thread form
+  // spectra path (FFT 8192 batches whose pairs share chunks): the pair kernel
+  // reads both chunks' spectra instead of transforming them
+  const int* pair_chunk;    // [pair][2]: target and query chunk indices
+  const float2* spec;       // [chunk][4][N] spectra, bin order (see SpecParams)
+  const uint32_t* chunk_flags;
+};
+
+// Chunk flags of the spectra path.
+enum : uint32_t {
+  CF_HIGH = 1u,      // a byte >= 128: the pairs with this chunk are rejected
+  CF_GENERIC = 2u,   // a byte other than A/C/G/T: its pairs go to the per-strand kernel
+};
+
+struct ChunkDesc {
+  uint32_t off;             // byte offset of the chunk in the sequence pool
+  int32_t len;
+};
+
+// spec_kernel: the transforms of each distinct chunk of a batch, once.
+struct SpecParams {
+  const ChunkDesc* chunks;
+  int count;
+  const uint8_t* pool;
+  LTables tab;
+  float2* spec;             // [chunk][4][N]: channels (A,T) even-bin, odd-bin transform, then (C,G); bin order
+  uint32_t* chunk_flags;    // [chunk]: CF_* (0 = spectra written)
 };
 
 // Global channel-sum scratch of one pair strand for FFT lengths beyond one
@@ -133,6 +159,10 @@ struct ScanParams {
 
 // Launchers (xc_corr.cu, xc_scan.cu).
 cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t s);
+// FFT 8192 with shared chunks: spec_kernel over the distinct chunks, then the
+// pair kernel from their spectra, then corr_kernel over the pairs handed back.
+cudaError_t launch_corr_spec(const SpecParams& sp, const CorrParams& p, int npairs, cudaStream_t s);
+size_t spec_bytes_per_chunk();
 cudaError_t launch_scan(int log2L, const ScanParams& p, int npairs, cudaStream_t s);
 cudaError_t launch_finalize(const int* res_cnt, const DevResult* res, int slots, int nslots,
                             int* dense_base, DevResult* dense, int* scan_tmp, cudaStream_t s);

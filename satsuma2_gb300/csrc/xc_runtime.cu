@@ -15,6 +15,7 @@
 #include <functional>
 #include <mutex>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 static_assert(sizeof(xc_result) == 72, "xc_result must match t_result (72 bytes)");
@@ -144,6 +145,9 @@ static int build_tables(Ctx* c) {
       const char* env = getenv("SATSUMA2_GB300_PAIR_KERNEL");
       c->pair_kernel = sym && !(env && env[0] == '0');
       c->pair_form = (env && env[0] == '1') ? 1 : 2;
+      // SATSUMA2_GB300_SPECTRA=0: no spectra path (every pair transforms its chunks)
+      const char* es = getenv("SATSUMA2_GB300_SPECTRA");
+      c->spec_reuse = !(es && es[0] == '0');
     }
     DevTables& t = c->tab[lg];
     XC_CHECK(cudaMalloc(&t.tw, tw.size() * sizeof(float2)));
@@ -354,6 +358,7 @@ Batch::~Batch() {
   cudaFree(d_res); cudaFree(d_rescnt); cudaFree(d_ovf); cudaFree(d_misc); cudaFree(d_base);
   cudaFree(d_dense); cudaFree(d_dbg); cudaFree(d_dbg_sig); cudaFree(d_dbg_xc); cudaFree(d_acc); cudaFree(d_fb);
   cudaFree(d_stradcnt); cudaFree(d_strad);
+  cudaFree(d_chunks); cudaFree(d_pairchunk); cudaFree(d_spec); cudaFree(d_chunkflags);
   cudaFreeHost(h_pool); cudaFreeHost(h_desc); cudaFreeHost(h_base); cudaFreeHost(h_dense);
   cudaFreeHost(h_misc); cudaFreeHost(h_ovf); cudaFreeHost(h_flags);
 }
@@ -387,17 +392,40 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
     start += counts[lg];
   }
   for (size_t i = 0; i < n; i++) b->order[fill[b->log2L[i]]++] = (int)i;
-  // pool and offset-list layout
+  // pool and offset-list layout; a chunk that several pairs pass by the same
+  // pointer and length (a block's target and query chunks) is stored once
   std::vector<uint64_t> toff(n), qoff(n);
   uint64_t pool = 0, offl = 0;
   b->desc_host.resize(n);
+  struct Src {
+    const char* p;
+    int len;
+    uint64_t off;
+  };
+  std::vector<Src> uniq;
+  uniq.reserve(2 * n);
+  struct KeyHash {
+    size_t operator()(const std::pair<const char*, int>& k) const {
+      return std::hash<const void*>()(k.first) * 31u + (size_t)k.second;
+    }
+  };
+  std::unordered_map<std::pair<const char*, int>, uint64_t, KeyHash> seen;
+  seen.reserve(2 * n);
+  auto place = [&](const char* ptr, int len) -> uint64_t {
+    if (len == 0) return pool;
+    auto it = seen.find({ptr, len});
+    if (it != seen.end()) return it->second;
+    const uint64_t o = pool;
+    seen.emplace(std::make_pair(ptr, len), o);
+    uniq.push_back({ptr, len, o});
+    pool += ((uint64_t)len + 15) & ~15ull;
+    return o;
+  };
   for (size_t d = 0; d < n; d++) {
     const xc_pair& p = pairs[b->order[d]];
     const int lg = b->log2L[b->order[d]];
-    toff[d] = pool;
-    pool += ((uint64_t)p.tlen + 15) & ~15ull;
-    qoff[d] = pool;
-    pool += ((uint64_t)p.qlen + 15) & ~15ull;
+    toff[d] = place(p.tseq, p.tlen);
+    qoff[d] = place(p.qseq, p.qlen);
     PairDesc& D = b->desc_host[d];
     D.t_off = (uint32_t)toff[d];
     D.q_off = (uint32_t)qoff[d];
@@ -435,20 +463,55 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   if ((r = host_grow(b->h_base, b->cap_h_base, nslots + 1)) != XC_OK) return r;
   if ((r = host_grow(b->h_misc, b->cap_h_misc, 4)) != XC_OK) return r;
   b->pool_bytes = pool;
-  // gather sequences into pinned staging (threads for large batches)
+  b->unique_bytes = pool;
+  // gather the distinct chunks into pinned staging (threads for large batches)
   uint8_t* hp = b->h_pool;
-  const std::vector<int>& ord = b->order;
-  parallel_for(n, 64, [&](size_t lo, size_t hi) {   // chunks of >= 64 pairs (0.5 MB)
-    for (size_t d = lo; d < hi; d++) {
-      const xc_pair& p = pairs[ord[d]];
-      if (p.tlen) memcpy(hp + toff[d], p.tseq, (size_t)p.tlen);
-      if (p.qlen) memcpy(hp + qoff[d], p.qseq, (size_t)p.qlen);
-    }
+  parallel_for(uniq.size(), 128, [&](size_t lo, size_t hi) {   // chunks of >= 128 chunks (0.5 MB)
+    for (size_t u = lo; u < hi; u++) memcpy(hp + uniq[u].off, uniq[u].p, (size_t)uniq[u].len);
   });
   memcpy(b->h_desc, b->desc_host.data(), n * sizeof(PairDesc));
   XC_CHECK(cudaMemcpyAsync(b->d_pool, b->h_pool, pool, cudaMemcpyHostToDevice, stream));
   XC_CHECK(cudaMemcpyAsync(b->d_desc, b->h_desc, n * sizeof(PairDesc), cudaMemcpyHostToDevice, stream));
   b->h2d_bytes = pool + n * sizeof(PairDesc);
+  // spectra path for the FFT-8192 bucket when its pairs share chunks
+  b->spec = false;
+  b->spec_chunks = 0;
+  for (const Bucket& bk : b->buckets) {
+    if (bk.log2L != PAIR_LOG2L || !c->pair_kernel || !c->spec_reuse) continue;
+    std::unordered_map<uint64_t, int> cidx;   // pool offset -> chunk index
+    b->chunk_host.clear();
+    b->pair_chunk_host.assign(2 * (size_t)n, 0);
+    for (int d = bk.first; d < bk.first + bk.count; d++) {
+      const PairDesc& D = b->desc_host[d];
+      const uint32_t off[2] = {D.t_off, D.q_off};
+      const int len[2] = {D.tlen, D.qlen};
+      for (int k = 0; k < 2; k++) {
+        auto it = cidx.find(((uint64_t)off[k] << 20) | (uint64_t)len[k]);
+        int ci;
+        if (it != cidx.end()) {
+          ci = it->second;
+        } else {
+          ci = (int)b->chunk_host.size();
+          cidx.emplace(((uint64_t)off[k] << 20) | (uint64_t)len[k], ci);
+          b->chunk_host.push_back({off[k], len[k]});
+        }
+        b->pair_chunk_host[2 * (size_t)d + k] = ci;
+      }
+    }
+    const size_t U = b->chunk_host.size();
+    if ((double)(2 * bk.count) < SPEC_MIN_REUSE * (double)U) continue;
+    if ((r = dev_grow(b->d_chunks, b->cap_chunks, U)) != XC_OK) return r;
+    if ((r = dev_grow(b->d_pairchunk, b->cap_pairchunk, 2 * (size_t)n)) != XC_OK) return r;
+    if ((r = dev_grow(b->d_spec, b->cap_spec, U * (spec_bytes_per_chunk() / sizeof(float2)))) != XC_OK) return r;
+    if ((r = dev_grow(b->d_chunkflags, b->cap_chunkflags, U)) != XC_OK) return r;
+    XC_CHECK(cudaMemcpyAsync(b->d_chunks, b->chunk_host.data(), U * sizeof(ChunkDesc), cudaMemcpyHostToDevice,
+                             stream));
+    XC_CHECK(cudaMemcpyAsync(b->d_pairchunk, b->pair_chunk_host.data(), 2 * (size_t)n * sizeof(int),
+                             cudaMemcpyHostToDevice, stream));
+    b->h2d_bytes += U * sizeof(ChunkDesc) + 2 * (size_t)n * sizeof(int);
+    b->spec = true;
+    b->spec_chunks = (int)U;
+  }
   b->graph_valid = false;
   b->graph_timed_valid = false;
   return XC_OK;
@@ -512,6 +575,20 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     }
     cp.strad_cnt = b->d_stradcnt;
     cp.strad_list = b->d_strad;
+    if (bk.log2L == PAIR_LOG2L && b->spec) {
+      SpecParams spp{};
+      spp.chunks = b->d_chunks;
+      spp.count = b->spec_chunks;
+      spp.pool = b->d_pool;
+      spp.tab = cp.tab;
+      spp.spec = b->d_spec;
+      spp.chunk_flags = b->d_chunkflags;
+      cp.pair_chunk = b->d_pairchunk;
+      cp.spec = b->d_spec;
+      cp.chunk_flags = b->d_chunkflags;
+      XC_CHECK(launch_corr_spec(spp, cp, bk.count, s));
+      continue;
+    }
     XC_CHECK(launch_corr(bk.log2L, cp, bk.count, s));
   }
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[1], s, cudaEventRecordExternal));
@@ -552,7 +629,8 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
 
 int batch_launch_count(const Ctx* c, const Batch* b) {
   int n = 2 * (int)b->buckets.size() + 2;
-  for (const Bucket& bk : b->buckets) n += bk.log2L == PAIR_LOG2L && c->pair_kernel;   // pair kernel + hand-back
+  for (const Bucket& bk : b->buckets)
+    if (bk.log2L == PAIR_LOG2L && c->pair_kernel) n += b->spec ? 2 : 1;   // (spectra,) pair kernel, hand-back
   return n;
 }
 

@@ -45,6 +45,17 @@ struct Batch {
   int* d_fb = nullptr;            size_t cap_fb = 0;     // those pairs' indices
   int* d_stradcnt = nullptr;      size_t cap_stradcnt = 0;   // near-threshold lags per pair strand
   int* d_strad = nullptr;         size_t cap_strad = 0;      // the first STRAD_CAP of them
+  // spectra path of the FFT-8192 bucket (its pairs share chunks): distinct
+  // chunks, each pair's two chunk indices, the chunks' spectra and flags
+  bool spec = false;
+  int spec_chunks = 0;
+  std::vector<ChunkDesc> chunk_host;
+  std::vector<int> pair_chunk_host;
+  ChunkDesc* d_chunks = nullptr;  size_t cap_chunks = 0;
+  int* d_pairchunk = nullptr;     size_t cap_pairchunk = 0;
+  float2* d_spec = nullptr;       size_t cap_spec = 0;
+  uint32_t* d_chunkflags = nullptr; size_t cap_chunkflags = 0;
+  uint64_t unique_bytes = 0;      // sequence bytes after de-duplication
   int* d_base = nullptr;          size_t cap_base = 0;
   DevResult* d_dense = nullptr;   size_t cap_dense = 0;
   float2* d_acc = nullptr;        size_t cap_acc = 0;     // channel sums of FFT lengths beyond one SM
@@ -103,10 +114,17 @@ struct Ctx {
   int sms = 152;               // multiprocessors of the device (sub-batch sizing)
   bool pair_kernel = false;    // both-strands correlation kernel usable (entropy table complement-symmetric)
   int pair_form = 2;           // its form: 2 persistent 512-thread kernel, 1 the 1024-thread one
+  bool spec_reuse = true;      // FFT-8192 batches whose pairs share chunks transform each chunk once
   unsigned char* noalloc_base = nullptr;   // xc_align_pair_noalloc's static array on this device (set at first use)
 };
 
 
+
+// Pairs per distinct chunk (2 x pairs / chunks) from which an FFT-8192 bucket
+// takes the spectra path: each chunk transformed once, 128 KB of spectra per
+// chunk written and read back from L2 per pair, where the both-strands kernel
+// transforms both chunks of every pair in shared memory.
+constexpr double SPEC_MIN_REUSE = 3.0;
 
 // batch_collect's status when the batch's device overflow pool filled during
 // the run (records were dropped on the device).  Internal only: every caller

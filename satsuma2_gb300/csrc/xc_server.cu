@@ -331,9 +331,18 @@ int xc_submit(xc_ctx* c, const xc_pair* pairs, size_t n, uint64_t* ticket) {
     if (r != XC_OK) return r;
   }
   Server* S = c->server;
-  // copy the caller's sequences (valid only during this call)
+  // copy the caller's sequences (valid only during this call); a chunk the
+  // request passes several times by the same pointer and length (a block's
+  // chunks) is copied once, so its pairs share it downstream
   Request* q = new Request();
   size_t bytes = 0;
+  struct KeyHash {
+    size_t operator()(const std::pair<const char*, int>& k) const {
+      return std::hash<const void*>()(k.first) * 31u + (size_t)k.second;
+    }
+  };
+  std::unordered_map<std::pair<const char*, int>, size_t, KeyHash> seen;
+  std::vector<std::pair<size_t, size_t>> where(n);   // byte offsets of each pair's target and query copy
   for (size_t i = 0; i < n; i++) {
     if (pairs[i].tlen < 0 || pairs[i].qlen < 0) {
       delete q;
@@ -348,20 +357,25 @@ int xc_submit(xc_ctx* c, const xc_pair* pairs, size_t n, uint64_t* ticket) {
       delete q;
       return XC_ERR_INPUT;
     }
-    bytes += (size_t)pairs[i].tlen + pairs[i].qlen;
+    auto at = [&](const char* ptr, int len) -> size_t {
+      auto it = seen.find({ptr, len});
+      if (it != seen.end()) return it->second;
+      seen.emplace(std::make_pair(ptr, len), bytes);
+      bytes += (size_t)len;
+      return bytes - (size_t)len;
+    };
+    where[i].first = at(pairs[i].tseq, pairs[i].tlen);
+    where[i].second = at(pairs[i].qseq, pairs[i].qlen);
     q->footprint += pair_footprint(c, pairs[i], S->slots[0].b->slots);
   }
   q->bytes.resize(bytes);
+  for (const auto& kv : seen)
+    if (kv.first.second) memcpy(&q->bytes[kv.second], kv.first.first, (size_t)kv.first.second);
   q->pairs.assign(pairs, pairs + n);
-  size_t o = 0;
   for (size_t i = 0; i < n; i++) {
     xc_pair& p = q->pairs[i];
-    if (p.tlen) memcpy(&q->bytes[o], p.tseq, p.tlen);
-    p.tseq = q->bytes.data() + o;
-    o += p.tlen;
-    if (p.qlen) memcpy(&q->bytes[o], p.qseq, p.qlen);
-    p.qseq = q->bytes.data() + o;
-    o += p.qlen;
+    p.tseq = q->bytes.data() + where[i].first;
+    p.qseq = q->bytes.data() + where[i].second;
   }
   q->results.reserve(n * 4);
   std::unique_lock<std::mutex> lk(S->mu);

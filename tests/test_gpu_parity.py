@@ -175,7 +175,7 @@ def test_split_scan_small_batch_vs_oracle(O):
     bucket, so the CTAs must agree on that order exactly: every pair's records
     equal the oracle's over the GPU's offsets, on three runs of the batch."""
     import satsuma2_gb300 as sg
-    items = [it for it in W.uneven_batch(400, seed=23) if W.uneven_fft_len(len(it[0]), len(it[1])) == 2048][:40]
+    items = [it for it in W.uneven_batch(1600, seed=23) if W.uneven_fft_len(len(it[0]), len(it[1])) == 2048][:40]
     assert len(items) >= 20
     TT = float(sum(len(t) for t, _ in items))
     x = sg.XCorr(fft_len=-1, target_total=TT)
@@ -296,6 +296,59 @@ def _block_items(tchunks, qchunks, tf, qf, n=24):
     return [dict(t=tchunks[ti], q=qchunks[qi], t_chunk_start=3072 * ti, target_id=0,
                  q_chunk_start=4096 * qi, query_id=0, query_size=4096 * len(qchunks))
             for qi in range(qf, qf + n) for ti in range(tf, tf + n)]
+
+
+def test_spectra_path_equals_pair_kernel(O, monkeypatch):
+    """Grid blocks of chunk pairs share their chunks: the spectra path
+    (spec_kernel once per distinct chunk, then the pair kernel from stored
+    spectra) forms each pair's sums with the same operations as the
+    both-strands kernel, so its offsets and records are identical to it,
+    and to the oracle over those offsets.  The chunks include an N run
+    (handed back to the per-strand kernel), an empty chunk and a short last
+    query chunk whose length is not a multiple of the entropy window."""
+    import satsuma2_gb300 as sg
+    rng = np.random.default_rng(93)
+    t = W.random_bases(rng, 3072 * 12 + 1024)
+    q = W.mutate(rng, t[2000:3072 * 12], 0.85)
+    q = np.concatenate([q, W.random_bases(rng, 4096 * 9 + 2001 - len(q))]) if len(q) < 4096 * 9 + 2001 else q[:4096 * 9 + 2001]
+    q[4096 * 2 + 100:4096 * 2 + 300] = ord("N")
+    tc = np.array(W.chunk_starts(len(t), 4096, 1024), np.int64)
+    qc = np.array(W.chunk_starts(len(q), 4096, 0), np.int64)
+    qc = np.concatenate([qc, [[len(q), len(q)]]])          # an empty chunk
+    blocks = [sg.block_pairs(t, tc, q, qc, 0, len(tc) - 1, 0, len(qc) - 1)]
+    items = blocks[0]
+    TT = float(len(t))
+    x_on = sg.XCorr(target_total=TT)
+    monkeypatch.setenv("SATSUMA2_GB300_SPECTRA", "0")
+    x_off = sg.XCorr(target_total=TT)
+    monkeypatch.delenv("SATSUMA2_GB300_SPECTRA")
+    b_on, b_off = x_on.upload(items), x_off.upload(items)
+    assert b_on.launches() == b_off.launches() + 1           # the spectra kernel
+    b_on.run()
+    b_off.run()
+    r_on, c_on = b_on.results(with_counts=True)
+    r_off, c_off = b_off.results(with_counts=True)
+    assert np.array_equal(c_on, c_off)
+    assert parity.same_results(r_on, r_off, prob_rtol=0.0, target_total=0.0)
+    o_on, o_off = b_on.offsets(), b_off.offsets()
+    for k in range(len(items)):
+        for s2 in range(2):
+            assert np.array_equal(o_on[k][s2], o_off[k][s2]), (k, s2)
+    assert len(r_on) > 0
+    P = O.params(target_total=TT)
+    starts = np.concatenate([[0], np.cumsum(c_on.astype(np.int64))])
+    tb, qb = t.tobytes(), q.tobytes()
+    for k in range(0, len(items), 7):
+        it = items[k]
+        ts, qs = int(it["t_chunk_start"]), int(it["q_chunk_start"])
+        pr = O.pair(tb[ts:ts + int(it["tlen"])], qb[qs:qs + int(it["qlen"])], t_chunk_start=ts, q_chunk_start=qs,
+                    query_size=len(qb))
+        want, _ = O.align_pair(P, pr, offsets_in=o_on[k])
+        assert parity.same_results(r_on[starts[k]:starts[k + 1]], want, target_total=TT), k
+    b_on.free()
+    b_off.free()
+    x_on.close()
+    x_off.close()
 
 
 def test_serving_probtable_blocks_overflow_vs_oracle(O):
