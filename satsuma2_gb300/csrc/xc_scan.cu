@@ -67,10 +67,11 @@ __device__ __forceinline__ int diag_len(int pos, int T, int Q) {
 }
 
 // Count of G/C bases in [a, e) from a per-word prefix and the bitplanes.
-__device__ __forceinline__ int gc_count(const uint32_t* b0, const uint32_t* b1, const int* pref, int a, int e) {
+__device__ __forceinline__ int gc_count(const uint2* b, const int* pref, int a, int e) {
   const int wa = a >> 5, we = e >> 5;
-  const int ga = pref[wa] + __popc((b0[wa] ^ b1[wa]) & lowmask(a & 31));
-  const int ge = pref[we] + __popc((b0[we] ^ b1[we]) & lowmask(e & 31));
+  const uint2 x = b[wa], y = b[we];
+  const int ga = pref[wa] + __popc((x.x ^ x.y) & lowmask(a & 31));
+  const int ge = pref[we] + __popc((y.x ^ y.y) & lowmask(e & 31));
   return ge - ga;
 }
 
@@ -84,11 +85,11 @@ __device__ __forceinline__ int warp_incl_sum(int v, int lane) {
 }
 
 // Warp-cooperative exclusive prefix of per-word G/C counts -> pref[0..nw].
-__device__ __forceinline__ void gc_prefix(const uint32_t* b0, const uint32_t* b1, int* pref, int nw, int lane) {
+__device__ __forceinline__ void gc_prefix(const uint2* b, int* pref, int nw, int lane) {
   int run = 0;
   for (int w0 = 0; w0 < nw; w0 += 32) {
     const int w = w0 + lane;
-    const int c = w < nw ? __popc(b0[w] ^ b1[w]) : 0;
+    const int c = w < nw ? __popc(b[w].x ^ b[w].y) : 0;
     const int incl = warp_incl_sum(c, lane);
     if (w < nw) pref[w] = run + incl - c;
     run += __shfl_sync(0xffffffffu, incl, 31);
@@ -97,13 +98,14 @@ __device__ __forceinline__ void gc_prefix(const uint32_t* b0, const uint32_t* b1
 }
 
 // 2-bit code planes of len bytes at g (16-byte aligned, readable up to the
-// next 16-byte boundary) into p0/p1 words 0..nw-1, positions >= len zero.
+// next 16-byte boundary) into words 0..nw-1 of p (plane 0 in .x, plane 1 in
+// .y: the two words of a position range come in one 8-byte access),
+// positions >= len zero.
 // Each lane loads 16 bytes, forms four codes per 32-bit word
 // ((b>>1 ^ b>>2) & 3, A=0 C=1 G=2 T=3), gathers their plane bits with one
 // multiply per word, and lanes 2j, 2j+1 join their 16 bits into one word.
 // Every thread of the CTA calls it.
-__device__ __forceinline__ void build_planes(const uint8_t* __restrict__ g, int len, uint32_t* p0, uint32_t* p1,
-                                             int nw, int tid) {
+__device__ __forceinline__ void build_planes(const uint8_t* __restrict__ g, int len, uint2* p, int nw, int tid) {
   for (int c0 = 0; c0 < 2 * nw; c0 += NT_SCAN) {
     const int c = c0 + tid;
     uint32_t m0 = 0u, m1 = 0u;
@@ -123,10 +125,7 @@ __device__ __forceinline__ void build_planes(const uint8_t* __restrict__ g, int 
       }
     }
     const uint32_t h0 = __shfl_down_sync(0xffffffffu, m0, 1), h1 = __shfl_down_sync(0xffffffffu, m1, 1);
-    if (!(tid & 1) && c < 2 * nw) {
-      p0[c >> 1] = m0 | (h0 << 16);
-      p1[c >> 1] = m1 | (h1 << 16);
-    }
+    if (!(tid & 1) && c < 2 * nw) p[c >> 1] = make_uint2(m0 | (h0 << 16), m1 | (h1 << 16));
   }
 }
 
@@ -189,12 +188,10 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
   uint8_t* st = smem;
   uint8_t* sq = st + N;
   uint32_t* queue = reinterpret_cast<uint32_t*>(smem);   // bitplane path only: item | bit << 12
-  uint32_t* tb0 = reinterpret_cast<uint32_t*>(smem + Gm::region);
-  uint32_t* tb1 = tb0 + TWP;
-  int* tgp = reinterpret_cast<int*>(tb1 + TWP);
-  uint32_t* qb0 = reinterpret_cast<uint32_t*>(tgp + (TW + 1));
-  uint32_t* qb1 = qb0 + QWP;
-  int* qgp = reinterpret_cast<int*>(qb1 + QWP);
+  uint2* tb = reinterpret_cast<uint2*>(smem + Gm::region);   // target planes (zero padded)
+  uint2* qb = tb + TWP;                                       // query planes, QPAD zero words first
+  int* tgp = reinterpret_cast<int*>(qb + QWP);
+  int* qgp = tgp + (TW + 1);
   int* offs = qgp + (TW + 1);
   uint32_t* wmask = reinterpret_cast<uint32_t*>(offs + OFF_CHUNK);    // [MW][NT_SCAN] pass-1 marked words
   uint32_t* items = wmask + Gm::MW * NT_SCAN;                         // [ICAP] diag | word << 7
@@ -246,17 +243,13 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
     // position 32w+u.  The pair is all A/C/G/T, whose complement flips both
     // code bits.  Strand 1 builds the query's forward planes in the (here
     // unused) byte region first and reads them backwards.
-    if (tid < QPAD) {
-      qb0[tid] = 0u;
-      qb1[tid] = 0u;
-    }
-    build_planes(gt, T, tb0, tb1, TWP, tid);
+    if (tid < QPAD) qb[tid] = make_uint2(0u, 0u);
+    build_planes(gt, T, tb, TWP, tid);
     if (!strand) {
-      build_planes(gq, Q, qb0 + QPAD, qb1 + QPAD, QWP - QPAD, tid);
+      build_planes(gq, Q, qb + QPAD, QWP - QPAD, tid);
     } else {
-      uint32_t* f0 = reinterpret_cast<uint32_t*>(smem);
-      uint32_t* f1 = f0 + (TW + 2);
-      build_planes(gq, Q, f0, f1, TW + 2, tid);
+      uint2* f = reinterpret_cast<uint2*>(smem);
+      build_planes(gq, Q, f, TW + 2, tid);
       __syncthreads();
       // word w of the reverse complement: forward positions Q-32-32w ..
       // Q-1-32w, bit-reversed and complemented; positions past Q are zero
@@ -268,23 +261,23 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
           uint32_t g0, g1;
           if (s0 >= 0) {
             const int fw = s0 >> 5, sh = s0 & 31;
-            g0 = __funnelshift_r(f0[fw], f0[fw + 1], sh);
-            g1 = __funnelshift_r(f1[fw], f1[fw + 1], sh);
+            const uint2 a = f[fw], b2 = f[fw + 1];
+            g0 = __funnelshift_r(a.x, b2.x, sh);
+            g1 = __funnelshift_r(a.y, b2.y, sh);
           } else {
-            g0 = f0[0] << -s0;
-            g1 = f1[0] << -s0;
+            g0 = f[0].x << -s0;
+            g1 = f[0].y << -s0;
           }
           const uint32_t m = lowmask(lim);
           r0 = ~__brev(g0) & m;
           r1 = ~__brev(g1) & m;
         }
-        qb0[QPAD + w] = r0;
-        qb1[QPAD + w] = r1;
+        qb[QPAD + w] = make_uint2(r0, r1);
       }
     }
     __syncthreads();
-    if (warp == 0) gc_prefix(tb0, tb1, tgp, TW, lane);
-    if (warp == 1) gc_prefix(qb0 + QPAD, qb1 + QPAD, qgp, TW, lane);
+    if (warp == 0) gc_prefix(tb, tgp, TW, lane);
+    if (warp == 1) gc_prefix(qb + QPAD, qgp, TW, lane);
   }
   __syncthreads();
 
@@ -295,9 +288,10 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
     if (w < 0) return 0u;
     const int qo = 32 * w + pos + 32 * QPAD;
     const int qw = qo >> 5, sh = qo & 31;
-    const uint32_t q0 = __funnelshift_r(qb0[qw], qb0[qw + 1], sh);
-    const uint32_t q1 = __funnelshift_r(qb1[qw], qb1[qw + 1], sh);
-    return ~((tb0[w] ^ q0) | (tb1[w] ^ q1));
+    const uint2 a = qb[qw], b = qb[qw + 1], t = tb[w];
+    const uint32_t q0 = __funnelshift_r(a.x, b.x, sh);
+    const uint32_t q1 = __funnelshift_r(a.y, b.y, sh);
+    return ~((t.x ^ q0) | (t.y ^ q1));
   };
   // Equal bases of segment [s0, s1) on diagonal pos.  (A version streaming
   // one query word per target word measured 17% slower over the whole scan.)
@@ -317,11 +311,16 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
   auto ewords3 = [&](int pos, int w, uint32_t& e2, uint32_t& e1, uint32_t& e0) {
     const int qo = 32 * (w - 2) + pos + 32 * QPAD;
     const int qw = qo >> 5, sh = qo & 31;
-    const uint32_t x0 = qb0[qw], x1 = qb0[qw + 1], x2 = qb0[qw + 2], x3 = qb0[qw + 3];
-    const uint32_t y0 = qb1[qw], y1 = qb1[qw + 1], y2 = qb1[qw + 2], y3 = qb1[qw + 3];
-    e2 = w >= 2 ? ~((tb0[w - 2] ^ __funnelshift_r(x0, x1, sh)) | (tb1[w - 2] ^ __funnelshift_r(y0, y1, sh))) : 0u;
-    e1 = ~((tb0[w - 1] ^ __funnelshift_r(x1, x2, sh)) | (tb1[w - 1] ^ __funnelshift_r(y1, y2, sh)));
-    e0 = ~((tb0[w] ^ __funnelshift_r(x2, x3, sh)) | (tb1[w] ^ __funnelshift_r(y2, y3, sh)));
+    const uint2 q0 = qb[qw], q1 = qb[qw + 1], q2 = qb[qw + 2], q3 = qb[qw + 3];
+    const uint2 t1 = tb[w - 1], t0 = tb[w];
+    if (w >= 2) {
+      const uint2 t2 = tb[w - 2];
+      e2 = ~((t2.x ^ __funnelshift_r(q0.x, q1.x, sh)) | (t2.y ^ __funnelshift_r(q0.y, q1.y, sh)));
+    } else {
+      e2 = 0u;
+    }
+    e1 = ~((t1.x ^ __funnelshift_r(q1.x, q2.x, sh)) | (t1.y ^ __funnelshift_r(q1.y, q2.y, sh)));
+    e0 = ~((t0.x ^ __funnelshift_r(q2.x, q3.x, sh)) | (t0.y ^ __funnelshift_r(q2.y, q3.y, sh)));
   };
 
   // One DoOne segment [s0, s1) on offset pos (CrossCorr.cc:693,713) through
@@ -343,8 +342,8 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
     if (len < P.min_len) return;
     double matches, gcT, gcQ;
     if (!generic) {
-      const int gT = gc_count(tb0, tb1, tgp, s0, s1);
-      const int gQ = gc_count(qb0 + QPAD, qb1 + QPAD, qgp, s0 + pos, s1 + pos);
+      const int gT = gc_count(tb, tgp, s0, s1);
+      const int gQ = gc_count(qb + QPAD, qgp, s0 + pos, s1 + pos);
       if (!P.ptable) {
         // FP32 screen on the z-score (pm*N - hits) / sd: reject only past a
         // threshold set on the host with a margin far beyond FP32 error;
@@ -527,13 +526,12 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
         const int qd = (pos + 32 * QPAD) >> 5, sh = (pos + 32 * QPAD) & 31;
         uint32_t e2 = eword(pos, wfirst - 2), e1 = eword(pos, wfirst - 1);
         int qi = wfirst + qd;
-        uint32_t a0 = qb0[qi], a1 = qb1[qi];
+        uint2 a = qb[qi];
         uint32_t acc = 0;
         for (int w = wfirst; w <= wlast; w++) {
-          const uint32_t n0 = qb0[qi + 1], n1 = qb1[qi + 1];
-          const uint32_t e0 = ~((tb0[w] ^ __funnelshift_r(a0, n0, sh)) | (tb1[w] ^ __funnelshift_r(a1, n1, sh)));
-          a0 = n0;
-          a1 = n1;
+          const uint2 nx = qb[qi + 1], tw = tb[w];
+          const uint32_t e0 = ~((tw.x ^ __funnelshift_r(a.x, nx.x, sh)) | (tw.y ^ __funnelshift_r(a.y, nx.y, sh)));
+          a = nx;
           qi++;
           const int q = w - wfirst;
           acc |= (uint32_t)screen_word(e2, e1, e0) << (q & 31);
