@@ -619,6 +619,12 @@ def run_ours(args):
         u = W.uneven_batch(20000, seed=SEED + rank)
         xu = sg.XCorr(fft_len=-1, target_total=float(sum(len(t) for t, _ in u)), device=local)
         other["uneven_20000_fft_1024_8192"] = device_rate(xu, u)
+        # the same batch after the autotuner has picked each length's kernel form
+        t0 = time.perf_counter()
+        table = xu.tune()
+        tune_s = time.perf_counter() - t0
+        other["uneven_20000_fft_1024_8192_tuned"] = device_rate(xu, u)
+        other["tuning"] = {"seconds": tune_s, "table": table.strip().splitlines()}
         xu.close()
         lg = W.large_batch(2000, seed=SEED + rank)
         xg = sg.XCorr(t_chunk=16384, q_chunk=16384, target_total=16384.0 * 2000, device=local)

@@ -191,6 +191,22 @@ int xc_debug_pair(xc_ctx* ctx, const xc_pair* pair, float* sig, float* xc, int* 
 int xc_align_pair_noalloc(xc_ctx* ctx, const xc_pair* pair, xc_result* out, size_t cap,
                           size_t* n_out);
 
+/* Autotuner of the correlation stage.  For each FFT length 1024..8192 it
+ * times, on a synthetic batch of that length, the kernel forms the library
+ * is built with -- threads per transform and pairs per CTA: the per-strand
+ * kernel with 512, 256 or 128 threads per strand at 1024..4096; at 8192 the
+ * persistent both-strands kernel, the one-CTA-per-pair form or the
+ * per-strand kernel -- and keeps the fastest in the context.  All forms give
+ * the same results bit for bit.  It replaces FFTReal's one fixed pass plan
+ * (extern/RealFFT/FFTReal.hpp:429-458).  table (if not NULL, cap bytes) gets
+ * the choices as text, one line per length, with every candidate's time;
+ * *table_len its length.  Takes about a second; serialises on the context. */
+int xc_tune(xc_ctx* ctx, char* table, size_t cap, size_t* table_len);
+/* Applies a table xc_tune wrote (lines "fft_len=L strand_threads=T" and, at
+ * 8192, "pair_form=F": 2 persistent, 1 one CTA per pair, 0 per-strand only).
+ * xc_create applies the file SATSUMA2_GB300_TUNING names, if set. */
+int xc_apply_tuning(xc_ctx* ctx, const char* table);
+
 /* Library version and the device it runs on. */
 const char* xc_version(void);
 int xc_device_name(xc_ctx* ctx, char* buf, size_t len);

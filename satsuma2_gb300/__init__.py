@@ -34,7 +34,7 @@ EXPORTS = ("xc_create", "xc_destroy", "xc_align_pairs", "xc_batch_upload", "xc_b
            "xc_batch_results", "xc_batch_free", "xc_batch_launches", "xc_batch_run_timed",
            "xc_transfer_stats", "xc_submit", "xc_wait", "xc_serving_stats", "xc_debug_pair",
            "xc_version", "xc_device_name", "xc_align_pair_noalloc", "xc_batch_offsets",
-           "xc_batch_straddles")
+           "xc_batch_straddles", "xc_tune", "xc_apply_tuning")
 STRAD_CAP = 16   # XC_STRAD_CAP: near-threshold lags listed per pair strand
 
 
@@ -99,6 +99,8 @@ def load(path=LIB_PATH):
     lib.xc_serving_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                      ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
     lib.xc_debug_pair.argtypes = [vp, ctypes.POINTER(Pair), vp, vp, vp, vp, vp, vp, i, ctypes.POINTER(i)]
+    lib.xc_tune.argtypes = [vp, ctypes.c_char_p, sz, ctypes.POINTER(sz)]
+    lib.xc_apply_tuning.argtypes = [vp, ctypes.c_char_p]
     lib.xc_version.restype = ctypes.c_char_p
     lib.xc_device_name.argtypes = [vp, ctypes.c_char_p, sz]
     _lib = lib
@@ -283,6 +285,16 @@ class XCorr:
                 continue
             _check(r, "xc_wait")
             return out[:n_out.value].copy()
+
+    def tune(self):
+        """Runs the autotuner (xc_tune) and returns its table (text)."""
+        n = ctypes.c_size_t()
+        buf = ctypes.create_string_buffer(8192)
+        _check(self.lib.xc_tune(self.ctx, buf, len(buf), ctypes.byref(n)), "xc_tune")
+        return buf.value.decode()
+
+    def apply_tuning(self, table):
+        _check(self.lib.xc_apply_tuning(self.ctx, table.encode()), "xc_apply_tuning")
 
     def transfer_stats(self):
         h, d = ctypes.c_uint64(), ctypes.c_uint64()

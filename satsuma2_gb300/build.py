@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # terms, probability table) must round exactly as the reference's x86-64 build.
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                  "-I", INCLUDE, "-I", CSRC]
-LIB_SOURCES = ["xc_corr.cu", "xc_scan.cu", "xc_runtime.cu", "xc_server.cu", "xc_noalloc.cu"]
+LIB_SOURCES = ["xc_corr.cu", "xc_scan.cu", "xc_runtime.cu", "xc_server.cu", "xc_noalloc.cu", "xc_tune.cu"]
 SLAVE_SOURCES = ["slave_main.cpp"]
 
 

@@ -92,7 +92,7 @@ __device__ __forceinline__ void hermitian_pack(float2* __restrict__ buf, const S
 // in strad_cnt[pair*2+strand] and the first STRAD_CAP of them are listed.
 // There the reference's FP32 FFT and this one may decide differently; every
 // other lag's decision is the same for both.
-template <int LOG2L, int NTF = NT_CORR, class SY = CtaBarrier>
+template <int LOG2L, int NTF = NT_CORR, class SY = CtaBarrier, int KMAX = (NTF <= 256 ? 32 : 16)>
 __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, uint32_t off_base, int pidx,
                                          int strand, const float2* __restrict__ buf, int t, int* s_warp,
                                          SY sync = SY(), float scale = 1.0f / (float)(1 << (LOG2L - 1))) {
@@ -108,10 +108,9 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
     const float2 z = buf[swz(n >> 1)];
     return ((n & 1) ? z.y : z.x) * scale;
   };
-  // Up to L = 8192 a lane's values stay in registers across the three passes
-  // (envelope, count, compaction): 16 on 512 threads, 32 on 256; longer
-  // transforms re-read them.
-  constexpr bool KEEP = ITER <= (NTF <= 256 ? 32 : 16);
+  // Up to KMAX values a lane's values stay in registers across the three
+  // passes (envelope, count, compaction); more are re-read from the buffer.
+  constexpr bool KEEP = ITER <= KMAX;
   float xs[KEEP ? ITER : 1];
   if constexpr (KEEP) {
 #pragma unroll
@@ -220,9 +219,11 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
   }
 }
 
-// One (pair, strand) on the CTA's NT_CORR threads; slot indexes the global
+// One (pair, strand) on the CTA's NT threads (512, or 256 / 128 at short FFT
+// lengths, where more CTAs then share an SM; the autotuner picks per length);
+// each of the two transform groups has NT/2 threads.  slot indexes the global
 // channel-sum scratch at L = 32768.
-template <int LOG2L>
+template <int LOG2L, int NT>
 __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int slot, int strand,
                                             unsigned char* smem) {
   constexpr int L = 1 << LOG2L;
@@ -251,7 +252,7 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
   __shared__ double s_off[8];
   __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
   __shared__ Split3 s_wf[2][8];    // the same as three floats each
-  __shared__ int s_warp[2 * NT_CORR / 32];
+  __shared__ int s_warp[2 * NT / 32];
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -262,7 +263,7 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
 
   // ---- 1. chunk bytes (DNAVector::ReverseComplement, DNAVector.cc:482-500) ----
   int high = 0, nonacgt = 0, th_t = 0, th_q = 0;
-  for (int i = tid; i < N; i += NT_CORR) {
+  for (int i = tid; i < N; i += NT) {
     unsigned b = 0;
     if (i < T) {
       b = gt[i];
@@ -281,7 +282,7 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
     }
     sq[i] = (uint8_t)c;
   }
-  for (int i = tid; i < NH; i += NT_CORR) {
+  for (int i = tid; i < NH; i += NT) {
     twNh[i] = P.tab.twN_hi[i];
     twLh[i] = P.tab.twL_hi[i];
   }
@@ -303,7 +304,7 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
   }
   if (tid == 0 && strand == 0) P.pair_flags[pidx] = (D.flags & PF_FAST) | (generic ? PF_GENERIC : 0u);
   if constexpr (!SEQ)
-    for (int i = tid; i < N + 8; i += NT_CORR) accE[i] = make_float2(0.f, 0.f);   // accE and accO
+    for (int i = tid; i < N + 8; i += NT) accE[i] = make_float2(0.f, 0.f);   // accE and accO
   float2* gaccE = nullptr;   // SEQ: this strand's channel sums in global memory
   float2* gaccO = nullptr;
   if constexpr (SEQ) {
@@ -316,8 +317,8 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
   //      without one-third letters have exact quarter-unit base sums, so Ent
   //      comes from a table the host computed with the same double
   //      expression; others repeat the reference's double arithmetic here. ----
-  {
-    const int which = tid >> 8, w = tid & 255;
+  for (int x = tid; x < 2 * NWIN; x += NT) {
+    const int which = x >> 8, w = x & 255;
     const uint8_t* s = which ? sq : st;
     const int len = which ? Q : T;
     const int third = which ? th_q : th_t;
@@ -375,7 +376,7 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
     if (!generic) {
       // A/C/G/T: one 8-bit count field per base (at most N / 512 <= 32 per thread)
       uint32_t ct = 0, cq = 0;
-      for (int i = tid; i < N; i += NT_CORR) {
+      for (int i = tid; i < N; i += NT) {
         if (i < T) ct += 1u << (8 * code_of(st[i]));
         if (i < Q) cq += 1u << (8 * code_of(sq[i]));
       }
@@ -385,7 +386,7 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
         cn[4 + k] = 4 * (int)((cq >> (8 * k)) & 255u);
       }
     } else {
-      for (int i = tid; i < N; i += NT_CORR) {
+      for (int i = tid; i < N; i += NT) {
         if (i < T) { const uchar4 q = c_w4q[st[i]]; cn[0] += q.x; cn[1] += q.y; cn[2] += q.z; cn[3] += q.w; }
         if (i < Q) { const uchar4 q = c_w4q[sq[i]]; cn[4] += q.x; cn[5] += q.y; cn[6] += q.z; cn[7] += q.w; }
       }
@@ -420,19 +421,22 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
   }
   __syncthreads();
 
-  const int grp = tid >> 8;   // 0: even-bin transform, 1: odd-bin transform
-  const int gtid = tid & 255;
+  constexpr int HG = NT / 2;   // threads of a transform group
+  const int grp = tid / HG;    // 0: even-bin transform, 1: odd-bin transform
+  const int gtid = tid % HG;
 
   for (int c = 0; c < 4; c++) {
     // Per-window channel values: out = float(entropy * (weight - mean))
     // (CrossCorr.cc:123), weight 0 or 1 for A/C/G/T.
     if (!generic) {
-      const float E = (grp ? Eq : Et)[gtid];
-      const int k = grp * 4 + c;
-      float2 v;
-      v.x = mul_round_f32(E, s_wf[0][k], s_wmo[0][k]);
-      v.y = mul_round_f32(E, s_wf[1][k], s_wmo[1][k]);
-      (grp ? vq : vt)[gtid] = v;
+      for (int w = gtid; w < NWIN; w += HG) {
+        const float E = (grp ? Eq : Et)[w];
+        const int k = grp * 4 + c;
+        float2 v;
+        v.x = mul_round_f32(E, s_wf[0][k], s_wmo[0][k]);
+        v.y = mul_round_f32(E, s_wf[1][k], s_wmo[1][k]);
+        (grp ? vq : vt)[w] = v;
+      }
     }
     __syncthreads();
 
@@ -445,8 +449,8 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
       const int stid = swz(tid);
       for (int g = 0; g < 2; g++) {
 #pragma unroll 4
-        for (int it = 0; it < N / NT_CORR; it++) {
-          const int n = tid + NT_CORR * it;
+        for (int it = 0; it < N / NT; it++) {
+          const int n = tid + NT * it;
           float x = 0.f, y = 0.f;
           const int w = n / WIN;
           if (!generic) {
@@ -462,12 +466,12 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
             ds[(size_t)(4 + c) * L + n] = y;
           }
           const float2 z = make_float2(x, y);
-          bufE[stid ^ swz(NT_CORR * it)] = g ? cmul(z, tw2(twLh, twLl, n)) : z;
+          bufE[stid ^ swz(NT * it)] = g ? cmul(z, tw2(twLh, twLl, n)) : z;
         }
         __syncthreads();
-        fft_forward<LOG2N>(bufE, twNh, twNl, tid, NT_CORR);
+        fft_forward<LOG2N>(bufE, twNh, twNl, tid, NT);
         if (g == 0) {
-          for (int m = tid; m <= N / 2; m += NT_CORR) {
+          for (int m = tid; m <= N / 2; m += NT) {
             const float2 A = bufE[lp<LOG2N>(m)];
             const float2 B = bufE[lp<LOG2N>((N - m) & (N - 1))];
             const float2 X = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
@@ -476,7 +480,7 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
             gaccE[m] = c ? cadd(gaccE[m], v) : v;
           }
         } else {
-          for (int m = tid; m < N / 2; m += NT_CORR) {
+          for (int m = tid; m < N / 2; m += NT) {
             const float2 A = bufE[lp<LOG2N>(m)];
             const float2 B = bufE[lp<LOG2N>(N - 1 - m)];
             const float2 X = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
@@ -500,8 +504,8 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
       const int stid = swz(tid);
       const float2 wt = tw2(twLh, twLl, tid);
 #pragma unroll
-      for (int it = 0; it < N / NT_CORR; it++) {
-        const int n = tid + NT_CORR * it;
+      for (int it = 0; it < N / NT; it++) {
+        const int n = tid + NT * it;
         float x = 0.f, y = 0.f;
         const int w = n / WIN;
         if (!generic) {
@@ -516,33 +520,33 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
           ds[(size_t)c * L + n] = x;
           ds[(size_t)(4 + c) * L + n] = y;
         }
-        const int sn = stid ^ swz(NT_CORR * it);   // tid and NT_CORR*it share no bit
-        // W_L^(512 it) = exp(-i pi (16384 it / L) / 16)
-        const float2 wc = make_float2(cos_pi16((16384 / L) * it), -sin_pi16((16384 / L) * it));
+        const int sn = stid ^ swz(NT * it);   // tid and NT*it share no bit
+        // W_L^(NT it) = exp(-i pi (32 NT it / L) / 16)
+        const float2 wc = make_float2(cos_pi16((32 * NT / L) * it), -sin_pi16((32 * NT / L) * it));
         bufE[sn] = make_float2(x, y);
         bufO[sn] = cmul(make_float2(x, y), cmul(wt, wc));
       }
     }
     __syncthreads();
 
-    fft_forward<LOG2N>(grp ? bufO : bufE, twNh, twNl, gtid, 256);
+    fft_forward<LOG2N>(grp ? bufO : bufE, twNh, twNl, gtid, HG);
 
     // Per-bin product (CrossCorrelation::DoOne, CrossCorr.cc:477-492):
     // X = target spectrum, Y = query spectrum from Z(k), Z(L-k).
     // conj(X)Y on bins 1..N-2, X(0)Y(0) on bin 0, and the target's own value
     // on bins N-1 and N, which the reference's loop leaves unmultiplied.
-    // Addresses: swz(posof(.)) is XOR-linear, so for m = gtid + 256*it it is
-    // lp(gtid) ^ lp(256*it) with the second term a compile-time constant.
+    // Addresses: swz(posof(.)) is XOR-linear, so for m = gtid + HG*it it is
+    // lp(gtid) ^ lp(HG*it) with the second term a compile-time constant.
     if (grp == 0) {
       const int la = lp<LOG2N>(gtid);
-      const int lb = lp<LOG2N>((256 - gtid) & 255);
+      const int lb = lp<LOG2N>((HG - gtid) & (HG - 1));
 #pragma unroll
-      for (int it = 0; it <= N / 512; it++) {
-        const int m = gtid + 256 * it;
+      for (int it = 0; it <= N / (2 * HG); it++) {
+        const int m = gtid + HG * it;
         if (m > N / 2) break;
-        // partner N-m = (N - 256(it+1)) | (256 - gtid) for gtid >= 1
-        const int pb = gtid ? (lb ^ lp<LOG2N>(N - 256 * (it + 1))) : lp<LOG2N>((N - 256 * it) & (N - 1));
-        const float2 A = bufE[la ^ lp<LOG2N>(256 * it)];
+        // partner N-m = (N - HG(it+1)) | (HG - gtid) for gtid >= 1
+        const int pb = gtid ? (lb ^ lp<LOG2N>(N - HG * (it + 1))) : lp<LOG2N>((N - HG * it) & (N - 1));
+        const float2 A = bufE[la ^ lp<LOG2N>(HG * it)];
         const float2 B = bufE[pb];
         const float2 X = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
         const float2 Y = make_float2(0.5f * (A.y + B.y), -0.5f * (A.x - B.x));
@@ -552,9 +556,9 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
     } else {
       const int la = lp<LOG2N>(gtid);
 #pragma unroll
-      for (int it = 0; it < N / 512; it++) {
-        const int m = gtid + 256 * it;
-        const int pa = la ^ lp<LOG2N>(256 * it);
+      for (int it = 0; it < N / (2 * HG); it++) {
+        const int m = gtid + HG * it;
+        const int pa = la ^ lp<LOG2N>(HG * it);
         const float2 A = bufO[pa];
         const float2 B = bufO[pa ^ lp<LOG2N>(N - 1)];   // N-1-m = m ^ (N-1)
         const float2 X = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
@@ -572,22 +576,27 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
     if constexpr (SEQ) return (k & 1) ? gaccO[k >> 1] : gaccE[k >> 1];
     return (k & 1) ? accO[k >> 1] : accE[k >> 1];
   };
-  hermitian_pack<LOG2L>(bufE, S, twLh, twLl, tid);
+  hermitian_pack<LOG2L, NT>(bufE, S, twLh, twLl, tid);
   __syncthreads();
-  fft_inverse<LOG2N>(bufE, twNh, twNl, tid, NT_CORR);
+  fft_inverse<LOG2N>(bufE, twNh, twNl, tid, NT);
 
   // ---- 5. FindTop ----
-  find_top<LOG2L>(P, D.flags, D.off_base, pidx, strand, bufE, tid, s_warp);
+  find_top<LOG2L, NT, CtaBarrier, 16>(P, D.flags, D.off_base, pidx, strand, bufE, tid, s_warp);
 }
 
-template <int LOG2L>
-__global__ void __launch_bounds__(NT_CORR, (LOG2L <= 13) ? 2 : 1) corr_kernel(const CorrParams P) {
+// Resident CTAs per SM the register budget is set for (64 registers per thread).
+__host__ __device__ constexpr int corr_min_blocks(int log2L, int nt) { return log2L <= 13 ? 1024 / nt : 1; }
+
+template <int LOG2L, int NT = NT_CORR>
+__global__ void __launch_bounds__(NT, corr_min_blocks(LOG2L, NT)) corr_kernel(const CorrParams P) {
+  static_assert(NT == 512 || (NT >= 128 && 32 * NT % (1 << LOG2L) == 0 && LOG2L <= 13),
+                "fewer threads per strand only where W_L^(NT it) is a multiple of pi/16");
   extern __shared__ __align__(16) unsigned char smem[];
   // One pair per CTA column, or (fb_list) the pairs corr_pair_kernel handed
   // back, CTA columns striding over the list.
   const int cnt = P.fb_list ? *P.fb_cnt : (int)blockIdx.x + 1;
   for (int j = blockIdx.x; j < cnt; j += gridDim.x) {
-    corr_strand<LOG2L>(P, P.fb_list ? P.fb_list[j] : P.first + j, j, blockIdx.y, smem);
+    corr_strand<LOG2L, NT>(P, P.fb_list ? P.fb_list[j] : P.first + j, j, blockIdx.y, smem);
     __syncthreads();
   }
 }
@@ -1585,10 +1594,32 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
 cudaError_t prepare_scan_kernels();
 cudaError_t upload_scan_constants(const unsigned char* rc256, const uchar4* w4q128, const double* w4d);
 
-template <int LOG2L>
+template <int LOG2L, int NT = NT_CORR>
 static cudaError_t set_corr_attrs() {
-  return cudaFuncSetAttribute(corr_kernel<LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(corr_kernel<LOG2L, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)corr_smem_bytes(LOG2L));
+}
+
+// The per-strand kernel at FFT length 2^log2L with nt threads per strand
+// (512; 256 up to 8192; 128 up to 4096), grid (x, 2).
+static cudaError_t launch_strand(int log2L, int nt, dim3 grid, const CorrParams& p, cudaStream_t s) {
+  const size_t sm = corr_smem_bytes(log2L);
+#define XC_STRAND(LG, NTV)                                  \
+  if (log2L == LG && nt == NTV) {                           \
+    corr_kernel<LG, NTV><<<grid, NTV, sm, s>>>(p);          \
+    return cudaGetLastError();                              \
+  }
+  XC_STRAND(10, 512) XC_STRAND(10, 256) XC_STRAND(10, 128)
+  XC_STRAND(11, 512) XC_STRAND(11, 256) XC_STRAND(11, 128)
+  XC_STRAND(12, 512) XC_STRAND(12, 256) XC_STRAND(12, 128)
+  XC_STRAND(13, 512) XC_STRAND(13, 256)
+  XC_STRAND(14, 512) XC_STRAND(15, 512)
+#undef XC_STRAND
+  return cudaErrorInvalidValue;
+}
+
+bool strand_threads_ok(int log2L, int nt) {
+  return nt == 512 || (nt == 256 && log2L <= 13) || (nt == 128 && log2L <= 12);
 }
 
 cudaError_t prepare_kernels() {
@@ -1608,6 +1639,13 @@ cudaError_t prepare_kernels() {
   if ((e = set_corr_attrs<11>()) != cudaSuccess) return e;
   if ((e = set_corr_attrs<12>()) != cudaSuccess) return e;
   if ((e = set_corr_attrs<13>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<10, 256>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<11, 256>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<12, 256>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<13, 256>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<10, 128>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<11, 128>()) != cudaSuccess) return e;
+  if ((e = set_corr_attrs<12, 128>()) != cudaSuccess) return e;
   if ((e = set_corr_attrs<14>()) != cudaSuccess) return e;
   if ((e = set_corr_attrs<15>()) != cudaSuccess) return e;
   return prepare_scan_kernels();
@@ -1616,7 +1654,7 @@ cudaError_t prepare_kernels() {
 cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t s) {
   if (npairs <= 0) return cudaSuccess;
   dim3 grid(npairs, 2);
-  const size_t sm = corr_smem_bytes(log2L);
+  const int nt = strand_threads_ok(log2L, p.strand_threads) ? p.strand_threads : NT_CORR;
   if (p.fb_list) {
     // both strands per CTA, then corr_kernel over the pairs handed back:
     // one wave of CTAs striding over the list (*fb_cnt starts at zero)
@@ -1632,18 +1670,11 @@ cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t
       corr_pair2_kernel<PAIR_LOG2L><<<std::min(npairs, sms), NT_PAIR2, corr_pair2_smem_bytes(), s>>>(q);
     else
       corr_pair_kernel<PAIR_LOG2L><<<npairs, NT_PAIR, corr_pair_smem_bytes(PAIR_LOG2L), s>>>(q);
-    grid.x = std::min(npairs, sms);
+    grid.x = std::min(npairs, sms * (NT_CORR / nt));
   }
-  switch (log2L) {
-    case 10: corr_kernel<10><<<grid, NT_CORR, sm, s>>>(p); break;
-    case 11: corr_kernel<11><<<grid, NT_CORR, sm, s>>>(p); break;
-    case 12: corr_kernel<12><<<grid, NT_CORR, sm, s>>>(p); break;
-    case 13: corr_kernel<13><<<grid, NT_CORR, sm, s>>>(p); break;
-    case 14: corr_kernel<14><<<grid, NT_CORR, sm, s>>>(p); break;
-    case 15: corr_kernel<15><<<grid, NT_CORR, sm, s>>>(p); break;
-    default: return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_strand(log2L, nt, grid, p, s);
 }
 
 cudaError_t launch_corr_spec(const SpecParams& sp, const CorrParams& p, int npairs, cudaStream_t s) {
@@ -1661,8 +1692,10 @@ cudaError_t launch_corr_spec(const SpecParams& sp, const CorrParams& p, int npai
   // the pairs handed back: one wave of per-strand CTAs striding over the list
   CorrParams h = p;
   h.pair_chunk = nullptr;
-  corr_kernel<PAIR_LOG2L><<<dim3(std::min(npairs, sms), 2), NT_CORR, corr_smem_bytes(PAIR_LOG2L), s>>>(h);
-  return cudaGetLastError();
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int nt = strand_threads_ok(PAIR_LOG2L, p.strand_threads) ? p.strand_threads : NT_CORR;
+  return launch_strand(PAIR_LOG2L, nt, dim3(std::min(npairs, sms * (NT_CORR / nt)), 2), h, s);
 }
 
 cudaError_t upload_constants(const unsigned char* rc256, const uchar4* w4q128, const double* w4d) {

@@ -97,6 +97,7 @@ struct CorrParams {
   int pair_form;            // with fb_list: 2 = persistent 512-thread kernel, 1 = 1024-thread form
   // spectra path (FFT 8192 batches whose pairs share chunks): the pair kernel
   // reads both chunks' spectra instead of transforming them
+  int strand_threads;       // threads per strand of the per-strand kernel (0 = NT_CORR; see strand_threads_ok)
   const int* pair_chunk;    // [pair][2]: target and query chunk indices
   const float2* spec;       // [chunk][4][N] spectra, bin order (see SpecParams)
   const uint32_t* chunk_flags;
@@ -163,6 +164,8 @@ cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t
 // pair kernel from their spectra, then corr_kernel over the pairs handed back.
 cudaError_t launch_corr_spec(const SpecParams& sp, const CorrParams& p, int npairs, cudaStream_t s);
 size_t spec_bytes_per_chunk();
+// Thread counts per strand the per-strand correlation kernel is built for.
+bool strand_threads_ok(int log2L, int nt);
 cudaError_t launch_scan(int log2L, const ScanParams& p, int npairs, cudaStream_t s);
 cudaError_t launch_finalize(const int* res_cnt, const DevResult* res, int slots, int nslots,
                             int* dense_base, DevResult* dense, int* scan_tmp, cudaStream_t s);

@@ -159,6 +159,7 @@ int align_pair_noalloc(Ctx* c, const xc_pair& p, xc_result* out, size_t cap, siz
     cp.fb_cnt = cnt + C_MISC + 3;
     cp.pair_form = c->pair_form;
   }
+  cp.strand_threads = c->strand_threads[lg];
   NA_CHECK(launch_corr(lg, cp, 1, s));
 
   ScanParams sp{};

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <functional>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -573,6 +574,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
       cp.fb_cnt = b->d_misc + 3;   // zeroed above
       cp.pair_form = c->pair_form;
     }
+    cp.strand_threads = c->strand_threads[bk.log2L];
     cp.strad_cnt = b->d_stradcnt;
     cp.strad_list = b->d_strad;
     if (bk.log2L == PAIR_LOG2L && b->spec) {
@@ -923,6 +925,21 @@ int xc_create(const xc_params* params, int device, xc_ctx** out) {
     if (r == XC_OK)
       r = cuda_err(cudaMemcpy(c->d_ptable, c->h_ptable.data(), c->h_ptable.size() * sizeof(double),
                               cudaMemcpyHostToDevice), "probtable copy");
+  }
+  if (r == XC_OK) {
+    // a tuning table written by xc_tune, when SATSUMA2_GB300_TUNING names one
+    const char* tf = getenv("SATSUMA2_GB300_TUNING");
+    if (tf && tf[0]) {
+      FILE* f = fopen(tf, "r");
+      if (f) {
+        std::string text;
+        char buf[4096];
+        size_t k;
+        while ((k = fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, k);
+        fclose(f);
+        r = apply_tuning_text(c, text.c_str());
+      }
+    }
   }
   if (r == XC_OK) {
     cudaDeviceProp prop;

@@ -115,6 +115,7 @@ struct Ctx {
   bool pair_kernel = false;    // both-strands correlation kernel usable (entropy table complement-symmetric)
   int pair_form = 2;           // its form: 2 persistent 512-thread kernel, 1 the 1024-thread one
   bool spec_reuse = true;      // FFT-8192 batches whose pairs share chunks transform each chunk once
+  int strand_threads[MAX_LOG2L + 1] = {};   // per-strand kernel's threads per FFT length (0 = 512; xc_tune)
   unsigned char* noalloc_base = nullptr;   // xc_align_pair_noalloc's static array on this device (set at first use)
 };
 
@@ -153,6 +154,9 @@ float screen_z(double min_prob, double target_total);
 int ctx_align_pipelined(Ctx* c, const xc_pair* pairs, size_t n, xc_result* out, size_t cap, size_t* n_out,
                         size_t* pair_counts);
 void server_stop(Ctx* c);
+// Applies a tuning table (xc_tune's text: "fft_len=L strand_threads=T" and
+// "pair_form=F" lines; other text ignored); XC_ERR_ARG on a bad value.
+int apply_tuning_text(Ctx* c, const char* text);
 
 }  // namespace xc
 
