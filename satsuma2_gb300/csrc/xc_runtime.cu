@@ -545,9 +545,13 @@ float screen_z(double min_prob, double target_total) {
 // Enqueues the kernels of one batch on stream.
 static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
   const int nslots = 2 * b->n;
+  // stage events: external event nodes inside a graph capture, plain records otherwise
+  cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+  if (timed) XC_CHECK(cudaStreamIsCapturing(s, &cst));
+  const unsigned evflags = cst == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
   XC_CHECK(cudaMemsetAsync(b->d_misc, 0, 4 * sizeof(int), s));
   XC_CHECK(cudaMemsetAsync(b->d_stradcnt, 0, nslots * sizeof(int), s));
-  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[0], s, cudaEventRecordExternal));
+  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[0], s, evflags));
   for (const Bucket& bk : b->buckets) {
     const DevTables& t = c->tab[bk.log2L];
     CorrParams cp{};
@@ -593,7 +597,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     }
     XC_CHECK(launch_corr(bk.log2L, cp, bk.count, s));
   }
-  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[1], s, cudaEventRecordExternal));
+  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[1], s, evflags));
   for (const Bucket& bk : b->buckets) {
     ScanParams sp{};
     sp.pairs = b->d_desc;
@@ -623,9 +627,9 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     sp.dbg_cap = b->dbg_cap;
     XC_CHECK(launch_scan(bk.log2L, sp, bk.count, s));
   }
-  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[2], s, cudaEventRecordExternal));
+  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[2], s, evflags));
   XC_CHECK(launch_finalize(b->d_rescnt, b->d_res, b->slots, nslots, b->d_base, b->d_dense, nullptr, s));
-  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[3], s, cudaEventRecordExternal));
+  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[3], s, evflags));
   return XC_OK;
 }
 
