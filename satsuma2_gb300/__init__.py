@@ -131,6 +131,14 @@ def make_pairs(items):
     return arr, keep
 
 
+def _pair_array(items):
+    """items as a contiguous PAIR_DTYPE array if it is an array of chunk-pair
+    records (PAIR_DTYPE, or a concatenation that lost its padding), else None."""
+    if isinstance(items, np.ndarray) and items.dtype.names == PAIR_DTYPE.names:
+        return np.ascontiguousarray(items.astype(PAIR_DTYPE, copy=False))
+    return None
+
+
 def block_pairs(tbuf, tchunks, qbuf, qchunks, tf, tt, qf, qt, target_id=0, query_id=0, fast=0):
     """The chunk pairs of one t_pair block (inclusive chunk ranges), query-major
     as HomologyByXCorr::align_target loops (HomologyByXCorrSlave.cc:281-299),
@@ -197,7 +205,9 @@ class XCorr:
     def align(self, items, with_counts=False):
         """Runs chunk pairs (both strands) -> structured array of t_result
         records.  items as for make_pairs, or a PAIR_DTYPE array."""
-        if isinstance(items, np.ndarray) and items.dtype == PAIR_DTYPE:
+        pa = _pair_array(items)
+        if pa is not None:
+            items = pa   # (kept alive for the call)
             arr, n = ctypes.c_void_p(items.ctypes.data), len(items)
         else:
             arr, keep = make_pairs(items)
@@ -249,7 +259,9 @@ class XCorr:
     def upload(self, items):
         """Packs and uploads chunk pairs (items as for align, or a PAIR_DTYPE
         array) as a device-resident batch."""
-        if isinstance(items, np.ndarray) and items.dtype == PAIR_DTYPE:
+        pa = _pair_array(items)
+        if pa is not None:
+            items = pa   # (kept alive for the call)
             arr, n = ctypes.c_void_p(items.ctypes.data), len(items)
         else:
             arr, keep = make_pairs(items)
@@ -263,7 +275,9 @@ class XCorr:
         """Queues chunk pairs for the GPU; items as for align, the (array,
         keepalive) pair make_pairs returns (built ahead of time), or a
         PAIR_DTYPE array (block_pairs).  The library copies the sequences."""
-        if isinstance(items, np.ndarray) and items.dtype == PAIR_DTYPE:
+        pa = _pair_array(items)
+        if pa is not None:
+            items = pa   # (kept alive for the call)
             arr, n = ctypes.c_void_p(items.ctypes.data), len(items)
         else:
             if isinstance(items, tuple) and len(items) == 2 and isinstance(items[0], ctypes.Array):

@@ -394,7 +394,9 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   }
   for (size_t i = 0; i < n; i++) b->order[fill[b->log2L[i]]++] = (int)i;
   // pool and offset-list layout; a chunk that several pairs pass by the same
-  // pointer and length (a block's target and query chunks) is stored once
+  // pointer and length (a block's target and query chunks) is stored once.
+  // The distinct chunks of the FFT-8192 bucket are numbered as they appear
+  // (the spectra path's chunk table; every empty chunk is one entry).
   std::vector<uint64_t> toff(n), qoff(n);
   uint64_t pool = 0, offl = 0;
   b->desc_host.resize(n);
@@ -402,31 +404,67 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
     const char* p;
     int len;
     uint64_t off;
+    int cid;   // chunk index in the FFT-8192 bucket's table, -1 before its first use there
   };
   std::vector<Src> uniq;
   uniq.reserve(2 * n);
-  struct KeyHash {
-    size_t operator()(const std::pair<const char*, int>& k) const {
-      return std::hash<const void*>()(k.first) * 31u + (size_t)k.second;
+  size_t hsize = 16;
+  while (hsize < 4 * n) hsize *= 2;
+  b->ht.assign(hsize, HashSlot{nullptr, 0, 0});   // open addressing, linear probing
+  const bool want_spec = c->pair_kernel && c->spec_reuse;
+  b->chunk_host.clear();
+  b->pair_chunk_host.assign(want_spec ? 2 * (size_t)n : 0, 0);
+  int empty_cid = -1;
+  auto place = [&](const char* ptr, int len, bool bucket8192, int* cid) -> uint64_t {
+    if (len == 0) {
+      if (bucket8192) {
+        if (empty_cid < 0) {
+          empty_cid = (int)b->chunk_host.size();
+          b->chunk_host.push_back({(uint32_t)0, 0});
+        }
+        *cid = empty_cid;
+      }
+      return pool;
     }
-  };
-  std::unordered_map<std::pair<const char*, int>, uint64_t, KeyHash> seen;
-  seen.reserve(2 * n);
-  auto place = [&](const char* ptr, int len) -> uint64_t {
-    if (len == 0) return pool;
-    auto it = seen.find({ptr, len});
-    if (it != seen.end()) return it->second;
-    const uint64_t o = pool;
-    seen.emplace(std::make_pair(ptr, len), o);
-    uniq.push_back({ptr, len, o});
-    pool += ((uint64_t)len + 15) & ~15ull;
-    return o;
+    size_t h = (((uint64_t)(uintptr_t)ptr * 0x9E3779B97F4A7C15ull) ^ (uint64_t)len * 0xC2B2AE3D27D4EB4Full) >> 20;
+    int u = -1;
+    for (;; h++) {
+      HashSlot& sl = b->ht[h & (hsize - 1)];
+      if (!sl.p) {   // new chunk
+        u = (int)uniq.size();
+        sl.p = ptr;
+        sl.len = len;
+        sl.uid = (uint32_t)u;
+        uniq.push_back({ptr, len, pool, -1});
+        pool += ((uint64_t)len + 15) & ~15ull;
+        break;
+      }
+      if (sl.p == ptr && sl.len == len) {
+        u = (int)sl.uid;
+        break;
+      }
+    }
+    Src& e = uniq[u];
+    if (bucket8192) {
+      if (e.cid < 0) {
+        e.cid = (int)b->chunk_host.size();
+        b->chunk_host.push_back({(uint32_t)e.off, len});
+      }
+      *cid = e.cid;
+    }
+    return e.off;
   };
   for (size_t d = 0; d < n; d++) {
     const xc_pair& p = pairs[b->order[d]];
     const int lg = b->log2L[b->order[d]];
-    toff[d] = place(p.tseq, p.tlen);
-    qoff[d] = place(p.qseq, p.qlen);
+    const bool sp = want_spec && lg == PAIR_LOG2L;
+    int ct = 0, cq = 0;
+    toff[d] = place(p.tseq, p.tlen, sp, &ct);
+    qoff[d] = place(p.qseq, p.qlen, sp, &cq);
+    if (sp) {
+      b->pair_chunk_host[2 * d] = ct;
+      b->pair_chunk_host[2 * d + 1] = cq;
+    }
     PairDesc& D = b->desc_host[d];
     D.t_off = (uint32_t)toff[d];
     D.q_off = (uint32_t)qoff[d];
@@ -478,27 +516,7 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   b->spec = false;
   b->spec_chunks = 0;
   for (const Bucket& bk : b->buckets) {
-    if (bk.log2L != PAIR_LOG2L || !c->pair_kernel || !c->spec_reuse) continue;
-    std::unordered_map<uint64_t, int> cidx;   // pool offset -> chunk index
-    b->chunk_host.clear();
-    b->pair_chunk_host.assign(2 * (size_t)n, 0);
-    for (int d = bk.first; d < bk.first + bk.count; d++) {
-      const PairDesc& D = b->desc_host[d];
-      const uint32_t off[2] = {D.t_off, D.q_off};
-      const int len[2] = {D.tlen, D.qlen};
-      for (int k = 0; k < 2; k++) {
-        auto it = cidx.find(((uint64_t)off[k] << 20) | (uint64_t)len[k]);
-        int ci;
-        if (it != cidx.end()) {
-          ci = it->second;
-        } else {
-          ci = (int)b->chunk_host.size();
-          cidx.emplace(((uint64_t)off[k] << 20) | (uint64_t)len[k], ci);
-          b->chunk_host.push_back({off[k], len[k]});
-        }
-        b->pair_chunk_host[2 * (size_t)d + k] = ci;
-      }
-    }
+    if (bk.log2L != PAIR_LOG2L || !want_spec) continue;
     const size_t U = b->chunk_host.size();
     if ((double)(2 * bk.count) < SPEC_MIN_REUSE * (double)U) continue;
     if ((r = dev_grow(b->d_chunks, b->cap_chunks, U)) != XC_OK) return r;

@@ -17,6 +17,13 @@ struct Bucket {
   int count;
 };
 
+// Slot of the table that finds a chunk passed again by the same pointer and length.
+struct HashSlot {
+  const char* p;
+  int len;
+  uint32_t uid;
+};
+
 // Device and pinned host buffers of one packed batch of chunk pairs.  Pairs
 // are stored in "device order" (grouped by FFT length); order[d] maps a device
 // index to the caller's index.
@@ -56,6 +63,7 @@ struct Batch {
   float2* d_spec = nullptr;       size_t cap_spec = 0;
   uint32_t* d_chunkflags = nullptr; size_t cap_chunkflags = 0;
   uint64_t unique_bytes = 0;      // sequence bytes after de-duplication
+  std::vector<HashSlot> ht;       // (pointer, length) -> distinct chunk, reused across packs
   int* d_base = nullptr;          size_t cap_base = 0;
   DevResult* d_dense = nullptr;   size_t cap_dense = 0;
   float2* d_acc = nullptr;        size_t cap_acc = 0;     // channel sums of FFT lengths beyond one SM

@@ -336,12 +336,11 @@ int xc_submit(xc_ctx* c, const xc_pair* pairs, size_t n, uint64_t* ticket) {
   // chunks) is copied once, so its pairs share it downstream
   Request* q = new Request();
   size_t bytes = 0;
-  struct KeyHash {
-    size_t operator()(const std::pair<const char*, int>& k) const {
-      return std::hash<const void*>()(k.first) * 31u + (size_t)k.second;
-    }
-  };
-  std::unordered_map<std::pair<const char*, int>, size_t, KeyHash> seen;
+  size_t hsize = 16;
+  while (hsize < 4 * n) hsize *= 2;
+  std::vector<HashSlot> ht(hsize, HashSlot{nullptr, 0, 0});   // open addressing: (pointer, length) -> copy
+  std::vector<std::pair<const char*, int>> srcs;               // distinct chunks, in copy order
+  std::vector<size_t> offs;
   std::vector<std::pair<size_t, size_t>> where(n);   // byte offsets of each pair's target and query copy
   for (size_t i = 0; i < n; i++) {
     if (pairs[i].tlen < 0 || pairs[i].qlen < 0) {
@@ -358,19 +357,28 @@ int xc_submit(xc_ctx* c, const xc_pair* pairs, size_t n, uint64_t* ticket) {
       return XC_ERR_INPUT;
     }
     auto at = [&](const char* ptr, int len) -> size_t {
-      auto it = seen.find({ptr, len});
-      if (it != seen.end()) return it->second;
-      seen.emplace(std::make_pair(ptr, len), bytes);
-      bytes += (size_t)len;
-      return bytes - (size_t)len;
+      if (len == 0) return bytes;
+      for (size_t h = (((uint64_t)(uintptr_t)ptr * 0x9E3779B97F4A7C15ull) ^ (uint64_t)len * 0xC2B2AE3D27D4EB4Full) >> 20;;
+           h++) {
+        HashSlot& sl = ht[h & (hsize - 1)];
+        if (!sl.p) {
+          sl.p = ptr;
+          sl.len = len;
+          sl.uid = (uint32_t)srcs.size();
+          srcs.emplace_back(ptr, len);
+          offs.push_back(bytes);
+          bytes += (size_t)len;
+          return bytes - (size_t)len;
+        }
+        if (sl.p == ptr && sl.len == len) return offs[sl.uid];
+      }
     };
     where[i].first = at(pairs[i].tseq, pairs[i].tlen);
     where[i].second = at(pairs[i].qseq, pairs[i].qlen);
     q->footprint += pair_footprint(c, pairs[i], S->slots[0].b->slots);
   }
   q->bytes.resize(bytes);
-  for (const auto& kv : seen)
-    if (kv.first.second) memcpy(&q->bytes[kv.second], kv.first.first, (size_t)kv.first.second);
+  for (size_t k = 0; k < srcs.size(); k++) memcpy(&q->bytes[offs[k]], srcs[k].first, (size_t)srcs[k].second);
   q->pairs.assign(pairs, pairs + n);
   for (size_t i = 0; i < n; i++) {
     xc_pair& p = q->pairs[i];
