@@ -730,15 +730,25 @@ def run_ours(args):
 
 def profile_case(args):
     """Fixed device-resident workload for profiler captures: uploads --pairs
-    seeded uniform 4096x4096 chunk pairs (FFT 8192) and runs the batch --runs
-    times without timing, so a profiler's launch list maps one-to-one onto
-    runs (each run: the correlation kernels, the scan kernel and the two
-    finalize kernels)."""
+    seeded uniform 4096x4096 chunk pairs (FFT 8192), or with --case blocks
+    the pairs of 24x24 grid blocks of the genome workload, and runs the batch
+    --runs times without timing, so a profiler's launch list maps one-to-one
+    onto runs (each run: the correlation kernels, the scan kernel and the
+    two finalize kernels)."""
     import satsuma2_gb300 as sg
     from satsuma2_gb300 import build, workloads
     build.build()
-    items = workloads.uniform_batch(args.pairs, seed=SEED)
-    x = sg.XCorr(target_total=TARGET_TOTAL)
+    if args.case == "blocks":   # 24x24 grid blocks of the genome workload (spectra path)
+        tb, qb, tc, qc, blocks = genome_workload()
+        items, k = [], 0
+        while sum(len(a) for a in items) < args.pairs:
+            items.append(sg.block_pairs(tb, tc, qb, qc, *blocks[k]))
+            k += 1
+        items = np.concatenate(items)[:args.pairs]
+        x = sg.XCorr(target_total=float(len(tb)))
+    else:
+        items = workloads.uniform_batch(args.pairs, seed=SEED)
+        x = sg.XCorr(target_total=TARGET_TOTAL)
     b = x.upload(items)
     for _ in range(args.runs):
         b.run(ctypes.c_void_p(0))
@@ -760,6 +770,8 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="profiler workload only: upload --pairs pairs and run them --runs times, untimed")
     ap.add_argument("--pairs", type=int, default=N_PAIRS)
+    ap.add_argument("--case", default="uniform", choices=["uniform", "blocks"],
+                    help="profiler workload: uniform pairs, or 24x24 grid blocks of the genome workload")
     ap.add_argument("--runs", type=int, default=3)
     args = ap.parse_args()
     if args.profile_case:
