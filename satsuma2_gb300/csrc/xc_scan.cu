@@ -4,8 +4,8 @@
 //                        SeqAnalyzer::DoOne over every FindTop offset, then
 //                        FilterMatches on the raw segments.
 //     A/C/G/T pairs, in rounds of 128 diagonals (longest first):
-//       pass 1 (warp = diagonal, lane = word): on 2-bit bitplanes, 32
-//         equality bits per word op, a branch-free screen marks the words holding a 4-check
+//       pass 1 (thread = diagonal): on 2-bit bitplanes, 32 equality bits per
+//         word op, a branch-free screen marks the words holding a 4-check
 //         block whose 49-position span holds >= 19 equal bases (the eight
 //         blocks of a word tested at once in byte lanes);
 //       items: the marked words of the round laid out contiguously per
@@ -202,8 +202,6 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
   __shared__ int s_wsum[NWARP];
   __shared__ int s_next, s_res, s_qn;
   __shared__ int s_cy_start[2];
-  __shared__ int s_wfl[NT_SCAN];   // pass 1: first | last word << 16 of each diagonal of the round (-1: none)
-  __shared__ int s_nbd[NT_SCAN];   //   and its marked words
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int pidx = P.first + blockIdx.x;
@@ -519,45 +517,33 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
       const bool valid = have && clast >= cfirst;
       const int wfirst = cfirst >> 5, wlast = clast >> 5;
 
-      // ---- pass 1 (warp = diagonal, lane = word): one bit per word, 32
-      //      words per entry of wmask[q >> 5][d]; no check of an unmarked
-      //      word can pass.  The lanes of a warp read consecutive plane words
-      //      (no bank conflicts); a word's two previous equality words come
-      //      from the lanes below, or from the chunk before. ----
-      s_wfl[tid] = valid ? (wfirst | (wlast << 16)) : -1;
-      __syncthreads();
-      for (int d = warp; d < NT_SCAN; d += NWARP) {
-        const int fl = s_wfl[d];
-        int nbd = 0;
-        if (fl >= 0) {
-          const int wf = fl & 0xffff, wl = fl >> 16, p = dpos[d];
-          const int qd = (p + 32 * QPAD) >> 5, sh = (p + 32 * QPAD) & 31;
-          uint32_t c1 = eword(p, wf - 1), c2 = eword(p, wf - 2);   // the words before the diagonal's first
-          for (int w0 = wf; w0 <= wl; w0 += 32) {
-            const int w = w0 + lane;
-            uint32_t e0 = 0u;
-            if (w <= wl) {
-              const uint2 a = qb[w + qd], nx = qb[w + qd + 1], tw = tb[w];
-              e0 = ~((tw.x ^ __funnelshift_r(a.x, nx.x, sh)) | (tw.y ^ __funnelshift_r(a.y, nx.y, sh)));
-            }
-            uint32_t e1 = __shfl_up_sync(FULL, e0, 1), e2 = __shfl_up_sync(FULL, e0, 2);
-            if (lane == 0) {
-              e1 = c1;
-              e2 = c2;
-            } else if (lane == 1) {
-              e2 = c1;
-            }
-            const unsigned bal = __ballot_sync(FULL, w <= wl && screen_word(e2, e1, e0));
-            if (lane == 0) wmask[((w0 - wf) >> 5) * NT_SCAN + d] = bal;
-            nbd += __popc(bal);
-            c1 = __shfl_sync(FULL, e0, 31);
-            c2 = __shfl_sync(FULL, e0, 30);
+      // ---- pass 1 (thread = diagonal): one bit per word, 32 words per entry
+      //      of wmask[q >> 5][tid]; no check of an unmarked word can pass.
+      int nb = 0;
+      if (valid) {
+        // The query word pair of target word w is (w + qd, w + qd + 1) at bit
+        // shift sh: one new query word per step.
+        const int qd = (pos + 32 * QPAD) >> 5, sh = (pos + 32 * QPAD) & 31;
+        uint32_t e2 = eword(pos, wfirst - 2), e1 = eword(pos, wfirst - 1);
+        int qi = wfirst + qd;
+        uint2 a = qb[qi];
+        uint32_t acc = 0;
+        for (int w = wfirst; w <= wlast; w++) {
+          const uint2 nx = qb[qi + 1], tw = tb[w];
+          const uint32_t e0 = ~((tw.x ^ __funnelshift_r(a.x, nx.x, sh)) | (tw.y ^ __funnelshift_r(a.y, nx.y, sh)));
+          a = nx;
+          qi++;
+          const int q = w - wfirst;
+          acc |= (uint32_t)screen_word(e2, e1, e0) << (q & 31);
+          if ((q & 31) == 31 || w == wlast) {
+            wmask[(q >> 5) * NT_SCAN + tid] = acc;
+            nb += __popc(acc);
+            acc = 0;
           }
+          e2 = e1;
+          e1 = e0;
         }
-        if (lane == 0) s_nbd[d] = nbd;
       }
-      __syncthreads();
-      const int nb = s_nbd[tid];
       // item index of this diagonal's first marked word: CTA exclusive scan
       const int nincl = warp_incl_sum(nb, lane);
       if (lane == 31) s_wsum[warp] = nincl;
