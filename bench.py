@@ -417,7 +417,7 @@ def genome_workload(seed=SEED):
     return _GENOME[seed]
 
 
-def genome_serving(local, rates=(5000.0, 50000.0, 200000.0, 1000000.0), seconds=3.0, seed=SEED):
+def genome_serving(local, rates=(5000.0, 50000.0, 200000.0, 1000000.0, 2000000.0), seconds=3.0, seed=SEED):
     """Serving on the genome workload: a 20 Mb target (GC 41%) and a query
     derived from it at 80% identity with 30 inversions, 20 segmental
     duplications and 10% novel insertions, chunked as the slave chunks them
