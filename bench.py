@@ -679,7 +679,7 @@ def run_ours(args):
     if os.path.exists(tpath):
         with open(tpath) as f:
             counters = json.load(f)
-        traffic = counters.get("corr_pair_kernel_dram_bytes_per_launch")
+        traffic = counters.get("corr_pair2_kernel_dram_bytes_per_launch")
     checks = checks_per_pair * N_PAIRS
     # the same algorithmic work on 24x24 grid blocks, where the spectra path
     # transforms each distinct chunk once
