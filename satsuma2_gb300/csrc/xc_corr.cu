@@ -82,16 +82,18 @@ __device__ __forceinline__ void hermitian_pack(float2* __restrict__ buf, const S
 // inverse in buf, for one strand: xc[i] = r[(i + N) mod L] / N; envelope
 // over 256-sample blocks when L/256 > 8; keep i with xc[i] > env*cutoff + 1
 // in increasing i.  Threads t < NTF; warp w of them owns the contiguous
-// range [w*L/(NTF/32), (w+1)*L/(NTF/32)), lanes stride by one.  Every thread
-// of the barrier's group calls it (two barriers).  s_warp holds 2 * NTF/32
-// ints.  scale is 1/N for an inverse of the spectrum itself (a power of two
-// smaller when the inverse carries a power-of-two factor).
+// range [w*L/(NTF/32), (w+1)*L/(NTF/32)) in steps of 64 lags, lane l taking
+// lags 2l and 2l+1 of a step (one complex value of the inverse).  Every
+// thread of the barrier's group calls it (two barriers).  s_warp holds
+// 2 * NTF/32 ints.  scale is 1/N for an inverse of the spectrum itself (a
+// power of two smaller when the inverse carries a power-of-two factor).
 //
 // Near-threshold lags: with P.strad_cnt set, every lag whose FP32 value lies
 // within straddle_rel(L) * max(1, max|xc|) of its FP32 threshold is counted
 // in strad_cnt[pair*2+strand] and the first STRAD_CAP of them are listed.
 // There the reference's FP32 FFT and this one may decide differently; every
-// other lag's decision is the same for both.
+// other lag's decision is the same for both.  A warp walks its lags for
+// them only when one of its lanes saw a lag that close.
 template <int LOG2L, int NTF = NT_CORR, class SY = CtaBarrier, int KMAX = (NTF <= 256 ? 32 : 16)>
 __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, uint32_t off_base, int pidx,
                                          int strand, const float2* __restrict__ buf, int t, int* s_warp,
@@ -101,41 +103,49 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
   constexpr int NW = NTF / 32;   // warps of the group
   const int lane = t & 31, warp = t >> 5;
   constexpr int PER_WARP = L / NW;
-  constexpr int ITER = PER_WARP / 32;
+  constexpr int ITER = PER_WARP / 64;   // steps of 64 lags
+  static_assert(PER_WARP % 64 == 0, "a warp's range is whole steps");
+  constexpr bool ENV = L / 256 > 8;
+  static_assert(!ENV || PER_WARP % 256 == 0, "envelope blocks lie within one warp's range");
   const int wbase = warp * PER_WARP;
-  auto xval = [&](int i) -> float {
-    const int n = (i + N) & (L - 1);
+  // lags wbase + 64 e + 2 lane and the one after (even n: one complex value)
+  auto xpair = [&](int e) -> float2 {
+    const int n = (wbase + 64 * e + 2 * lane + N) & (L - 1);
     const float2 z = buf[swz(n >> 1)];
-    return ((n & 1) ? z.y : z.x) * scale;
+    return make_float2(z.x * scale, z.y * scale);
   };
-  // Up to KMAX values a lane's values stay in registers across the three
-  // passes (envelope, count, compaction); more are re-read from the buffer.
-  constexpr bool KEEP = ITER <= KMAX;
-  float xs[KEEP ? ITER : 1];
+  // Up to KMAX values a lane's values stay in registers across the passes
+  // (envelope, count, compaction); more are re-read from the buffer.
+  constexpr bool KEEP = 2 * ITER <= KMAX;
+  float2 xs[KEEP ? ITER : 1];
   if constexpr (KEEP) {
 #pragma unroll
-    for (int e = 0; e < ITER; e++) xs[e] = xval(wbase + e * 32 + lane);
+    for (int e = 0; e < ITER; e++) xs[e] = xpair(e);
   }
-  auto xat = [&](int e) -> float {
+  auto xat = [&](int e) -> float2 {
     if constexpr (KEEP) return xs[e];
-    else return xval(wbase + e * 32 + lane);
+    else return xpair(e);
   };
-  float thrb[PER_WARP >= 256 ? PER_WARP / 256 : 1];
-  if constexpr (L / 256 > 8) {
+  float thrb[ENV ? PER_WARP / 256 : 1];
+  if constexpr (ENV) {
     const float cut = (float)((flags & PF_FAST) ? P.cutoff_fast : P.cutoff);
 #pragma unroll
     for (int bb = 0; bb < PER_WARP / 256; bb++) {
       // squares are float products as in the reference; compensated FP32
-      // sum per lane, pairwise across the warp
+      // sum per lane (its eight lags of the block), pairwise across the warp
       float s = 0.f, comp = 0.f;
 #pragma unroll
-      for (int e = 0; e < 8; e++) {
-        const float x = xat(bb * 8 + e);
-        const float v = __fmul_rn(x, x);
-        const float y = __fsub_rn(v, comp);
-        const float t2 = __fadd_rn(s, y);
-        comp = __fsub_rn(__fsub_rn(t2, s), y);
-        s = t2;
+      for (int e = 0; e < 4; e++) {
+        const float2 x2 = xat(bb * 4 + e);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const float x = h ? x2.y : x2.x;
+          const float v = __fmul_rn(x, x);
+          const float y = __fsub_rn(v, comp);
+          const float t2 = __fadd_rn(s, y);
+          comp = __fsub_rn(__fsub_rn(t2, s), y);
+          s = t2;
+        }
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -154,19 +164,26 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
   } else {
     thrb[0] = 1.0f;
   }
+  auto thr_of = [&](int e) -> float { return thrb[ENV ? (e >> 2) : 0]; };
   int wcount = 0;
-  float amax = 0.f;   // max |xc| of the lane's lags (for the near-threshold band)
-  constexpr bool KEEPM = KEEP && ITER <= 16;   // ballots kept too (registers allowing)
-  unsigned msk[KEEPM ? ITER : 1];
+  float amax = 0.f;      // max |xc| of the lane's lags (for the near-threshold band)
+  float dmin = 3.0e38f;  // min |xc - threshold| of the lane's lags
+  constexpr bool KEEPM = KEEP && ITER <= 8;   // ballots kept too (registers allowing)
+  unsigned msk[KEEPM ? 2 * ITER : 1];
 #pragma unroll(KEEP ? ITER : 4)
   for (int e = 0; e < ITER; e++) {
-    const int i = wbase + e * 32 + lane;
-    const float x = xat(e);
-    const unsigned m = __ballot_sync(0xffffffffu, x > thrb[(L / 256 > 8) ? (e >> 3) : 0]);
-    if constexpr (KEEPM) msk[e] = m;
-    wcount += __popc(m);
-    amax = fmaxf(amax, fabsf(x));
-    if (P.dbg_xc) P.dbg_xc[(size_t)(pidx * 2 + strand) * L + i] = x;
+    const float2 x = xat(e);
+    const float thr = thr_of(e);
+    const unsigned me = __ballot_sync(0xffffffffu, x.x > thr), mo = __ballot_sync(0xffffffffu, x.y > thr);
+    if constexpr (KEEPM) {
+      msk[2 * e] = me;
+      msk[2 * e + 1] = mo;
+    }
+    wcount += __popc(me) + __popc(mo);
+    amax = fmaxf(amax, fmaxf(fabsf(x.x), fabsf(x.y)));
+    dmin = fminf(dmin, fminf(fabsf(x.x - thr), fabsf(x.y - thr)));
+    if (P.dbg_xc)
+      *reinterpret_cast<float2*>(P.dbg_xc + (size_t)(pidx * 2 + strand) * L + wbase + 64 * e + 2 * lane) = x;
   }
   int* s_max = s_warp + NW;   // max |xc| bits per warp (non-negative floats order as ints)
   if (P.strad_cnt) {
@@ -199,21 +216,40 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
   const unsigned lt = (1u << lane) - 1u;
 #pragma unroll(KEEP ? ITER : 4)
   for (int e = 0; e < ITER; e++) {
-    const int i = wbase + e * 32 + lane;
-    const float thr = thrb[(L / 256 > 8) ? (e >> 3) : 0];
-    unsigned m;
-    if constexpr (KEEPM) m = msk[e];
-    else m = __ballot_sync(0xffffffffu, xat(e) > thr);
-    if ((m >> lane) & 1u) out[run + __popc(m & lt)] = i;
-    run += __popc(m);
-    if (P.strad_cnt) {
-      const unsigned nm = __ballot_sync(0xffffffffu, fabsf(xat(e) - thr) <= band);
-      if (nm) {
+    const int i = wbase + 64 * e + 2 * lane;
+    unsigned me, mo;
+    if constexpr (KEEPM) {
+      me = msk[2 * e];
+      mo = msk[2 * e + 1];
+    } else {
+      const float2 x = xat(e);
+      const float thr = thr_of(e);
+      me = __ballot_sync(0xffffffffu, x.x > thr);
+      mo = __ballot_sync(0xffffffffu, x.y > thr);
+    }
+    const unsigned be = (me >> lane) & 1u;
+    const int k = run + __popc(me & lt) + __popc(mo & lt);
+    if (be) out[k] = i;
+    if ((mo >> lane) & 1u) out[k + (int)be] = i + 1;
+    run += __popc(me) + __popc(mo);
+  }
+  if (__any_sync(0xffffffffu, dmin <= band)) {
+#pragma unroll(KEEP ? ITER : 4)
+    for (int e = 0; e < ITER; e++) {
+      const float2 x = xat(e);
+      const float thr = thr_of(e);
+      const unsigned ne = __ballot_sync(0xffffffffu, fabsf(x.x - thr) <= band);
+      const unsigned no = __ballot_sync(0xffffffffu, fabsf(x.y - thr) <= band);
+      if (ne | no) {
         int base = 0;
-        if (lane == 0) base = atomicAdd(&P.strad_cnt[pidx * 2 + strand], __popc(nm));
+        if (lane == 0) base = atomicAdd(&P.strad_cnt[pidx * 2 + strand], __popc(ne) + __popc(no));
         base = __shfl_sync(0xffffffffu, base, 0);
-        const int k = base + __popc(nm & lt);
-        if (((nm >> lane) & 1u) && k < STRAD_CAP) P.strad_list[(size_t)(pidx * 2 + strand) * STRAD_CAP + k] = i;
+        const unsigned be = (ne >> lane) & 1u;
+        const int k = base + __popc(ne & lt) + __popc(no & lt);
+        const int i = wbase + 64 * e + 2 * lane;
+        int* lst = P.strad_list + (size_t)(pidx * 2 + strand) * STRAD_CAP;
+        if (be && k < STRAD_CAP) lst[k] = i;
+        if (((no >> lane) & 1u) && k + (int)be < STRAD_CAP) lst[k + (int)be] = i + 1;
       }
     }
   }
@@ -1058,6 +1094,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
   float4* vv = reinterpret_cast<float4*>(Eq + NWIN);   // [sequence][window]: c0 (w=0, w=1), c1 (w=0, w=1)
   uint32_t* cw = reinterpret_cast<uint32_t*>(vv + 2 * NWIN);   // [sequence][g]
   __shared__ int s_cnt4[8];
+  __shared__ unsigned s_flags;     // bit 0: a byte >= 128; bit 1: a byte other than A, C, G, T
   __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
   __shared__ Split3 s_wf[2][8];    // the same as three floats each
   __shared__ int s_warp[2][2 * 256 / 32];
@@ -1083,32 +1120,78 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
     const int T = P.pairs[pidx].tlen, Q = P.pairs[pidx].qlen;
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     if (tid < 8) s_cnt4[tid] = 0;
-    __syncthreads();
+    if (tid == 0) s_flags = 0u;
+    __syncthreads();   // the chunk bytes are in; the counters are zero
 
-    // ---- 1. byte checks on this thread's 16-byte piece (zero past the end):
-    //      per byte, exactly, (y & 0x7f) + 0x7f | y has bit 7 clear iff y == 0 ----
-    int high = 0, nonacgt = 0;
+    // ---- 1. thread (G, g) takes bytes 16g..16g+15 of sequence G, which are
+    //      also its entropy window (WIN = 16): byte checks (per byte,
+    //      exactly, (y & 0x7f) + 0x7f | y has bit 7 clear iff y == 0), the
+    //      2-bit codes (A=0 C=1 G=2 T=3), base counts for the channel means
+    //      (SeqToPCM, CrossCorr.cc:108-116) and the window's entropy weight
+    //      (CCSignal::ComputeEntropy, CrossCorr.cc:35-93).  Bytes past the
+    //      chunk end (zero) are masked out. ----
+    uint32_t* cwin = reinterpret_cast<uint32_t*>(vv);   // [sequence][window] codes; vv is free until step 3a
     {
-      const int which = tid >> 8, c = tid & 255;
-      const int valid = (which ? Q : T) - 16 * c;
-      const uint4 v = *reinterpret_cast<const uint4*>((which ? sq : st) + 16 * c);
+      const int len = G ? Q : T;
+      const int valid = len - 16 * g;
+      const uint8_t* sb = G ? sq : st;
+      const uint4 v = *reinterpret_cast<const uint4*>(sb + 16 * g);
       const uint32_t x[4] = {v.x, v.y, v.z, v.w};
       auto nz = [](uint32_t y) { return (((y & 0x7f7f7f7fu) + 0x7f7f7f7fu) | y) & 0x80808080u; };
+      uint32_t high = 0u, bad = 0u, p0 = 0u, p1 = 0u, codes = 0u;
 #pragma unroll
       for (int k = 0; k < 4; k++) {
         const int vk = min(max(valid - 4 * k, 0), 4);
         const uint32_t m = vk >= 4 ? 0xffffffffu : (1u << (8 * vk)) - 1u;
-        high |= (x[k] & m & 0x80808080u) != 0u;
-        const uint32_t bad = nz(x[k] ^ 0x41414141u) & nz(x[k] ^ 0x43434343u) & nz(x[k] ^ 0x47474747u) &
-                             nz(x[k] ^ 0x54545454u);   // bit 7: byte is not A, C, G or T
-        nonacgt |= (bad & m & 0x80808080u) != 0u;
+        high |= x[k] & m & 0x80808080u;
+        bad |= nz(x[k] ^ 0x41414141u) & nz(x[k] ^ 0x43434343u) & nz(x[k] ^ 0x47474747u) & nz(x[k] ^ 0x54545454u) &
+               m & 0x80808080u;   // bit 7: byte is not A, C, G or T
+        const uint32_t cd = ((x[k] >> 1) ^ (x[k] >> 2)) & 0x03030303u & m;
+        p0 |= (((cd & 0x01010101u) * 0x10204080u) >> 28) << (4 * k);          // bit j: code bit 0 of byte j
+        p1 |= ((((cd >> 1) & 0x01010101u) * 0x10204080u) >> 28) << (4 * k);   // bit j: code bit 1
+        const uint32_t c2 = cd | (cd >> 6);   // codes of bytes 0, 1 in bits 0-3, of bytes 2, 3 in bits 16-19
+        codes |= ((c2 & 0xfu) | ((c2 >> 12) & 0xf0u)) << (8 * k);
+      }
+      cwin[tid] = codes;
+      const int nv = min(max(valid, 0), 16);
+      const int nt = __popc(p0 & p1), nc = __popc(p0) - nt, ng = __popc(p1) - nt, na = nv - nc - ng - nt;
+      float E = 0.f;
+      if (len < 1024) {
+        E = 1.f;
+      } else if (nv == 16) {
+        E = __ldg(&P.tab.ent_acgt[(na * (WIN + 1) + nc) * (WIN + 1) + ng]);
+      } else if (nv > 0) {
+        int a4 = 0, c4 = 0, g4 = 0, t4 = 0;
+        for (int j = 0; j < nv; j++) {
+          const uchar4 q = c_w4q[sb[16 * g + j]];
+          a4 += q.x; c4 += q.y; g4 += q.z; t4 += q.w;
+        }
+        const double* et = P.tab.ent + nv * (4 * WIN + 1);
+        const double sv =
+            __dadd_rn(__dadd_rn(__dadd_rn(__ldg(et + a4), __ldg(et + c4)), __ldg(et + g4)), __ldg(et + t4));
+        E = __double2float_rn(-sv);
+        if (E < 0.f) E = 0.f;
+      }
+      (G ? Eq : Et)[g] = E;
+      // counts in 16-bit fields (at most 16 x 32 per warp), four quarter
+      // units per base
+      const uint32_t lo = __reduce_add_sync(0xffffffffu, (uint32_t)na | ((uint32_t)nc << 16));
+      const uint32_t hi = __reduce_add_sync(0xffffffffu, (uint32_t)ng | ((uint32_t)nt << 16));
+      const uint32_t fl = __reduce_or_sync(0xffffffffu, (high ? 1u : 0u) | (bad ? 2u : 0u));
+      if ((tid & 31) == 0) {
+        atomicAdd(&s_cnt4[4 * G + 0], 4 * (int)(lo & 0xffffu));
+        atomicAdd(&s_cnt4[4 * G + 1], 4 * (int)(lo >> 16));
+        atomicAdd(&s_cnt4[4 * G + 2], 4 * (int)(hi & 0xffffu));
+        atomicAdd(&s_cnt4[4 * G + 3], 4 * (int)(hi >> 16));
+        if (fl) atomicOr(&s_flags, fl);
       }
     }
-    const int any_high = __syncthreads_or(high);
-    const int generic = __syncthreads_or(nonacgt);
-    if (any_high || generic || (Q >= 1024 && Q % WIN != 0) || P.dbg_sig) {
+    __syncthreads();   // the chunk bytes are no longer read: the next pair's may come in
+    if (next >= 0) pair2_prefetch(P, next, st, sq, tid);
+    const uint32_t flg = s_flags;
+    if ((flg & 1u) || (flg & 2u) || (Q >= 1024 && Q % WIN != 0) || P.dbg_sig) {
       if (tid == 0) {
-        if (any_high) {
+        if (flg & 1u) {
           P.off_cnt[pidx * 2] = 0;
           P.off_cnt[pidx * 2 + 1] = 0;
           P.pair_flags[pidx] = PF_INVALID;
@@ -1116,66 +1199,12 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
           P.fb_list[atomicAdd(P.fb_cnt, 1)] = pidx;   // the per-strand kernel takes it
         }
       }
-      if (next >= 0) pair2_prefetch(P, next, st, sq, tid);   // the bytes were read before the barriers above
+      __syncthreads();   // cwin (in vv) and the flags are reused by the next pair
       continue;
     }
     if (tid == 0) P.pair_flags[pidx] = P.pairs[pidx].flags & PF_FAST;
-
-    // ---- 2a. entropy weight per window (CCSignal::ComputeEntropy,
-    //      CrossCorr.cc:35-93): group 0 target windows, group 1 query ----
-    {
-      const uint8_t* sb = G ? sq : st;
-      const int len = G ? Q : T;
-      float E = 0.f;
-      if (len < 1024) {
-        E = 1.f;
-      } else if (g * WIN + WIN <= len) {
-        const int i0 = g * WIN;
-        uint32_t cnt = 0;
-        for (int j = 0; j < WIN; j++) cnt += 1u << (8 * code_of(sb[i0 + j]));
-        const int a = cnt & 255u, c = (cnt >> 8) & 255u, gg = (cnt >> 16) & 255u;
-        E = __ldg(&P.tab.ent_acgt[(a * (WIN + 1) + c) * (WIN + 1) + gg]);
-      } else if (g * WIN < len) {
-        const int i0 = g * WIN;
-        const int k = len - i0;
-        int a4 = 0, c4 = 0, g4 = 0, t4 = 0;
-        for (int j = 0; j < k; j++) {
-          const uchar4 q = c_w4q[sb[i0 + j]];
-          a4 += q.x; c4 += q.y; g4 += q.z; t4 += q.w;
-        }
-        const double* et = P.tab.ent + k * (4 * WIN + 1);
-        const double sv =
-            __dadd_rn(__dadd_rn(__dadd_rn(__ldg(et + a4), __ldg(et + c4)), __ldg(et + g4)), __ldg(et + t4));
-        E = __double2float_rn(-sv);
-        if (E < 0.f) E = 0.f;
-      }
-      (G ? Eq : Et)[g] = E;
-    }
-    // ---- 2b. base counts for the channel means (SeqToPCM, CrossCorr.cc:108-116),
-    //      and the 2-bit codes of positions g + 256 r in one word per thread ----
-    {
-      uint32_t ct = 0, cq = 0;   // one 8-bit count field per base, at most N / 512 each
-      for (int i = tid; i < N; i += NT_PAIR2) {
-        if (i < T) ct += 1u << (8 * code_of(st[i]));
-        if (i < Q) cq += 1u << (8 * code_of(sq[i]));
-      }
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        const int vt = __reduce_add_sync(0xffffffffu, 4 * (int)((ct >> (8 * k)) & 255u));
-        const int vq = __reduce_add_sync(0xffffffffu, 4 * (int)((cq >> (8 * k)) & 255u));
-        if ((tid & 31) == 0) {
-          if (vt) atomicAdd(&s_cnt4[k], vt);
-          if (vq) atomicAdd(&s_cnt4[4 + k], vq);
-        }
-      }
-      const uint8_t* sb = G ? sq : st;
-      uint32_t w = 0;
-#pragma unroll
-      for (int r = 0; r < 16; r++) w |= code_of(sb[g + 256 * r]) << (2 * r);
-      cw[tid] = w;
-    }
-    __syncthreads();   // the chunk bytes are no longer read: the next pair's may come in
-    if (next >= 0) pair2_prefetch(P, next, st, sq, tid);
+    // ---- 2. channel means (FP64, as the reference) and the codes of
+    //      positions g + 256 r, one word per thread ----
     if (tid < 8) {
       const int len = (tid >> 2) ? Q : T;
       const double off = len > 0 ? __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len) : 0.0;
@@ -1183,6 +1212,14 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
       s_wmo[1][tid] = __dsub_rn(1.0, off);
       s_wf[0][tid] = split3(s_wmo[0][tid]);
       s_wf[1][tid] = split3(s_wmo[1][tid]);
+    }
+    {
+      const uint32_t* cs = cwin + G * NWIN + (g >> 4);
+      const int sh = 2 * (g & 15);
+      uint32_t w = 0;
+#pragma unroll
+      for (int r = 0; r < 16; r++) w |= ((cs[16 * r] >> sh) & 3u) << (2 * r);
+      cw[tid] = w;
     }
     __syncthreads();
 
