@@ -347,11 +347,17 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
       if (!P.ptable) {
         // FP32 screen on the z-score (pm*N - hits) / sd: reject only past a
         // threshold set on the host with a margin far beyond FP32 error;
-        // anything else goes to the exact test.
-        const float Nf = (float)len, gq = (float)gQ, gtf = (float)gT / Nf;
-        const float pm = (gq * gtf + (Nf - gq) * (1.f - gtf)) / Nf * 0.5f;
-        const float sg = sqrtf(pm * (1.f - pm) * Nf);
-        if (pm * Nf - (float)hits > P.screen_z * sg) return;
+        // anything else goes to the exact test.  With A = gQ gT + (N-gQ)(N-gT),
+        // pm N = A / 2N and sd^2 = A (2N^2 - A) / 4N^3, so the test is
+        // D = A - 2N hits > z sqrt(A (2N^2 - A) / N), squared without
+        // divisions (A = 0: sd = 0, left to the exact test).
+        const int A = gQ * gT + (len - gQ) * (len - gT);
+        if (A > 0) {
+          const float D = (float)(A - 2 * len * hits);
+          const float Lf = D * D * (float)len;
+          const float R = P.screen_z * P.screen_z * (float)A * (float)(2 * len * len - A);
+          if (P.screen_z >= 0.f ? (D > 0.f && Lf > R) : (D >= 0.f || Lf < R)) return;
+        }
       }
       matches = (double)hits;
       gcT = (double)gT;
@@ -525,23 +531,25 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
         // shift sh: one new query word per step.
         const int qd = (pos + 32 * QPAD) >> 5, sh = (pos + 32 * QPAD) & 31;
         uint32_t e2 = eword(pos, wfirst - 2), e1 = eword(pos, wfirst - 1);
-        int qi = wfirst + qd;
-        uint2 a = qb[qi];
-        uint32_t acc = 0;
-        for (int w = wfirst; w <= wlast; w++) {
-          const uint2 nx = qb[qi + 1], tw = tb[w];
-          const uint32_t e0 = ~((tw.x ^ __funnelshift_r(a.x, nx.x, sh)) | (tw.y ^ __funnelshift_r(a.y, nx.y, sh)));
-          a = nx;
-          qi++;
-          const int q = w - wfirst;
-          acc |= (uint32_t)screen_word(e2, e1, e0) << (q & 31);
-          if ((q & 31) == 31 || w == wlast) {
-            wmask[(q >> 5) * NT_SCAN + tid] = acc;
-            nb += __popc(acc);
-            acc = 0;
+        const uint2* qp = qb + wfirst + qd;
+        const uint2* tp = tb + wfirst;
+        uint2 a = qp[0];
+        const int nw = wlast - wfirst + 1;
+        for (int q0 = 0; q0 < nw; q0 += 32) {
+          const int m = min(32, nw - q0);
+          uint32_t acc = 0;
+#pragma unroll 4
+          for (int q = 0; q < m; q++) {
+            const uint2 nx = qp[q0 + q + 1], tw = tp[q0 + q];
+            const uint32_t e0 = ~((tw.x ^ __funnelshift_r(a.x, nx.x, sh)) | (tw.y ^ __funnelshift_r(a.y, nx.y, sh)));
+            a = nx;
+            acc = __funnelshift_r(acc, screen_word(e2, e1, e0) ? 1u : 0u, 1);   // in at bit 31
+            e2 = e1;
+            e1 = e0;
           }
-          e2 = e1;
-          e1 = e0;
+          acc >>= 32 - m;   // bit q: word q0 + q
+          wmask[(q0 >> 5) * NT_SCAN + tid] = acc;
+          nb += __popc(acc);
         }
       }
       // item index of this diagonal's first marked word: CTA exclusive scan
