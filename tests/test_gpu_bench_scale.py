@@ -14,8 +14,9 @@ For each configuration the batch is uploaded and run as bench.py runs it
 * the correlation is within 1e-3 of FP64 (relative to the peak) on a sample.
 
 Configurations: the 4096-pair uniform batch (seed 42, the benchmark's), 2000
-pairs of the uneven-length batch (FFT 1024-8192) and 200 pairs of 16384 bp at
-FFT 32768.  With SATSUMA2_PARITY_REPORT=<path> the figures are written there
+pairs of the uneven-length batch (FFT 1024-8192), four 24x24 grid blocks of
+the genome workload (2304 pairs with chunk coordinates, through the spectra
+path) and 200 pairs of 16384 bp at FFT 32768.  With SATSUMA2_PARITY_REPORT=<path> the figures are written there
 as JSON (profiles/parity_bench_configs.json is that file from a GB300 run)."""
 import json
 import os
@@ -40,8 +41,14 @@ def O():
     return oracle.Oracle()
 
 
-def _check_batch(O, x, items, L_of, P, target_total, cutoff=1.8, n_xc_sample=48):
-    b = x.upload(items)
+def _check_batch(O, x, items, L_of, P, target_total, cutoff=1.8, n_xc_sample=48, upload=None, pair_of=None,
+                 launches=None):
+    """items: (t, q) byte pairs; upload: what to upload instead (a chunk-pair
+    array of the same pairs); pair_of(k): oracle pair fields of pair k
+    (chunk coordinates) besides t and q; launches: the batch's kernel count."""
+    b = x.upload(items if upload is None else upload)
+    if launches is not None:
+        assert b.launches() == launches
     b.run()
     res, counts = b.results(with_counts=True)
     offs = b.offsets()
@@ -63,7 +70,7 @@ def _check_batch(O, x, items, L_of, P, target_total, cutoff=1.8, n_xc_sample=48)
             diff_n += len(diff)
             if diff and near_cnt[k, s] <= near_lags.shape[2]:
                 not_listed += len(diff - set(near_lags[k, s][:near_cnt[k, s]].tolist()))
-        want, _ = O.align_pair(P(L), O.pair(t, q), offsets_in=offs[k])
+        want, _ = O.align_pair(P(L), O.pair(t, q, **(pair_of(k) if pair_of else {})), offsets_in=offs[k])
         mine = res[starts[k]:starts[k + 1]]
         ok = parity.same_results(mine, want, target_total=target_total)
         return diff_n, not_listed, ok
@@ -120,6 +127,37 @@ def test_uneven_2000_vs_oracle(O):
     x.close()
     assert fig["offsets_differing_from_fp64"] <= max(8, fig["pairs"] // 100), fig
     _report("uneven_2000_fft1024_8192", fig)
+
+
+def test_grid_blocks_vs_oracle(O):
+    """Config 3: the first four 24x24 blocks of the genome workload in
+    grid-search order, uploaded as chunk-pair arrays into the genome buffers
+    (chunks shared within a block: the spectra path), records with their
+    chunk coordinates and reverse-strand query positions."""
+    import satsuma2_gb300 as sg
+    t, q, (src, _) = W.serving_genomes(seed=SEED, with_map=True)
+    tb, qb = np.frombuffer(t, np.uint8), np.frombuffer(q, np.uint8)
+    tc = np.array(W.chunk_starts(len(t), 4096, 1024), np.int64)
+    qc = np.array(W.chunk_starts(len(q), 4096, 0), np.int64)
+    blocks = W.grid_search_blocks(src, len(tc), len(qc))[:4]
+    arr = np.concatenate([sg.block_pairs(tb, tc, qb, qc, *blk) for blk in blocks])
+    base_t, base_q = tb.ctypes.data, qb.ctypes.data
+    items = [(t[a - base_t:a - base_t + lt], q[c - base_q:c - base_q + lq])
+             for a, lt, c, lq in zip(arr["tseq"].tolist(), arr["tlen"].tolist(), arr["qseq"].tolist(),
+                                     arr["qlen"].tolist())]
+
+    def pair_of(k):
+        return {"t_chunk_start": int(arr["t_chunk_start"][k]), "q_chunk_start": int(arr["q_chunk_start"][k]),
+                "query_size": int(arr["query_size"][k])}
+
+    TT = float(len(t))
+    x = sg.XCorr(target_total=TT)
+    # spectra kernel, correlation from spectra, hand-back, scan, two finalize kernels
+    fig = _check_batch(O, x, items, lambda t, q: 8192, lambda L: O.params(target_total=TT), TT,
+                       upload=arr, pair_of=pair_of, launches=6)
+    x.close()
+    assert fig["offsets_differing_from_fp64"] <= max(8, fig["pairs"] // 100), fig
+    _report("grid_blocks_4x576_fft8192_spectra", fig)
 
 
 def test_large_200_fft32768_vs_oracle(O):
