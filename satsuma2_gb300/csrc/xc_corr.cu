@@ -42,14 +42,16 @@ size_t corr_smem_bytes(int log2L) {
 // ---------------------------------------------------------------------------
 
 // Step 4: the half-length complex array of the Hermitian sum S (bins
-// k = 0..N of the L-point spectrum, N = L/2, given by S(k)), ready for the
-// N-point inverse: Z(k) = E(k) + i O(k), E = (S(k) + conj S(N-k))/2,
-// O = (S(k) - conj S(N-k)) conj(W_L^k)/2; the inverse then holds
-// z[m] = r[2m] + i r[2m+1].  Threads t < NTF.  HALF = 0.5f as written; the
-// both-strands pair kernel passes 1.0f (its inverse then carries a power of
-// two, which FindTop's scale removes exactly).
+// k = 0..N of the L-point spectrum, N = L/2; S2(k, a, b) gives a = S(k) and
+// b = S(N-k)), ready for the N-point inverse: Z(k) = E(k) + i O(k),
+// E = (S(k) + conj S(N-k))/2, O = (S(k) - conj S(N-k)) conj(W_L^k)/2; the
+// inverse then holds z[m] = r[2m] + i r[2m+1].  W_L^(N-k) = -conj(W_L^k)
+// (W_L^N = -1), so one twiddle serves both bins.  Threads t < NTF.
+// HALF = 0.5f as written; the both-strands pair kernel passes 1.0f (its
+// inverse then carries a power of two, which FindTop's scale removes
+// exactly).
 template <int LOG2L, int NTF = NT_CORR, class SF>
-__device__ __forceinline__ void hermitian_pack(float2* __restrict__ buf, const SF& S, const float2* twLh,
+__device__ __forceinline__ void hermitian_pack(float2* __restrict__ buf, const SF& S2, const float2* twLh,
                                                const float2* twLl, int t, float HALF = 0.5f) {
   constexpr int N = 1 << (LOG2L - 1);
   constexpr int LOG2N = LOG2L - 1;
@@ -59,12 +61,13 @@ __device__ __forceinline__ void hermitian_pack(float2* __restrict__ buf, const S
   for (int it = 0; it <= N / (2 * NTF); it++) {
     const int k = t + NTF * it;
     if (k > N / 2) break;
-    const float2 Sk = S(k);
-    const float2 Sn = S(N - k);
+    float2 Sk, Sn;
+    S2(k, Sk, Sn);
+    const float2 w = tw2(twLh, twLl, k);   // W_L^k
     {
       const float2 Ev = make_float2(HALF * (Sk.x + Sn.x), HALF * (Sk.y - Sn.y));
       const float2 Dv = make_float2(HALF * (Sk.x - Sn.x), HALF * (Sk.y + Sn.y));
-      const float2 Ov = cmulc(Dv, tw2(twLh, twLl, k));
+      const float2 Ov = cmulc(Dv, w);
       buf[la ^ lp<LOG2N>(NTF * it)] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
     }
     if (k != 0 && k != N / 2) {
@@ -72,10 +75,24 @@ __device__ __forceinline__ void hermitian_pack(float2* __restrict__ buf, const S
       const int pb = t ? (lb ^ lp<LOG2N>(N - NTF * (it + 1))) : lp<LOG2N>(N - NTF * it);
       const float2 Ev = make_float2(HALF * (Sn.x + Sk.x), HALF * (Sn.y - Sk.y));
       const float2 Dv = make_float2(HALF * (Sn.x - Sk.x), HALF * (Sn.y + Sk.y));
-      const float2 Ov = cmulc(Dv, tw2(twLh, twLl, N - k));
+      const float2 Ov = cmulc(Dv, make_float2(-w.x, w.y));   // W_L^(N-k)
       buf[pb] = make_float2(Ev.x - Ov.y, Ev.y + Ov.x);
     }
   }
+}
+
+// S2 for hermitian_pack from a per-bin S(k).
+template <int N, class SF>
+struct BothBins {
+  const SF& S;
+  __device__ __forceinline__ void operator()(int k, float2& a, float2& b) const {
+    a = S(k);
+    b = S(N - k);
+  }
+};
+template <int N, class SF>
+__device__ __forceinline__ BothBins<N, SF> both_bins(const SF& S) {
+  return BothBins<N, SF>{S};
 }
 
 // Step 5: FindTop (SeqAnalyzer::FindTop, CrossCorr.cc:878-944) over the
@@ -168,7 +185,7 @@ __device__ __forceinline__ void find_top(const CorrParams& P, uint32_t flags, ui
   int wcount = 0;
   float amax = 0.f;      // max |xc| of the lane's lags (for the near-threshold band)
   float dmin = 3.0e38f;  // min |xc - threshold| of the lane's lags
-  constexpr bool KEEPM = KEEP && ITER <= 8;   // ballots kept too (registers allowing)
+  constexpr bool KEEPM = KEEP && ITER <= 16;   // ballots kept too (registers allowing)
   unsigned msk[KEEPM ? 2 * ITER : 1];
 #pragma unroll(KEEP ? ITER : 4)
   for (int e = 0; e < ITER; e++) {
@@ -612,7 +629,7 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
     if constexpr (SEQ) return (k & 1) ? gaccO[k >> 1] : gaccE[k >> 1];
     return (k & 1) ? accO[k >> 1] : accE[k >> 1];
   };
-  hermitian_pack<LOG2L, NT>(bufE, S, twLh, twLl, tid);
+  hermitian_pack<LOG2L, NT>(bufE, both_bins<N>(S), twLh, twLl, tid);
   __syncthreads();
   fft_inverse<LOG2N>(bufE, twNh, twNl, tid, NT);
 
@@ -928,19 +945,18 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
   //      target-only bins are the same for both strands ----
   float2* buf = half ? WE : ZE;
   if (half == 0) {
-    hermitian_pack<LOG2L, NT_CORR>(ZE, [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; }, twLh, twLl,
-                          ht);
+    auto SF = [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; };
+    hermitian_pack<LOG2L, NT_CORR>(ZE, both_bins<N>(SF), twLh, twLl, ht);
   } else {
-    hermitian_pack<LOG2L, NT_CORR>(WE,
-                          [&](int k) -> float2 {
-                            if (k >= N - 1) return (k & 1) ? aFO[k >> 1] : aFE[k >> 1];
-                            const float2 r = (k & 1) ? aRO[k >> 1] : aRE[k >> 1];
-                            const int j = ((Q - 1) * k) & (L - 1);
-                            float2 w = tw2(twLh, twLl, j & (N - 1));   // W_L^j, j < L/2
-                            if (j & N) w = make_float2(-w.x, -w.y);   // W_L^(j + L/2) = -W_L^j
-                            return cmulc(w, r);
-                          },
-                          twLh, twLl, ht);
+    auto SR = [&](int k) -> float2 {
+      if (k >= N - 1) return (k & 1) ? aFO[k >> 1] : aFE[k >> 1];
+      const float2 r = (k & 1) ? aRO[k >> 1] : aRE[k >> 1];
+      const int j = ((Q - 1) * k) & (L - 1);
+      float2 w = tw2(twLh, twLl, j & (N - 1));   // W_L^j, j < L/2
+      if (j & N) w = make_float2(-w.x, -w.y);   // W_L^(j + L/2) = -W_L^j
+      return cmulc(w, r);
+    };
+    hermitian_pack<LOG2L, NT_CORR>(WE, both_bins<N>(SR), twLh, twLl, ht);
   }
   // each half packs, inverts and scans its own buffer: named barriers 5, 6
   const GroupBarrier hb{5 + half, NT_CORR};
@@ -981,6 +997,31 @@ size_t corr_pair2_smem_bytes() {
          + 2 * 256 * sizeof(float)                         // entropy weight per window
          + 2 * 256 * sizeof(float4)                        // window values of a channel pair
          + 2 * 256 * sizeof(uint32_t);                     // 2-bit codes of positions g + 256 r
+}
+
+// Bins k and N-k (k <= N/2) of the reverse strand's packed sum in the
+// both-strands kernels: S_r(k) = W_L^((Q-1)k) i conj(2i R(k)), with
+// i conj(x + iy) = y + ix; bins N-1 and N are the targets' own sums, the same
+// for both strands.  W_L^((Q-1)(N-k)) = (-1)^(Q-1) conj(W_L^((Q-1)k)), so one
+// twiddle serves both bins.
+template <int LOG2L>
+__device__ __forceinline__ void reverse_bins(int k, int Q, const float2* aFE, const float2* aFO, const float2* aRE,
+                                             const float2* aRO, const float2* twLh, const float2* twLl, float2& a,
+                                             float2& b) {
+  constexpr int L = 1 << LOG2L, N = L >> 1;
+  const int j = ((Q - 1) * k) & (L - 1);
+  float2 w = tw2(twLh, twLl, j & (N - 1));   // W_L^j, j < L/2
+  if (j & N) w = make_float2(-w.x, -w.y);   // W_L^(j + L/2) = -W_L^j
+  const float2 r = (k & 1) ? aRO[k >> 1] : aRE[k >> 1];
+  a = cmul(w, make_float2(r.y, r.x));
+  const int kn = N - k;
+  if (kn >= N - 1) {
+    b = (kn & 1) ? aFO[kn >> 1] : aFE[kn >> 1];
+  } else {
+    const float2 wn = (Q & 1) ? make_float2(w.x, -w.y) : make_float2(-w.x, w.y);   // (-1)^(Q-1) conj(w)
+    const float2 rn = (kn & 1) ? aRO[kn >> 1] : aRE[kn >> 1];
+    b = cmul(wn, make_float2(rn.y, rn.x));
+  }
 }
 
 // Per-bin step of the both-strands kernels at a general bin, from the packed
@@ -1299,19 +1340,12 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
     //      carry factors 2 and 2: FindTop scales by 1/(4N). ----
     float2* buf = G ? WE : ZE;
     if (G == 0) {
-      hermitian_pack<LOG2L, 256>(ZE, [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; }, twLh,
-                                 twLl, g, 1.0f);
+      auto SF = [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; };
+      hermitian_pack<LOG2L, 256>(ZE, both_bins<N>(SF), twLh, twLl, g, 1.0f);
     } else {
-      hermitian_pack<LOG2L, 256>(WE,
-                                 [&](int k) -> float2 {
-                                   if (k >= N - 1) return (k & 1) ? aFO[k >> 1] : aFE[k >> 1];
-                                   const float2 r = (k & 1) ? aRO[k >> 1] : aRE[k >> 1];
-                                   const int j = ((Q - 1) * k) & (L - 1);
-                                   float2 w = tw2(twLh, twLl, j & (N - 1));   // W_L^j, j < L/2
-                                   if (j & N) w = make_float2(-w.x, -w.y);   // W_L^(j + L/2) = -W_L^j
-                                   return cmul(w, make_float2(r.y, r.x));
-                                 },
-                                 twLh, twLl, g, 1.0f);
+      hermitian_pack<LOG2L, 256>(
+          WE, [&](int k, float2& a, float2& b) { reverse_bins<LOG2L>(k, Q, aFE, aFO, aRE, aRO, twLh, twLl, a, b); },
+          twLh, twLl, g, 1.0f);
     }
     gb();
     fft_inverse<LOG2N, Plan<LOG2N>, Plan<LOG2N>::n - 1, GroupBarrier>(buf, twNh, twNl, g, 256, gb);
@@ -1376,6 +1410,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
   float4* vv = reinterpret_cast<float4*>(Es + NWIN);     // [channel pair][window]
   uint32_t* cw = reinterpret_cast<uint32_t*>(vv + 2 * NWIN);
   __shared__ int s_cnt4[4];
+  __shared__ unsigned s_flags;   // bit 0: a byte >= 128; bit 1: a byte other than A, C, G, T
   __shared__ double s_wmo[2][8];
   __shared__ Split3 s_wf[2][8];
 
@@ -1397,81 +1432,87 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
     const int len = S.chunks[u].len;
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     if (tid < 4) s_cnt4[tid] = 0;
+    if (tid == 0) s_flags = 0u;
     __syncthreads();
-    // byte checks of the 16-byte pieces (zero past the end)
-    int high = 0, nonacgt = 0;
+    // thread g < 256 takes bytes 16g..16g+15, which are also entropy window g
+    // (WIN = 16): byte checks, 2-bit codes, base counts and the window's
+    // entropy weight from one load, as corr_pair2_kernel's prologue
+    uint32_t* cwin = reinterpret_cast<uint32_t*>(vv);   // codes per window; vv is free until the window values
     if (tid < 256) {
-      const int valid = len - 16 * tid;
-      const uint4 v = *reinterpret_cast<const uint4*>(sb + 16 * tid);
+      const int g = tid;
+      const int valid = len - 16 * g;
+      const uint4 v = *reinterpret_cast<const uint4*>(sb + 16 * g);
       const uint32_t x[4] = {v.x, v.y, v.z, v.w};
       auto nz = [](uint32_t y) { return (((y & 0x7f7f7f7fu) + 0x7f7f7f7fu) | y) & 0x80808080u; };
+      uint32_t high = 0u, bad = 0u, p0 = 0u, p1 = 0u, codes = 0u;
 #pragma unroll
       for (int k = 0; k < 4; k++) {
         const int vk = min(max(valid - 4 * k, 0), 4);
         const uint32_t m = vk >= 4 ? 0xffffffffu : (1u << (8 * vk)) - 1u;
-        high |= (x[k] & m & 0x80808080u) != 0u;
-        const uint32_t bad = nz(x[k] ^ 0x41414141u) & nz(x[k] ^ 0x43434343u) & nz(x[k] ^ 0x47474747u) &
-                             nz(x[k] ^ 0x54545454u);
-        nonacgt |= (bad & m & 0x80808080u) != 0u;
+        high |= x[k] & m & 0x80808080u;
+        bad |= nz(x[k] ^ 0x41414141u) & nz(x[k] ^ 0x43434343u) & nz(x[k] ^ 0x47474747u) & nz(x[k] ^ 0x54545454u) &
+               m & 0x80808080u;
+        const uint32_t cd = ((x[k] >> 1) ^ (x[k] >> 2)) & 0x03030303u & m;
+        p0 |= (((cd & 0x01010101u) * 0x10204080u) >> 28) << (4 * k);
+        p1 |= ((((cd >> 1) & 0x01010101u) * 0x10204080u) >> 28) << (4 * k);
+        const uint32_t c2 = cd | (cd >> 6);
+        codes |= ((c2 & 0xfu) | ((c2 >> 12) & 0xf0u)) << (8 * k);
       }
-    }
-    const int any_high = __syncthreads_or(high);
-    const int generic = __syncthreads_or(nonacgt);
-    if (any_high || generic) {
-      if (tid == 0) S.chunk_flags[u] = (any_high ? CF_HIGH : 0u) | CF_GENERIC;
-      if (next >= 0) spec_prefetch(S, next, sb, tid);
-      continue;
-    }
-    // entropy weights (group 0), 2-bit codes (group 1), base counts (all)
-    if (G == 0) {
+      cwin[g] = codes;
+      const int nv = min(max(valid, 0), 16);
+      const int nt = __popc(p0 & p1), nc = __popc(p0) - nt, ng = __popc(p1) - nt, na = nv - nc - ng - nt;
       float E = 0.f;
       if (len < 1024) {
         E = 1.f;
-      } else if (g * WIN + WIN <= len) {
-        const int i0 = g * WIN;
-        uint32_t cnt = 0;
-        for (int j = 0; j < WIN; j++) cnt += 1u << (8 * code_of(sb[i0 + j]));
-        const int a = cnt & 255u, c = (cnt >> 8) & 255u, gg = (cnt >> 16) & 255u;
-        E = __ldg(&S.tab.ent_acgt[(a * (WIN + 1) + c) * (WIN + 1) + gg]);
-      } else if (g * WIN < len) {
-        const int i0 = g * WIN;
-        const int k = len - i0;
+      } else if (nv == 16) {
+        E = __ldg(&S.tab.ent_acgt[(na * (WIN + 1) + nc) * (WIN + 1) + ng]);
+      } else if (nv > 0) {
         int a4 = 0, c4 = 0, g4 = 0, t4 = 0;
-        for (int j = 0; j < k; j++) {
-          const uchar4 q = c_w4q[sb[i0 + j]];
+        for (int j = 0; j < nv; j++) {
+          const uchar4 q = c_w4q[sb[16 * g + j]];
           a4 += q.x; c4 += q.y; g4 += q.z; t4 += q.w;
         }
-        const double* et = S.tab.ent + k * (4 * WIN + 1);
+        const double* et = S.tab.ent + nv * (4 * WIN + 1);
         const double sv =
             __dadd_rn(__dadd_rn(__dadd_rn(__ldg(et + a4), __ldg(et + c4)), __ldg(et + g4)), __ldg(et + t4));
         E = __double2float_rn(-sv);
         if (E < 0.f) E = 0.f;
       }
       Es[g] = E;
-    } else {
-      uint32_t w = 0;
-#pragma unroll
-      for (int r = 0; r < 16; r++) w |= code_of(sb[g + 256 * r]) << (2 * r);
-      cw[g] = w;
-    }
-    {
-      uint32_t ct = 0;
-      for (int i = tid; i < N; i += NT_PAIR2)
-        if (i < len) ct += 1u << (8 * code_of(sb[i]));
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        const int v = __reduce_add_sync(0xffffffffu, 4 * (int)((ct >> (8 * k)) & 255u));
-        if ((tid & 31) == 0 && v) atomicAdd(&s_cnt4[k], v);
+      const uint32_t lo = __reduce_add_sync(0xffffffffu, (uint32_t)na | ((uint32_t)nc << 16));
+      const uint32_t hi = __reduce_add_sync(0xffffffffu, (uint32_t)ng | ((uint32_t)nt << 16));
+      const uint32_t fl = __reduce_or_sync(0xffffffffu, (high ? 1u : 0u) | (bad ? 2u : 0u));
+      if ((tid & 31) == 0) {
+        atomicAdd(&s_cnt4[0], 4 * (int)(lo & 0xffffu));
+        atomicAdd(&s_cnt4[1], 4 * (int)(lo >> 16));
+        atomicAdd(&s_cnt4[2], 4 * (int)(hi & 0xffffu));
+        atomicAdd(&s_cnt4[3], 4 * (int)(hi >> 16));
+        if (fl) atomicOr(&s_flags, fl);
       }
     }
     __syncthreads();   // the chunk bytes are no longer read
     if (next >= 0) spec_prefetch(S, next, sb, tid);
+    const uint32_t flg = s_flags;
+    if (flg) {
+      if (tid == 0) S.chunk_flags[u] = ((flg & 1u) ? CF_HIGH : 0u) | CF_GENERIC;
+      __syncthreads();   // cwin (in vv) and the flags are reused by the next chunk
+      continue;
+    }
     if (tid < 4) {
       const double off = len > 0 ? __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len) : 0.0;
       s_wmo[0][tid] = __dsub_rn(0.0, off);
       s_wmo[1][tid] = __dsub_rn(1.0, off);
       s_wf[0][tid] = split3(s_wmo[0][tid]);
       s_wf[1][tid] = split3(s_wmo[1][tid]);
+    }
+    if (tid >= 256) {   // the codes of positions g + 256 r, one word per g
+      const int g = tid - 256;
+      const uint32_t* cs = cwin + (g >> 4);
+      const int sh = 2 * (g & 15);
+      uint32_t w = 0;
+#pragma unroll
+      for (int r = 0; r < 16; r++) w |= ((cs[16 * r] >> sh) & 3u) << (2 * r);
+      cw[g] = w;
     }
     __syncthreads();
     // group G transforms channel pair G: (A, T) or (C, G)
@@ -1603,19 +1644,12 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
     // ---- inverses and FindTop, as corr_pair2_kernel ----
     float2* buf = G ? WE : ZE;
     if (G == 0) {
-      hermitian_pack<LOG2L, 256>(ZE, [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; }, twLh,
-                                 twLl, g, 1.0f);
+      auto SF = [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; };
+      hermitian_pack<LOG2L, 256>(ZE, both_bins<N>(SF), twLh, twLl, g, 1.0f);
     } else {
-      hermitian_pack<LOG2L, 256>(WE,
-                                 [&](int k) -> float2 {
-                                   if (k >= N - 1) return (k & 1) ? aFO[k >> 1] : aFE[k >> 1];
-                                   const float2 r = (k & 1) ? aRO[k >> 1] : aRE[k >> 1];
-                                   const int j = ((Q - 1) * k) & (L - 1);
-                                   float2 w = tw2(twLh, twLl, j & (N - 1));
-                                   if (j & N) w = make_float2(-w.x, -w.y);
-                                   return cmul(w, make_float2(r.y, r.x));
-                                 },
-                                 twLh, twLl, g, 1.0f);
+      hermitian_pack<LOG2L, 256>(
+          WE, [&](int k, float2& a, float2& b) { reverse_bins<LOG2L>(k, Q, aFE, aFO, aRE, aRO, twLh, twLl, a, b); },
+          twLh, twLl, g, 1.0f);
     }
     gb();
     fft_inverse<LOG2N, Plan<LOG2N>, Plan<LOG2N>::n - 1, GroupBarrier>(buf, twNh, twNl, g, 256, gb);
