@@ -1105,6 +1105,17 @@ __device__ __forceinline__ void pair2_prefetch(const CorrParams& P, int pidx, ui
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
+// Work order of the persistent kernels over count items: CTA b takes items
+// b + r * grid for rounds r = 0..S (S = count / grid - 2, at least 0), then
+// items from the work counter (offset (S + 1) * grid) until none is left.
+// The rounds balance equal-cost items with no atomics; the counter absorbs
+// items of unequal cost (pairs handed back, chunks flagged) and CTAs that
+// start late at the end.
+__device__ __forceinline__ int static_rounds(int count) { return max(0, count / (int)gridDim.x - 2); }
+__device__ __forceinline__ int take_item(int* work, int r, int S) {
+  return r <= S ? (int)blockIdx.x + r * (int)gridDim.x : atomicAdd(work, 1) + (S + 1) * (int)gridDim.x;
+}
+
 template <int LOG2L>
 __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParams P) {
   constexpr int L = 1 << LOG2L;
@@ -1136,6 +1147,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
   uint32_t* cw = reinterpret_cast<uint32_t*>(vv + 2 * NWIN);   // [sequence][g]
   __shared__ int s_cnt4[8];
   __shared__ unsigned s_flags;     // bit 0: a byte >= 128; bit 1: a byte other than A, C, G, T
+  __shared__ int s_take;           // the CTA's next pair
   __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
   __shared__ Split3 s_wf[2][8];    // the same as three floats each
   __shared__ int s_warp[2][2 * 256 / 32];
@@ -1154,15 +1166,23 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
     twLl[tid] = P.tab.twL_lo[tid];
   }
   if ((int)blockIdx.x < P.count) pair2_prefetch(P, P.first + blockIdx.x, st, sq, tid);
+  // Pairs in the order take_item gives, each taken one pair ahead (the next
+  // pair's bytes are prefetched while this one is worked on; thread 0 uses a
+  // counter result one pair after taking it).
+  const int S = static_rounds(P.count);
+  if (tid == 0) s_take = take_item(P.work, 1, S);
 
-  for (int p = blockIdx.x; p < P.count; p += gridDim.x) {
+  for (int p = blockIdx.x, r = 0; p < P.count; r++) {
     const int pidx = P.first + p;
-    const int next = p + (int)gridDim.x < P.count ? P.first + p + (int)gridDim.x : -1;
     const int T = P.pairs[pidx].tlen, Q = P.pairs[pidx].qlen;
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     if (tid < 8) s_cnt4[tid] = 0;
     if (tid == 0) s_flags = 0u;
-    __syncthreads();   // the chunk bytes are in; the counters are zero
+    __syncthreads();   // the chunk bytes are in; the counters are zero; the next pair is known
+    const int np = s_take;
+    const int next = np < P.count ? P.first + np : -1;
+    int take = 0;
+    if (tid == 0) take = take_item(P.work, r + 2, S);   // the pair after next
 
     // ---- 1. thread (G, g) takes bytes 16g..16g+15 of sequence G, which are
     //      also its entropy window (WIN = 16): byte checks (per byte,
@@ -1240,7 +1260,9 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
           P.fb_list[atomicAdd(P.fb_cnt, 1)] = pidx;   // the per-strand kernel takes it
         }
       }
-      __syncthreads();   // cwin (in vv) and the flags are reused by the next pair
+      if (tid == 0) s_take = take;
+      __syncthreads();   // cwin (in vv), the flags and the next pair's index are reused
+      p = np;
       continue;
     }
     if (tid == 0) P.pair_flags[pidx] = P.pairs[pidx].flags & PF_FAST;
@@ -1353,7 +1375,9 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
     // ---- 5. FindTop, one strand per group ----
     find_top<LOG2L, 256, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, G, buf, g, s_warp[G], gb,
                                        1.0f / (float)(4 * N));
+    if (tid == 0) s_take = take;
     __syncthreads();   // buffers and per-pair words are reused by the next pair
+    p = np;
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
@@ -1411,6 +1435,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
   uint32_t* cw = reinterpret_cast<uint32_t*>(vv + 2 * NWIN);
   __shared__ int s_cnt4[4];
   __shared__ unsigned s_flags;   // bit 0: a byte >= 128; bit 1: a byte other than A, C, G, T
+  __shared__ int s_take;         // the CTA's next chunk
   __shared__ double s_wmo[2][8];
   __shared__ Split3 s_wf[2][8];
 
@@ -1427,13 +1452,20 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
     twLl[tid] = S.tab.twL_lo[tid];
   }
   if ((int)blockIdx.x < S.count) spec_prefetch(S, blockIdx.x, sb, tid);
-  for (int u = blockIdx.x; u < S.count; u += gridDim.x) {
-    const int next = u + (int)gridDim.x < S.count ? u + (int)gridDim.x : -1;
+  // chunks in the order take_item gives, each taken one chunk ahead, as
+  // corr_pair2_kernel takes its pairs
+  const int SR = static_rounds(S.count);
+  if (tid == 0) s_take = take_item(S.work, 1, SR);
+  for (int u = blockIdx.x, r = 0; u < S.count; r++) {
     const int len = S.chunks[u].len;
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     if (tid < 4) s_cnt4[tid] = 0;
     if (tid == 0) s_flags = 0u;
     __syncthreads();
+    const int nu = s_take;
+    const int next = nu < S.count ? nu : -1;
+    int take = 0;
+    if (tid == 0) take = take_item(S.work, r + 2, SR);
     // thread g < 256 takes bytes 16g..16g+15, which are also entropy window g
     // (WIN = 16): byte checks, 2-bit codes, base counts and the window's
     // entropy weight from one load, as corr_pair2_kernel's prologue
@@ -1495,7 +1527,9 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
     const uint32_t flg = s_flags;
     if (flg) {
       if (tid == 0) S.chunk_flags[u] = ((flg & 1u) ? CF_HIGH : 0u) | CF_GENERIC;
-      __syncthreads();   // cwin (in vv) and the flags are reused by the next chunk
+      if (tid == 0) s_take = take;
+      __syncthreads();   // cwin (in vv), the flags and the next chunk's index are reused
+      u = nu;
       continue;
     }
     if (tid < 4) {
@@ -1536,8 +1570,12 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
       out[g + 256 * it] = bE[pa];
       out[N + g + 256 * it] = bO[pa];
     }
-    if (tid == 0) S.chunk_flags[u] = 0u;
+    if (tid == 0) {
+      S.chunk_flags[u] = 0u;
+      s_take = take;
+    }
     __syncthreads();
+    u = nu;
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
@@ -1566,6 +1604,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
   float2* twLh = twNl + 64;
   float2* twLl = twLh + NH;
   __shared__ int s_warp[2][2 * 256 / 32];
+  __shared__ int s_take;   // the CTA's next pair
 
   const int tid = threadIdx.x;
   const int G = tid >> 8;   // product: 0 even bins, 1 odd bins; then 0 forward strand, 1 reverse
@@ -1580,8 +1619,16 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
     twLl[tid] = P.tab.twL_lo[tid];
   }
   __syncthreads();
-  for (int p = blockIdx.x; p < P.count; p += gridDim.x) {
+  // pairs in the order take_item gives, each taken one pair ahead, as
+  // corr_pair2_kernel takes them
+  const int S = static_rounds(P.count);
+  if (tid == 0) s_take = take_item(P.work, 1, S);
+  __syncthreads();
+  for (int p = blockIdx.x, r = 0; p < P.count; r++) {
     const int pidx = P.first + p;
+    const int np = s_take;
+    int take = 0;
+    if (tid == 0) take = take_item(P.work, r + 2, S);
     const int tc = P.pair_chunk[2 * pidx], qc = P.pair_chunk[2 * pidx + 1];
     const int Q = P.pairs[pidx].qlen;
     const uint32_t fl = P.chunk_flags[tc] | P.chunk_flags[qc];
@@ -1595,6 +1642,9 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
           P.fb_list[atomicAdd(P.fb_cnt, 1)] = pidx;
         }
       }
+      if (tid == 0) s_take = take;
+      __syncthreads();   // s_take is rewritten for the next pair
+      p = np;
       continue;
     }
     if (tid == 0) P.pair_flags[pidx] = P.pairs[pidx].flags & PF_FAST;
@@ -1655,7 +1705,9 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
     fft_inverse<LOG2N, Plan<LOG2N>, Plan<LOG2N>::n - 1, GroupBarrier>(buf, twNh, twNl, g, 256, gb);
     find_top<LOG2L, 256, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, G, buf, g, s_warp[G], gb,
                                        1.0f / (float)(4 * N));
+    if (tid == 0) s_take = take;
     __syncthreads();
+    p = np;
   }
 }
 

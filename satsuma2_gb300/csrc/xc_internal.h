@@ -94,6 +94,7 @@ struct CorrParams {
   int* strad_cnt;           // optional: near-threshold lags per [pair*2 + strand] (zeroed before)
   int* strad_list;          //   and the first STRAD_CAP of them, [pair*2 + strand][STRAD_CAP]
   int count;                // pairs of this launch (set by launch_corr)
+  int* work;                // persistent kernels: counter of pairs taken after each CTA's first (zeroed before the launch)
   int pair_form;            // with fb_list: 2 = persistent 512-thread kernel, 1 = 1024-thread form
   // spectra path (FFT 8192 batches whose pairs share chunks): the pair kernel
   // reads both chunks' spectra instead of transforming them
@@ -122,6 +123,7 @@ struct SpecParams {
   LTables tab;
   float2* spec;             // [chunk][4][N]: channels (A,T) even-bin, odd-bin transform, then (C,G); bin order
   uint32_t* chunk_flags;    // [chunk]: CF_* (0 = spectra written)
+  int* work;                // counter of chunks taken after each CTA's first (zeroed before the launch)
 };
 
 // Global channel-sum scratch of one pair strand for FFT lengths beyond one

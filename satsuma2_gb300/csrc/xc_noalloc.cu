@@ -50,6 +50,7 @@ constexpr size_t NA_BYTES = NA_DENSE + align256((size_t)2 * NA_SLOTS * sizeof(De
 // counter words inside NA_CNT
 constexpr int C_OFFCNT = 0;   // [2] FindTop offsets per strand
 constexpr int C_FLAGS = 2;    // [1] pair flags
+constexpr int C_WORK = 6;     // [1] the both-strands kernel's work counter
 constexpr int C_RESCNT = 4;   // [2] kept matches per strand
 constexpr int C_MISC = 8;     // [4] overflow count, error bits, debug count, pairs handed back
 constexpr int C_BASE = 12;    // [3] dense result bases
@@ -159,6 +160,7 @@ int align_pair_noalloc(Ctx* c, const xc_pair& p, xc_result* out, size_t cap, siz
     cp.fb_cnt = cnt + C_MISC + 3;
     cp.pair_form = c->pair_form;
   }
+  cp.work = cnt + C_WORK;
   cp.strand_threads = c->strand_threads[lg];
   NA_CHECK(launch_corr(lg, cp, 1, s));
 

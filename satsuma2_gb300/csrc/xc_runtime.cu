@@ -490,7 +490,7 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   if ((r = dev_grow(b->d_res, b->cap_res, nslots * slots)) != XC_OK) return r;
   if ((r = dev_grow(b->d_rescnt, b->cap_rescnt, nslots)) != XC_OK) return r;
   if ((r = dev_grow(b->d_ovf, b->cap_ovf, (size_t)b->ovf_cap)) != XC_OK) return r;
-  if ((r = dev_grow(b->d_misc, b->cap_misc, 4)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_misc, b->cap_misc, 8)) != XC_OK) return r;
   if ((r = dev_grow(b->d_fb, b->cap_fb, n)) != XC_OK) return r;
   if ((r = dev_grow(b->d_stradcnt, b->cap_stradcnt, nslots)) != XC_OK) return r;
   if ((r = dev_grow(b->d_strad, b->cap_strad, nslots * STRAD_CAP)) != XC_OK) return r;
@@ -567,7 +567,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
   cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
   if (timed) XC_CHECK(cudaStreamIsCapturing(s, &cst));
   const unsigned evflags = cst == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
-  XC_CHECK(cudaMemsetAsync(b->d_misc, 0, 4 * sizeof(int), s));
+  XC_CHECK(cudaMemsetAsync(b->d_misc, 0, 8 * sizeof(int), s));   // counters, error words, work counters
   XC_CHECK(cudaMemsetAsync(b->d_stradcnt, 0, nslots * sizeof(int), s));
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[0], s, evflags));
   for (const Bucket& bk : b->buckets) {
@@ -591,6 +591,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     cp.dbg_sig = b->d_dbg_sig;
     cp.dbg_xc = b->d_dbg_xc;
     cp.acc = b->d_acc;
+    cp.work = b->d_misc + 4;   // zeroed above; one FFT-8192 bucket per batch
     if (bk.log2L == PAIR_LOG2L && c->pair_kernel) {
       cp.fb_list = b->d_fb;
       cp.fb_cnt = b->d_misc + 3;   // zeroed above
@@ -607,6 +608,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
       spp.tab = cp.tab;
       spp.spec = b->d_spec;
       spp.chunk_flags = b->d_chunkflags;
+      spp.work = b->d_misc + 5;
       cp.pair_chunk = b->d_pairchunk;
       cp.spec = b->d_spec;
       cp.chunk_flags = b->d_chunkflags;
