@@ -6,6 +6,7 @@
 #include "xc_runtime.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -295,7 +296,7 @@ class HostPool {
       chunks_ = chunks;
       next_ = 0;
       left_ = chunks;
-      gen_++;
+      gen_.fetch_add(1, std::memory_order_release);
     }
     cv_.notify_all();
     work();
@@ -310,14 +311,23 @@ class HostPool {
     workers_ = std::max(1u, std::min(16u, hc ? hc : 1u)) - 1;
     for (unsigned i = 0; i < workers_; i++) std::thread([this] { loop(); }).detach();
   }
+  // A worker polls for the next job for a while (SPIN_US) before it sleeps:
+  // the sub-batches of one call arrive a few hundred microseconds apart, and
+  // a wake-up from the condition variable costs tens of microseconds.
+  static constexpr int SPIN_US = 200;
   void loop() {
     uint64_t seen = 0;
     for (;;) {
-      {
-        std::unique_lock<std::mutex> lk(mu_);
-        cv_.wait(lk, [&] { return gen_ != seen; });
-        seen = gen_;
+      const auto t0 = std::chrono::steady_clock::now();
+      for (int i = 0; gen_.load(std::memory_order_acquire) == seen; i++) {
+        if ((i & 255) == 255 &&
+            std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(SPIN_US)) {
+          std::unique_lock<std::mutex> lk(mu_);
+          cv_.wait(lk, [&] { return gen_.load(std::memory_order_acquire) != seen; });
+          break;
+        }
       }
+      seen = gen_.load(std::memory_order_acquire);
       work();
     }
   }
@@ -343,7 +353,7 @@ class HostPool {
   std::condition_variable cv_, done_cv_;
   const std::function<void(size_t, size_t)>* job_ = nullptr;
   size_t n_ = 0, chunks_ = 0, next_ = 0, left_ = 0;
-  uint64_t gen_ = 0;
+  std::atomic<uint64_t> gen_{0};
 };
 
 static void parallel_for(size_t n, size_t grain, const std::function<void(size_t, size_t)>& f) {
@@ -776,46 +786,56 @@ int batch_collect(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_t cap, 
   if (pair_counts)
     for (int i = 0; i < n; i++) pair_counts[i] = cnt[i];
   if (need > cap || (!out && need)) return XC_ERR_CAPACITY;
-  size_t o = 0;
+  // each pair's records from its output offset; pair ranges in parallel when
+  // there are many records
+  std::vector<size_t> first(n + 1, 0);
+  for (int i = 0; i < n; i++) first[i + 1] = first[i] + cnt[i];
   const int qchunk = c->prm.q_chunk;
-  std::vector<DevResult> merged;
-  for (int i = 0; i < n; i++) {
-    const int d = dev_of[i];
-    const xc_pair& p = b->meta[i];
-    for (int s2 = 0; s2 < 2; s2++) {
-      const int sl = 2 * d + s2;
-      const DevResult* rec = b->h_dense + b->h_base[sl];
-      size_t nrec = (size_t)(b->h_base[sl + 1] - b->h_base[sl]);
-      if (novf > 0 && extra_of[sl] >= 0) {   // slot records plus its overflow records, reordered
-        const auto& e = extra[extra_of[sl]];
-        merged.assign(rec, rec + nrec);
-        merged.insert(merged.end(), e.begin(), e.end());
-        std::sort(merged.begin(), merged.end(), [](const DevResult& a, const DevResult& q) {
-          return a.key < q.key || (a.key == q.key && a.tstart < q.tstart);
-        });
-        rec = merged.data();
-        nrec = merged.size();
-      }
-      for (size_t j = 0; j < nrec; j++) {
-        const DevResult& rr = rec[j];
-        xc_result& x = out[o++];
-        memset(&x, 0, sizeof(x));
-        // FilterMatches coordinate mapping (HomologyByXCorrSlave.cc:175-181, RCQuery :56-60)
-        const int tStart = p.t_chunk_start + rr.tstart;
-        const int qStart = s2 == 0 ? p.q_chunk_start + rr.qstart
-                                   : rr.qstart + (int)p.query_size - p.q_chunk_start - qchunk;
-        x.query_id = p.query_id;
-        x.target_id = p.target_id;
-        x.query_size = p.query_size;
-        x.qstart = (unsigned long)(long)qStart;
-        x.tstart = (unsigned long)(long)tStart;
-        x.len = (unsigned long)(long)rr.len;
-        x.reverse = (unsigned char)s2;
-        x.prob = rr.prob;
-        x.ident = rr.ident;
+  auto convert = [&](size_t lo_pair, size_t hi_pair) {
+    std::vector<DevResult> merged;
+    for (size_t i = lo_pair; i < hi_pair; i++) {
+      size_t o = first[i];
+      const int d = dev_of[i];
+      const xc_pair& p = b->meta[i];
+      for (int s2 = 0; s2 < 2; s2++) {
+        const int sl = 2 * d + s2;
+        const DevResult* rec = b->h_dense + b->h_base[sl];
+        size_t nrec = (size_t)(b->h_base[sl + 1] - b->h_base[sl]);
+        if (novf > 0 && extra_of[sl] >= 0) {   // slot records plus its overflow records, reordered
+          const auto& e = extra[extra_of[sl]];
+          merged.assign(rec, rec + nrec);
+          merged.insert(merged.end(), e.begin(), e.end());
+          std::sort(merged.begin(), merged.end(), [](const DevResult& a, const DevResult& q) {
+            return a.key < q.key || (a.key == q.key && a.tstart < q.tstart);
+          });
+          rec = merged.data();
+          nrec = merged.size();
+        }
+        for (size_t j = 0; j < nrec; j++) {
+          const DevResult& rr = rec[j];
+          xc_result& x = out[o++];
+          memset(&x, 0, sizeof(x));
+          // FilterMatches coordinate mapping (HomologyByXCorrSlave.cc:175-181, RCQuery :56-60)
+          const int tStart = p.t_chunk_start + rr.tstart;
+          const int qStart = s2 == 0 ? p.q_chunk_start + rr.qstart
+                                     : rr.qstart + (int)p.query_size - p.q_chunk_start - qchunk;
+          x.query_id = p.query_id;
+          x.target_id = p.target_id;
+          x.query_size = p.query_size;
+          x.qstart = (unsigned long)(long)qStart;
+          x.tstart = (unsigned long)(long)tStart;
+          x.len = (unsigned long)(long)rr.len;
+          x.reverse = (unsigned char)s2;
+          x.prob = rr.prob;
+          x.ident = rr.ident;
+        }
       }
     }
-  }
+  };
+  if (need >= 4096)
+    parallel_for((size_t)n, 64, convert);
+  else
+    convert(0, (size_t)n);
   return XC_OK;
 }
 
