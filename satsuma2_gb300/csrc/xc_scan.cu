@@ -144,8 +144,9 @@ __device__ __forceinline__ uint32_t nib_popc(uint32_t x) {
 // all eight blocks at once in byte lanes: even blocks 2j in one word, odd
 // blocks 2j+1 in another, each count biased by 128 - MIN_HITS so that bit 7
 // of its byte is the test.  Every byte stays within 0..255 (counts <= 49,
-// nibble differences biased by 4, prefix sums <= 48).
-__device__ __forceinline__ bool screen_word(uint32_t e2, uint32_t e1, uint32_t e0) {
+// nibble differences biased by 4, prefix sums <= 48).  Returns the test bits
+// (nonzero: the word is marked).
+__device__ __forceinline__ uint32_t screen_word(uint32_t e2, uint32_t e1, uint32_t e0) {
   const uint32_t pl = nib_popc(__funnelshift_r(e2, e1, 19));   // nibble k: bits 19+4k.. leaving
   const uint32_t pe = nib_popc(e0 >> 4);                        // nibble k: bits 68+4k.. entering
   const uint32_t de = (pe & 0x0f0f0f0fu) + 0x04040404u - (pl & 0x0f0f0f0fu);                 // 4 + d(2j)
@@ -154,26 +155,29 @@ __device__ __forceinline__ bool screen_word(uint32_t e2, uint32_t e1, uint32_t e
   const uint32_t c0 = __popc(e2 >> 19) + __popc(e1) + __popc(e0 & 15u);
   const uint32_t x = sx + (c0 + (128 - MIN_HITS)) * 0x01010101u - 0x18100800u;   // 128 - 19 + c(2j)
   const uint32_t x2 = x + de - 0x04040404u;                                        // 128 - 19 + c(2j+1)
-  return ((x | x2) & 0x80808080u) != 0u;
+  return (x | x2) & 0x80808080u;
 }
 
 // Exact window bits of one word: bit u set when check u's window holds
 // >= MIN_HITS equal bases.  Four byte lanes (checks 8j + s) step s = 0..7
-// together: count(u+1) = count(u) + bit u+65 - bit u+19 of e2:e1:e0; the
-// counts stay within 0..46, so no lane borrows from or carries into the next.
+// together: count(u+1) = count(u) + bit u+65 - bit u+19 of e2:e1:e0.  Each
+// lane holds its count plus 128 - MIN_HITS, so bit 7 is the test; biased
+// counts stay within 109..155, so no lane borrows from or carries into the
+// next, and bit 7 of lane j moves to bit 8j + s with one shift and a mask.
 __device__ __forceinline__ uint32_t exact_word(uint32_t e2, uint32_t e1, uint32_t e0) {
   const uint64_t U = ((uint64_t)e1 << 32) | e2;
-  uint32_t w = (uint32_t)(__popcll(U >> 19) + __popc(e0 & 1u)) |
-               (uint32_t)(__popcll(U >> 27) + __popc(e0 & 0x1ffu)) << 8 |
-               (uint32_t)(__popcll(U >> 35) + __popc(e0 & 0x1ffffu)) << 16 |
-               (uint32_t)(__popcll(U >> 43) + __popc(e0 & 0x1ffffffu)) << 24;
+  uint32_t w = ((uint32_t)(__popcll(U >> 19) + __popc(e0 & 1u)) |
+                (uint32_t)(__popcll(U >> 27) + __popc(e0 & 0x1ffu)) << 8 |
+                (uint32_t)(__popcll(U >> 35) + __popc(e0 & 0x1ffffu)) << 16 |
+                (uint32_t)(__popcll(U >> 43) + __popc(e0 & 0x1ffffffu)) << 24) +
+               (128 - MIN_HITS) * 0x01010101u;
   const uint32_t lv = __funnelshift_r(e2, e1, 19);   // bit 8j+s: leaves after check 8j+s
   const uint32_t en = e0 >> 1;                       // bit 8j+s: enters at check 8j+s+1
   uint32_t g = 0;
 #pragma unroll
   for (int s = 0; s < 8; s++) {
     if (s) w = w + ((en >> (s - 1)) & 0x01010101u) - ((lv >> (s - 1)) & 0x01010101u);
-    g |= (((w + (128 - MIN_HITS) * 0x01010101u) >> 7) & 0x01010101u) << s;
+    g |= (w >> (7 - s)) & (0x01010101u << s);
   }
   return g;
 }
@@ -543,7 +547,7 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
             const uint2 nx = qp[q0 + q + 1], tw = tp[q0 + q];
             const uint32_t e0 = ~((tw.x ^ __funnelshift_r(a.x, nx.x, sh)) | (tw.y ^ __funnelshift_r(a.y, nx.y, sh)));
             a = nx;
-            acc = __funnelshift_r(acc, screen_word(e2, e1, e0) ? 1u : 0u, 1);   // in at bit 31
+            acc = __funnelshift_r(acc, min(screen_word(e2, e1, e0), 1u), 1);   // in at bit 31
             e2 = e1;
             e1 = e0;
           }
