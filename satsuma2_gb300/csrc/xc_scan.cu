@@ -41,7 +41,13 @@ template <int LOG2L> struct ScanGeom {
   // chunk byte arrays, which only the byte-table path fills.
   static constexpr int ICAP = 1280;   // items (8 bytes each: word, passing bits)
   static constexpr int QCAP = 2048;
-  static constexpr size_t region = (size_t)QCAP * 4 > 2 * (size_t)N ? (size_t)QCAP * 4 : 2 * (size_t)N;
+  // Survivors of the probability screen awaiting the FP64 tail, after the
+  // queue: 64, or as many as the rest of the byte region holds.
+  static constexpr int SVB = 28;   // bytes per survivor (Surv)
+  static constexpr int SVCAP = 2 * N > QCAP * 4 + 64 * SVB ? (2 * N - QCAP * 4) / SVB : 64;
+  static constexpr size_t region = (size_t)QCAP * 4 + (size_t)SVCAP * SVB > 2 * (size_t)N
+                                       ? (size_t)QCAP * 4 + (size_t)SVCAP * SVB
+                                       : 2 * (size_t)N;
   static constexpr size_t bytes = region +
       (size_t)(2 * TWP + (TW + 1) + 2 * QWP + (TW + 1) + OFF_CHUNK + MW * NT_SCAN + 2 * ICAP + NT_SCAN) * 4 +
       (size_t)OFF_CHUNK * 2;
@@ -182,6 +188,13 @@ __device__ __forceinline__ uint32_t exact_word(uint32_t e2, uint32_t e1, uint32_
   return g;
 }
 
+// A segment that passed the FP32 probability screen, waiting for the FP64
+// tail (GetMatchProbabilityEx and the record write).
+struct Surv {
+  int key, pos, s0, len, hits, gT, gQ;
+};
+static_assert(sizeof(Surv) == 28, "ScanGeom::SVB");
+
 template <int LOG2L>
 __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const ScanParams P) {
   using Gm = ScanGeom<LOG2L>;
@@ -192,6 +205,7 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
   uint8_t* st = smem;
   uint8_t* sq = st + N;
   uint32_t* queue = reinterpret_cast<uint32_t*>(smem);   // bitplane path only: item | bit << 12
+  Surv* surv = reinterpret_cast<Surv*>(smem + (size_t)Gm::QCAP * 4);   // bitplane path only
   uint2* tb = reinterpret_cast<uint2*>(smem + Gm::region);   // target planes (zero padded)
   uint2* qb = tb + TWP;                                       // query planes, QPAD zero words first
   int* tgp = reinterpret_cast<int*>(qb + QWP);
@@ -204,7 +218,7 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
   uint16_t* order = reinterpret_cast<uint16_t*>(dpos + NT_SCAN);
   __shared__ int s_hist[64];
   __shared__ int s_wsum[NWARP];
-  __shared__ int s_next, s_res, s_qn;
+  __shared__ int s_next, s_res, s_qn, s_nsv;
   __shared__ int s_cy_start[2];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -230,6 +244,7 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
   if (tid == 0) {
     s_res = 0;
     s_qn = 0;
+    s_nsv = 0;
   }
   if (generic) {
     // chunk bytes; strand 1 reverse-complements the query (DNAVector.cc:482-500)
@@ -327,56 +342,9 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
     e0 = ~((t0.x ^ __funnelshift_r(q2.x, q3.x, sh)) | (t0.y ^ __funnelshift_r(q2.y, q3.y, sh)));
   };
 
-  // One DoOne segment [s0, s1) on offset pos (CrossCorr.cc:693,713) through
-  // FilterMatches (HomologyByXCorrSlave.cc:171-212).  hits: exact equal-base
-  // count for A/C/G/T pairs (ignored on the generic path).
-  auto emit = [&](int key, int pos, int s0, int s1, int hits) {
-    const int len = s1 - s0;
-    if (P.dbg) {
-      const int d = atomicAdd(P.dbg_cnt, 1);
-      if (d < P.dbg_cap) {
-        DbgSeg g;
-        g.slot = slot; g.key = key; g.tstart = s0; g.qstart = s0 + pos; g.len = len;
-        g.pad[0] = g.pad[1] = g.pad[2] = 0;
-        P.dbg[d] = g;
-      } else {
-        atomicOr(P.err, 2);
-      }
-    }
-    if (len < P.min_len) return;
-    double matches, gcT, gcQ;
-    if (!generic) {
-      const int gT = gc_count(tb, tgp, s0, s1);
-      const int gQ = gc_count(qb + QPAD, qgp, s0 + pos, s1 + pos);
-      if (!P.ptable) {
-        // FP32 screen on the z-score (pm*N - hits) / sd: reject only past a
-        // threshold set on the host with a margin far beyond FP32 error;
-        // anything else goes to the exact test.  With A = gQ gT + (N-gQ)(N-gT),
-        // pm N = A / 2N and sd^2 = A (2N^2 - A) / 4N^3, so the test is
-        // D = A - 2N hits > z sqrt(A (2N^2 - A) / N), squared without
-        // divisions (A = 0: sd = 0, left to the exact test).
-        const int A = gQ * gT + (len - gQ) * (len - gT);
-        if (A > 0) {
-          const float D = (float)(A - 2 * len * hits);
-          const float Lf = D * D * (float)len;
-          const float R = P.screen_z * P.screen_z * (float)A * (float)(2 * len * len - A);
-          if (P.screen_z >= 0.f ? (D > 0.f && Lf > R) : (D >= 0.f || Lf < R)) return;
-        }
-      }
-      matches = (double)hits;
-      gcT = (double)gT;
-      gcQ = (double)gQ;
-    } else {
-      // GetMatchProbabilityEx's sums, in its order (AlignProbability.cc:79-95).
-      matches = 0.0; gcT = 0.0; gcQ = 0.0;
-      for (int i = 0; i < len; i++) {
-        const int a = st[s0 + i], b = sq[s0 + pos + i];
-        matches = __dadd_rn(matches, __ldg(&P.eq[a * 128 + b]));
-        gcT = __dadd_rn(gcT, __ldg(&P.gcw[a]));
-        gcQ = __dadd_rn(gcQ, __ldg(&P.gcw[b]));
-      }
-    }
-    // GetMatchProbabilityEx (AlignProbability.cc:107-125) in FP64, no FMA.
+  // GetMatchProbabilityEx (AlignProbability.cc:107-125) in FP64, no FMA, or
+  // the ProbTable lookup, and the record of a segment that passes.
+  auto score = [&](int key, int pos, int s0, int len, double matches, double gcT, double gcQ) {
     const double Nd = (double)len;
     const double ident = __ddiv_rn(matches, Nd);
     const double gct = __ddiv_rn(gcT, Nd);
@@ -416,6 +384,63 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
         atomicOr(P.err, 1);
       }
     }
+  };
+
+  // One DoOne segment [s0, s1) on offset pos (CrossCorr.cc:693,713) through
+  // FilterMatches (HomologyByXCorrSlave.cc:171-212).  hits: exact equal-base
+  // count for A/C/G/T pairs (ignored on the generic path).  A/C/G/T segments
+  // that pass the FP32 screen wait in the survivor buffer, scored after phase
+  // C by one thread each (the FP64 pipe's cost is per warp instruction,
+  // whatever the active lanes); a full buffer scores in place.
+  auto emit = [&](int key, int pos, int s0, int s1, int hits) {
+    const int len = s1 - s0;
+    if (P.dbg) {
+      const int d = atomicAdd(P.dbg_cnt, 1);
+      if (d < P.dbg_cap) {
+        DbgSeg g;
+        g.slot = slot; g.key = key; g.tstart = s0; g.qstart = s0 + pos; g.len = len;
+        g.pad[0] = g.pad[1] = g.pad[2] = 0;
+        P.dbg[d] = g;
+      } else {
+        atomicOr(P.err, 2);
+      }
+    }
+    if (len < P.min_len) return;
+    if (!generic) {
+      const int gT = gc_count(tb, tgp, s0, s1);
+      const int gQ = gc_count(qb + QPAD, qgp, s0 + pos, s1 + pos);
+      if (!P.ptable) {
+        // FP32 screen on the z-score (pm*N - hits) / sd: reject only past a
+        // threshold set on the host with a margin far beyond FP32 error;
+        // anything else goes to the exact test.  With A = gQ gT + (N-gQ)(N-gT),
+        // pm N = A / 2N and sd^2 = A (2N^2 - A) / 4N^3, so the test is
+        // D = A - 2N hits > z sqrt(A (2N^2 - A) / N), squared without
+        // divisions (A = 0: sd = 0, left to the exact test).
+        const int A = gQ * gT + (len - gQ) * (len - gT);
+        if (A > 0) {
+          const float D = (float)(A - 2 * len * hits);
+          const float Lf = D * D * (float)len;
+          const float R = P.screen_z * P.screen_z * (float)A * (float)(2 * len * len - A);
+          if (P.screen_z >= 0.f ? (D > 0.f && Lf > R) : (D >= 0.f || Lf < R)) return;
+        }
+      }
+      const int v = atomicAdd(&s_nsv, 1);
+      if (v < Gm::SVCAP) {
+        surv[v] = Surv{key, pos, s0, len, hits, gT, gQ};
+      } else {
+        score(key, pos, s0, len, (double)hits, (double)gT, (double)gQ);
+      }
+      return;
+    }
+    // GetMatchProbabilityEx's sums, in its order (AlignProbability.cc:79-95).
+    double matches = 0.0, gcT = 0.0, gcQ = 0.0;
+    for (int i = 0; i < len; i++) {
+      const int a = st[s0 + i], b = sq[s0 + pos + i];
+      matches = __dadd_rn(matches, __ldg(&P.eq[a * 128 + b]));
+      gcT = __dadd_rn(gcT, __ldg(&P.gcw[a]));
+      gcQ = __dadd_rn(gcQ, __ldg(&P.gcw[b]));
+    }
+    score(key, pos, s0, len, matches, gcT, gcQ);
   };
 
   int rbase = 0, gbase = 0;   // rounds and byte-table groups of the earlier chunks
@@ -723,7 +748,17 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
           }
         }
         __syncthreads();
-        if (tid == 0) s_qn = 0;
+        // ---- the FP64 tail of the screen's survivors, one thread each ----
+        const int nsv = min(s_nsv, Gm::SVCAP);
+        for (int k = tid; k < nsv; k += NT_SCAN) {
+          const Surv v = surv[k];
+          score(v.key, v.pos, v.s0, v.len, (double)v.hits, (double)v.gT, (double)v.gQ);
+        }
+        __syncthreads();
+        if (tid == 0) {
+          s_qn = 0;
+          s_nsv = 0;
+        }
       }
       __syncthreads();
     }
