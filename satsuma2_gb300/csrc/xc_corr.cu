@@ -1,11 +1,17 @@
 // Correlation + FindTop kernels of the satsuma2 cross-correlation path (sm_103a).
 //
-// corr_pair_kernel<13>: at FFT 8192, one CTA of 1024 threads per chunk pair,
-// both strands from one set of spectra (A/C/G/T pairs whose query windows map
-// onto each other under reverse complement; described at the kernel).  Other
-// pairs it hands back on a list to
-// corr_kernel<log2 L>: one CTA of 512 threads per (chunk pair, strand), which
-// also runs every other FFT length.
+// At FFT 8192, both strands from one set of spectra (A/C/G/T pairs whose
+// query windows map onto each other under reverse complement; described at
+// corr_pair_kernel):
+//   corr_pair2_kernel<13>  persistent, one CTA of 512 threads per SM walking
+//                          the pairs (the default);
+//   corr_pair_kernel<13>   one CTA of 1024 threads per pair (a tuner form);
+//   spec_kernel<13> + corr_spec_kernel<13>  batches whose pairs share chunks:
+//                          each distinct chunk transformed once, each pair
+//                          correlated from the stored spectra.
+// Pairs outside the premise go on a hand-back list to
+// corr_kernel<log2 L, NT>: one CTA per (chunk pair, strand), which also runs
+// every other FFT length.  Its steps:
 //   1. chunk bytes to shared memory; strand 1 reverse-complements the query
 //   2. CCSignal: per-window entropy weights and per-channel means
 //   3. per channel: z = target_c + i*query_c; the even-bin group (threads
