@@ -1404,7 +1404,7 @@ size_t spec_bytes_per_chunk() { return (size_t)4 * 4096 * sizeof(float2); }
 
 static size_t spec_smem_bytes() {
   constexpr size_t N = 4096, NH = N / 64;
-  return (4 * N + 2 * (NH + 64)) * sizeof(float2)   // 4 transforms, twiddles
+  return (4 * N + 2 * (NH + 64) + 16 * TW16_ROW) * sizeof(float2)   // 4 transforms, twiddles
          + N                                        // chunk bytes
          + 256 * sizeof(float)                      // entropy weight per window
          + 2 * 256 * sizeof(float4)                 // window values per channel pair
@@ -1435,7 +1435,8 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
   float2* twNl = twNh + NH;
   float2* twLh = twNl + 64;
   float2* twLl = twLh + NH;
-  uint8_t* sb = reinterpret_cast<uint8_t*>(twLl + 64);
+  float2* tw16t = twLl + 64;   // twiddles of the span-256 pass (build_tw16_table)
+  uint8_t* sb = reinterpret_cast<uint8_t*>(tw16t + 16 * TW16_ROW);
   float* Es = reinterpret_cast<float*>(sb + N);
   float4* vv = reinterpret_cast<float4*>(Es + NWIN);     // [channel pair][window]
   uint32_t* cw = reinterpret_cast<uint32_t*>(vv + 2 * NWIN);
@@ -1458,6 +1459,8 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
     twLl[tid] = S.tab.twL_lo[tid];
   }
   if ((int)blockIdx.x < S.count) spec_prefetch(S, blockIdx.x, sb, tid);
+  __syncthreads();
+  build_tw16_table(tw16t, twNh, twNl, N / 256, tid);   // read after the first barrier of the loop
   // chunks in the order take_item gives, each taken one chunk ahead, as
   // corr_pair2_kernel takes its pairs
   const int SR = static_rounds(S.count);
@@ -1563,7 +1566,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
     gb();
     first_pass_from_codes(cw[g], len, vv + G * NWIN + (g >> 4), g, c0, c1, twLh, twLl, twNh, twNl, bE, bO);
     gb();
-    fft_pass16_x2<N, N / 16>(bE, bO, twNh, twNl, g);
+    fft_pass16_x2_tab<N, N / 16>(bE, bO, tw16t, g);
     gb();
     fft_pass16_x2<N, N / 256>(bE, bO, twNh, twNl, g);
     gb();
@@ -1588,14 +1591,13 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
 
 static size_t corr_spec_smem_bytes() {
   constexpr size_t N = 4096, NH = N / 64;
-  return (2 * N + 2 * N + 16 + 2 * (NH + 64)) * sizeof(float2);   // 2 inverses, F and R sums, twiddles
+  return (2 * N + 2 * N + 16 + 2 * (NH + 64) + 16 * TW16_ROW) * sizeof(float2);   // 2 inverses, F and R sums, twiddles
 }
 
 template <int LOG2L>
 __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams P) {
   constexpr int L = 1 << LOG2L;
   constexpr int N = L >> 1;
-  constexpr int LOG2N = LOG2L - 1;
   constexpr int WIN = L / 512;
   constexpr int NH = N / 64;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1609,6 +1611,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
   float2* twNl = twNh + NH;
   float2* twLh = twNl + 64;
   float2* twLl = twLh + NH;
+  float2* tw16t = twLl + 64;   // twiddles of the span-256 inverse pass (build_tw16_table)
   __shared__ int s_warp[2][2 * 256 / 32];
   __shared__ int s_take;   // the CTA's next pair
 
@@ -1625,6 +1628,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
     twLl[tid] = P.tab.twL_lo[tid];
   }
   __syncthreads();
+  build_tw16_table(tw16t, twNh, twNl, N / 256, tid);   // read after the loop's barriers
   // pairs in the order take_item gives, each taken one pair ahead, as
   // corr_pair2_kernel takes them
   const int S = static_rounds(P.count);
@@ -1708,7 +1712,12 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
           twLh, twLl, g, 1.0f);
     }
     gb();
-    fft_inverse<LOG2N, Plan<LOG2N>, Plan<LOG2N>::n - 1, GroupBarrier>(buf, twNh, twNl, g, 256, gb);
+    fft_pass<16, N, 16, true>(buf, twNh, twNl, g, 256);
+    gb();
+    fft_pass16_inv_tab<N, 256>(buf, tw16t, g);
+    gb();
+    fft_pass<16, N, N, true>(buf, twNh, twNl, g, 256);
+    gb();
     find_top<LOG2L, 256, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, G, buf, g, s_warp[G], gb,
                                        1.0f / (float)(4 * N));
     if (tid == 0) s_take = take;

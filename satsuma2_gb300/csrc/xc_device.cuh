@@ -238,6 +238,71 @@ __device__ __forceinline__ void fft_pass16_x2(float2* __restrict__ bufA, float2*
   }
 }
 
+// Twiddles of the radix-16 passes whose butterflies have j < 16 (span S =
+// 16 * 16: the forward pass after the first, the inverse pass before the
+// last): row j of 17 entries holds W_N^(j r N/S) for r < 16, the same
+// products tw16 / fft_pass form (so the values are identical), one row per
+// j; the odd row length spreads a half-warp's rows over the banks.
+constexpr int TW16_ROW = 17;
+__device__ __forceinline__ void build_tw16_table(float2* tab, const float2* twh, const float2* twl, int m_step, int t) {
+  if (t >= 256) return;
+  const int j = t >> 4, r = t & 15;
+  const Tw16 tw = tw16(twh, twl, j * m_step);
+  const int a = r >> 2, bb = r & 3;
+  const float2 wa = a == 1 ? tw.w4 : a == 2 ? tw.w8 : tw.w12;
+  const float2 wb = bb == 1 ? tw.w1 : bb == 2 ? tw.w2 : tw.w3;
+  tab[j * TW16_ROW + r] = r == 0 ? make_float2(1.f, 0.f) : a == 0 ? wb : bb == 0 ? wa : cmul(wa, wb);
+}
+
+// fft_pass16_x2 for span S = 256 (j < 16) with the twiddles from the table.
+template <int N, int S>
+__device__ __forceinline__ void fft_pass16_x2_tab(float2* __restrict__ bufA, float2* __restrict__ bufB,
+                                                  const float2* __restrict__ tab, int b) {
+  constexpr int d = S / 16;
+  static_assert(d == 16, "table rows are j < 16");
+  const int j = b & (d - 1);
+  const int sb = swz((b - j) * 16 + j);
+  float2 xa[16], xb[16];
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    xa[r] = bufA[sb ^ swz(r * d)];
+    xb[r] = bufB[sb ^ swz(r * d)];
+  }
+  DFT<16, -1>::run(xa);
+  DFT<16, -1>::run(xb);
+  const float2* tr = tab + j * TW16_ROW;
+#pragma unroll
+  for (int r = 1; r < 16; r++) {
+    const float2 w = tr[r];
+    xa[r] = cmul(xa[r], w);
+    xb[r] = cmul(xb[r], w);
+  }
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    bufA[sb ^ swz(r * d)] = xa[r];
+    bufB[sb ^ swz(r * d)] = xb[r];
+  }
+}
+
+// The inverse radix-16 pass of span S = 256 (fft_pass<16, N, 256, true>) for
+// butterfly b, its twiddles from the table.
+template <int N, int S>
+__device__ __forceinline__ void fft_pass16_inv_tab(float2* __restrict__ buf, const float2* __restrict__ tab, int b) {
+  constexpr int d = S / 16;
+  static_assert(d == 16, "table rows are j < 16");
+  const int j = b & (d - 1);
+  const int sb = swz((b - j) * 16 + j);
+  float2 x[16];
+#pragma unroll
+  for (int r = 0; r < 16; r++) x[r] = buf[sb ^ swz(r * d)];
+  const float2* tr = tab + j * TW16_ROW;
+#pragma unroll
+  for (int r = 1; r < 16; r++) x[r] = cmulc(x[r], tr[r]);
+  DFT<16, 1>::run(x);
+#pragma unroll
+  for (int r = 0; r < 16; r++) buf[sb ^ swz(r * d)] = x[r];
+}
+
 // One in-place pass of span S and radix R over an N-point buffer.
 // Forward (decimation in frequency): butterfly, then twiddle W_S^(j r').
 // Inverse (decimation in time, the exact reverse): conjugate twiddle, then
