@@ -240,9 +240,9 @@ __device__ __forceinline__ void fft_pass16_x2(float2* __restrict__ bufA, float2*
 
 // Twiddles of the radix-16 passes whose butterflies have j < 16 (span S =
 // 16 * 16: the forward pass after the first, the inverse pass before the
-// last): row j of 17 entries holds W_N^(j r N/S) for r < 16, the same
-// products tw16 / fft_pass form (so the values are identical), one row per
-// j; the odd row length spreads a half-warp's rows over the banks.
+// last): row j of 17 entries holds W_N^(j r N/S) for r < 16, formed by the
+// same products as tw16 / fft_pass, one row per j; the odd row length
+// spreads a half-warp's rows over the banks.
 constexpr int TW16_ROW = 17;
 __device__ __forceinline__ void build_tw16_table(float2* tab, const float2* twh, const float2* twl, int m_step, int t) {
   if (t >= 256) return;
