@@ -1262,6 +1262,8 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
           P.off_cnt[pidx * 2] = 0;
           P.off_cnt[pidx * 2 + 1] = 0;
           P.pair_flags[pidx] = PF_INVALID;
+        } else if (P.fb2_list && !(flg & 2u) && !P.dbg_sig) {
+          P.fb2_list[atomicAdd(P.fb2_cnt, 1)] = pidx;   // a ragged query window: corr_rcq_kernel takes it
         } else {
           P.fb_list[atomicAdd(P.fb_cnt, 1)] = pidx;   // the per-strand kernel takes it
         }
@@ -1401,6 +1403,328 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
 // the same bit for bit, and runs the inverses and FindTop.
 // ---------------------------------------------------------------------------
 size_t spec_bytes_per_chunk() { return (size_t)4 * 4096 * sizeof(float2); }
+
+// ---------------------------------------------------------------------------
+// corr_rcq_kernel<13>: both strands of an A/C/G/T pair whose query is at least
+// 1024 bases and not a multiple of the entropy window (16).  There the
+// reverse-complemented query's windows do not map onto the forward ones, so
+// the reverse strand's query signal is its own (CCSignal over the reverse
+// complement, as the reference builds it), and the spectra cannot be shared
+// the way corr_pair2_kernel shares them.  The target is still transformed
+// once for both strands (two per-strand CTAs transform it twice): per channel
+// pair, group 0 transforms the target and group 1 the forward query (two
+// transforms each, as corr_pair2_kernel), the forward sum takes
+// f = conj(A) C + B conj(D); then group 0 transforms the reverse-complemented
+// query's even-bin signal and group 1 its odd-bin signal, and the reverse
+// sum takes the same formula.  12 forward and 2 inverse half-length
+// transforms per pair, where two corr_kernel CTAs take 16 and 2.  The pairs
+// come from corr_pair2_kernel's second hand-back list, already checked to be
+// A/C/G/T; CTAs stride over it.
+// ---------------------------------------------------------------------------
+size_t corr_rcq_smem_bytes() {
+  return corr_pair2_smem_bytes() + 256 * sizeof(float)   // reverse-complement window weights
+         + 256 * sizeof(float4)                          // its window values
+         + 256 * sizeof(uint32_t);                       // its codes of positions g + 256 r
+}
+
+// First forward pass of one transform of the packed signal z = s_c0 + i s_c1
+// (ODD: the odd-bin transform, input z W_L^n), input built in registers as in
+// first_pass_from_codes; thread g takes butterfly g.
+template <bool ODD>
+__device__ __forceinline__ void first_pass_one(uint32_t codes, int len, const float4* __restrict__ vw, int g, int c0,
+                                               int c1, const float2* twLh, const float2* twLl, const float2* twNh,
+                                               const float2* twNl, float2* __restrict__ buf) {
+  float2 x[16];
+  float2 wg = make_float2(1.f, 0.f);
+  if (ODD) wg = tw2(twLh, twLl, g);
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    const float4 v = vw[16 * r];
+    const uint32_t code = (codes >> (2 * r)) & 3u;
+    float2 z = make_float2(0.f, 0.f);
+    if (g + 256 * r < len) z = make_float2(code == (uint32_t)c0 ? v.y : v.x, code == (uint32_t)c1 ? v.w : v.z);
+    x[r] = ODD ? cmul(cmul(z, wg), make_float2(cos_pi16(r), -sin_pi16(r))) : z;
+  }
+  DFT<16, -1>::run(x);
+  const Tw16 tw = tw16(twNh, twNl, g);
+#pragma unroll
+  for (int r = 1; r < 16; r++) x[r] = cmul(x[r], tw16_r(tw, r));
+  const int sb = swz(g);
+#pragma unroll
+  for (int r = 0; r < 16; r++) buf[sb ^ swz(256 * r)] = x[r];
+}
+
+template <int LOG2L>
+__global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams P) {
+  constexpr int L = 1 << LOG2L;
+  constexpr int N = L >> 1;
+  constexpr int LOG2N = LOG2L - 1;
+  constexpr int WIN = L / 512;
+  constexpr int NWIN = 256;
+  constexpr int NH = N / 64;
+  static_assert(N == 16 * NWIN && N == 4096 && WIN == 16, "thread g of a group owns positions g + 256 r, r < 16");
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* ZE = reinterpret_cast<float2*>(smem);   // z = t_c0 + i t_c1, even-bin transform
+  float2* ZO = ZE + N;                            // z * W_L^n, odd-bin transform
+  float2* WE = ZO + N;                            // w = q_c0 + i q_c1, then the reverse complement's
+  float2* WO = WE + N;
+  float2* aFE = WO + N;                           // 2 x forward-strand sum, bins 2m, m <= N/2
+  float2* aFO = aFE + (N / 2 + 8);                // bins 2m+1
+  float2* aRE = aFO + N / 2;                      // 2 x reverse-strand sum, bins 2m (m < N/2)
+  float2* aRO = aRE + (N / 2 + 8);                // bins 2m+1 (m < N/2 - 1)
+  float2* twNh = aRO + N / 2;
+  float2* twNl = twNh + NH;
+  float2* twLh = twNl + 64;
+  float2* twLl = twLh + NH;
+  uint8_t* st = reinterpret_cast<uint8_t*>(twLl + 64);
+  uint8_t* sq = st + N;
+  float* Et = reinterpret_cast<float*>(sq + N);
+  float* Eq = Et + NWIN;
+  float4* vv = reinterpret_cast<float4*>(Eq + NWIN);   // [sequence][window]: c0 (w=0, w=1), c1 (w=0, w=1)
+  uint32_t* cw = reinterpret_cast<uint32_t*>(vv + 2 * NWIN);   // [sequence][g]
+  float* Er = reinterpret_cast<float*>(cw + 2 * NWIN);        // reverse complement: window weights
+  float4* vr = reinterpret_cast<float4*>(Er + NWIN);          // its window values
+  uint32_t* cr = reinterpret_cast<uint32_t*>(vr + NWIN);      // its codes of positions g + 256 r
+  __shared__ int s_cnt4[8];
+  __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
+  __shared__ Split3 s_wf[2][8];    // the same as three floats each
+  __shared__ int s_warp[2][2 * 256 / 32];
+
+  const int tid = threadIdx.x;
+  const int G = tid >> 8;
+  const int g = tid & 255;
+  const GroupBarrier gb{1 + G, 256};
+  const int count = *P.fb2_cnt;
+
+  for (int i = tid; i < NH; i += NT_PAIR2) {
+    twNh[i] = P.tab.twN_hi[i];
+    twLh[i] = P.tab.twL_hi[i];
+  }
+  if (tid < 64) {
+    twNl[tid] = P.tab.twN_lo[tid];
+    twLl[tid] = P.tab.twL_lo[tid];
+  }
+  if ((int)blockIdx.x < count) pair2_prefetch(P, P.fb2_list[blockIdx.x], st, sq, tid);
+
+  for (int p = blockIdx.x; p < count; p += gridDim.x) {
+    const int pidx = P.fb2_list[p];
+    const int next = p + (int)gridDim.x < count ? P.fb2_list[p + gridDim.x] : -1;
+    const int T = P.pairs[pidx].tlen, Q = P.pairs[pidx].qlen;
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    if (tid < 8) s_cnt4[tid] = 0;
+    __syncthreads();   // the chunk bytes are in; the counters are zero
+
+    // ---- 1. thread (G, g): bytes 16g..16g+15 of sequence G (entropy window
+    //      g): 2-bit codes, base counts, window weight, as corr_pair2_kernel.
+    //      The query's last reverse window (the reverse complement's
+    //      positions 16k.. with fewer than 16 left) is weighed here from the
+    //      bytes; its full windows after the barrier, from the codes. ----
+    uint32_t* cwin = reinterpret_cast<uint32_t*>(vv);   // [sequence][window] codes; vv is free until step 3
+    {
+      const int len = G ? Q : T;
+      const int valid = len - 16 * g;
+      const uint8_t* sb = G ? sq : st;
+      const uint4 v = *reinterpret_cast<const uint4*>(sb + 16 * g);
+      const uint32_t x[4] = {v.x, v.y, v.z, v.w};
+      uint32_t p0 = 0u, p1 = 0u, codes = 0u;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int vk = min(max(valid - 4 * k, 0), 4);
+        const uint32_t m = vk >= 4 ? 0xffffffffu : (1u << (8 * vk)) - 1u;
+        const uint32_t cd = ((x[k] >> 1) ^ (x[k] >> 2)) & 0x03030303u & m;
+        p0 |= (((cd & 0x01010101u) * 0x10204080u) >> 28) << (4 * k);
+        p1 |= ((((cd >> 1) & 0x01010101u) * 0x10204080u) >> 28) << (4 * k);
+        const uint32_t c2 = cd | (cd >> 6);
+        codes |= ((c2 & 0xfu) | ((c2 >> 12) & 0xf0u)) << (8 * k);
+      }
+      cwin[tid] = codes;
+      const int nv = min(max(valid, 0), 16);
+      const int nt = __popc(p0 & p1), nc = __popc(p0) - nt, ng = __popc(p1) - nt, na = nv - nc - ng - nt;
+      auto partial = [&](const uint8_t* bytes, int n, bool rc) -> float {
+        int a4 = 0, c4 = 0, g4 = 0, t4 = 0;
+        for (int j = 0; j < n; j++) {
+          const unsigned b = bytes[j];
+          const uchar4 q = c_w4q[rc ? c_rc[b] : b];
+          a4 += q.x; c4 += q.y; g4 += q.z; t4 += q.w;
+        }
+        const double* et = P.tab.ent + n * (4 * WIN + 1);
+        const double sv =
+            __dadd_rn(__dadd_rn(__dadd_rn(__ldg(et + a4), __ldg(et + c4)), __ldg(et + g4)), __ldg(et + t4));
+        const float E = __double2float_rn(-sv);
+        return E < 0.f ? 0.f : E;
+      };
+      float E = 0.f;
+      if (len < 1024) E = 1.f;
+      else if (nv == 16) E = __ldg(&P.tab.ent_acgt[(na * (WIN + 1) + nc) * (WIN + 1) + ng]);
+      else if (nv > 0) E = partial(sb + 16 * g, nv, false);
+      (G ? Eq : Et)[g] = E;
+      if (G == 1) {
+        // reverse window k = g: the reverse complement's positions 16k..16k+15,
+        // forward positions Q-16k-16..Q-16k-1; the last one is partial
+        const int nr = min(Q - 16 * g, 16);
+        if (nr > 0 && nr < 16) Er[g] = partial(sq, nr, true);   // forward positions 0..nr-1
+        else if (nr <= 0) Er[g] = 0.f;
+      }
+      const uint32_t lo = __reduce_add_sync(0xffffffffu, (uint32_t)na | ((uint32_t)nc << 16));
+      const uint32_t hi = __reduce_add_sync(0xffffffffu, (uint32_t)ng | ((uint32_t)nt << 16));
+      if ((tid & 31) == 0) {
+        atomicAdd(&s_cnt4[4 * G + 0], 4 * (int)(lo & 0xffffu));
+        atomicAdd(&s_cnt4[4 * G + 1], 4 * (int)(lo >> 16));
+        atomicAdd(&s_cnt4[4 * G + 2], 4 * (int)(hi & 0xffffu));
+        atomicAdd(&s_cnt4[4 * G + 3], 4 * (int)(hi >> 16));
+      }
+    }
+    __syncthreads();   // the chunk bytes are no longer read: the next pair's may come in
+    if (next >= 0) pair2_prefetch(P, next, st, sq, tid);
+    if (tid == 0) P.pair_flags[pidx] = P.pairs[pidx].flags & PF_FAST;
+    // ---- 2. channel means (FP64); the codes of positions g + 256 r of the
+    //      target, the query and the reverse complement (3 - the code of
+    //      forward position Q-1-n); the reverse complement's full windows
+    //      (its counts are the forward counts of the complement bases) ----
+    if (tid < 8) {
+      const int len = (tid >> 2) ? Q : T;
+      const double off = len > 0 ? __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len) : 0.0;
+      s_wmo[0][tid] = __dsub_rn(0.0, off);
+      s_wmo[1][tid] = __dsub_rn(1.0, off);
+      s_wf[0][tid] = split3(s_wmo[0][tid]);
+      s_wf[1][tid] = split3(s_wmo[1][tid]);
+    }
+    {
+      const uint32_t* cs = cwin + G * NWIN + (g >> 4);
+      const int sh = 2 * (g & 15);
+      uint32_t w = 0;
+#pragma unroll
+      for (int r = 0; r < 16; r++) w |= ((cs[16 * r] >> sh) & 3u) << (2 * r);
+      cw[tid] = w;
+    }
+    const uint32_t* cq = cwin + NWIN;   // the query's codes per window
+    if (G == 0) {
+      uint32_t w = 0;
+#pragma unroll
+      for (int r = 0; r < 16; r++) {
+        const int m = Q - 1 - (g + 256 * r);
+        if (m >= 0) w |= (3u - ((cq[m >> 4] >> (2 * (m & 15))) & 3u)) << (2 * r);
+      }
+      cr[g] = w;
+    } else if (Q - 16 * g >= 16) {
+      const int a = Q - 16 * g - 16;   // forward positions a..a+15
+      const int wa = a >> 4, sh = 2 * (a & 15);
+      const uint32_t c16 = __funnelshift_r(cq[wa], wa + 1 < NWIN ? cq[wa + 1] : 0u, sh);
+      const int nt = __popc(c16 & (c16 >> 1) & 0x55555555u), nc = __popc(c16 & 0x55555555u) - nt,
+                ng = __popc(c16 & 0xaaaaaaaau) - nt, na = 16 - nc - ng - nt;
+      // reverse complement: A <- T, C <- G, G <- C
+      Er[g] = Q < 1024 ? 1.f : __ldg(&P.tab.ent_acgt[(nt * (WIN + 1) + ng) * (WIN + 1) + nc]);
+      (void)na;
+    }
+    __syncthreads();
+
+#pragma unroll 1
+    for (int stg = 0; stg < 2; stg++) {
+      const int c0 = stg ? 1 : 0, c1 = stg ? 2 : 3;
+      const bool first = stg == 0;
+      // ---- 3a. window values; the reverse complement's channel c has the
+      //      forward query's mean of comp(c) = 3 - c ----
+      vv[G * NWIN + g] = window_values((G ? Eq : Et)[g], s_wf, s_wmo, G * 4 + c0, G * 4 + c1);
+      if (G == 0) vr[g] = window_values(Er[g], s_wf, s_wmo, 4 + 3 - c0, 4 + 3 - c1);
+      __syncthreads();
+      // ---- 3b. target (group 0) and forward query (group 1), both
+      //      transforms of each ----
+      first_pass_from_codes(cw[tid], G ? Q : T, vv + G * NWIN + (g >> 4), g, c0, c1, twLh, twLl, twNh, twNl,
+                            G ? WE : ZE, (G ? WE : ZE) + N);
+      gb();
+      {
+        float2* bE = G ? WE : ZE;
+        fft_pass16_x2<N, N / 16>(bE, bE + N, twNh, twNl, g);
+        gb();
+        fft_pass16_x2<N, N / 256>(bE, bE + N, twNh, twNl, g);
+      }
+      __syncthreads();
+      // ---- 3c. forward sum f = conj(A) C + B conj(D); bins N-1 and N keep
+      //      the targets' own values (as corr_pair2_kernel) ----
+      auto per_bin = [&](const float2* VE, const float2* VO, float2* oE, float2* oO, bool fwd) {
+        if (G == 0) {
+          const int la = lp<LOG2N>(g);
+          const int lb = lp<LOG2N>((256 - g) & 255);
+#pragma unroll
+          for (int it = 0; it <= N / 512; it++) {
+            const int m = g + 256 * it;
+            if (m > N / 2) break;
+            const int pa = la ^ lp<LOG2N>(256 * it);
+            const int pb = g ? (lb ^ lp<LOG2N>(N - 256 * (it + 1))) : lp<LOG2N>((N - 256 * it) & (N - 1));
+            const float2 A = ZE[pa];
+            if (m == N / 2) {
+              if (fwd) {
+                const float2 f = pair_bin_nyquist(A);
+                oE[m] = first ? f : cadd(oE[m], f);
+              }
+            } else {
+              const float2 B = ZE[pb], C = VE[pa], D = VE[pb];
+              const float2 f = cadd(cmulc(C, A), cmulc(B, D));
+              oE[m] = first ? f : cadd(oE[m], f);
+            }
+          }
+        } else {
+          const int la = lp<LOG2N>(g);
+#pragma unroll
+          for (int it = 0; it < N / 512; it++) {
+            const int m = g + 256 * it;
+            const int pa = la ^ lp<LOG2N>(256 * it);
+            const int pb = pa ^ lp<LOG2N>(N - 1);
+            const float2 A = ZO[pa], B = ZO[pb];
+            if (m == N / 2 - 1) {
+              if (fwd) {
+                const float2 f = pair_bin_nm1(A, B);
+                oO[m] = first ? f : cadd(oO[m], f);
+              }
+            } else {
+              const float2 C = VO[pa], D = VO[pb];
+              const float2 f = cadd(cmulc(C, A), cmulc(B, D));
+              oO[m] = first ? f : cadd(oO[m], f);
+            }
+          }
+        }
+      };
+      per_bin(WE, WO, aFE, aFO, true);
+      __syncthreads();
+      // ---- 3d. the reverse complement's even-bin (group 0) and odd-bin
+      //      (group 1) transforms, one per group ----
+      {
+        float2* b = G ? WO : WE;
+        if (G) first_pass_one<true>(cr[g], Q, vr + (g >> 4), g, c0, c1, twLh, twLl, twNh, twNl, b);
+        else first_pass_one<false>(cr[g], Q, vr + (g >> 4), g, c0, c1, twLh, twLl, twNh, twNl, b);
+        gb();
+        fft_pass<16, N, N / 16, false>(b, twNh, twNl, g, 256);
+        gb();
+        fft_pass<16, N, N / 256, false>(b, twNh, twNl, g, 256);
+      }
+      __syncthreads();
+      // ---- 3e. reverse sum, the same formula over the reverse complement ----
+      per_bin(WE, WO, aRE, aRO, false);
+      __syncthreads();
+    }
+
+    // ---- 4. inverses: group 0 the forward strand into ZE, group 1 the
+    //      reverse strand into WE (bins N-1 and N: the targets' own values,
+    //      the same for both strands).  Sums and the pack carry factors 2
+    //      and 2: FindTop scales by 1/(4N). ----
+    float2* buf = G ? WE : ZE;
+    auto SF = [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; };
+    auto SRc = [&](int k) -> float2 {
+      if (k >= N - 1) return (k & 1) ? aFO[k >> 1] : aFE[k >> 1];
+      return (k & 1) ? aRO[k >> 1] : aRE[k >> 1];
+    };
+    if (G == 0) hermitian_pack<LOG2L, 256>(ZE, both_bins<N>(SF), twLh, twLl, g, 1.0f);
+    else hermitian_pack<LOG2L, 256>(WE, both_bins<N>(SRc), twLh, twLl, g, 1.0f);
+    gb();
+    fft_inverse<LOG2N, Plan<LOG2N>, Plan<LOG2N>::n - 1, GroupBarrier>(buf, twNh, twNl, g, 256, gb);
+    // ---- 5. FindTop, one strand per group ----
+    find_top<LOG2L, 256, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, G, buf, g, s_warp[G], gb,
+                                       1.0f / (float)(4 * N));
+    __syncthreads();   // buffers and per-pair words are reused by the next pair
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
 
 static size_t spec_smem_bytes() {
   constexpr size_t N = 4096, NH = N / 64;
@@ -1648,6 +1972,8 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
           P.off_cnt[pidx * 2] = 0;
           P.off_cnt[pidx * 2 + 1] = 0;
           P.pair_flags[pidx] = PF_INVALID;
+        } else if (P.fb2_list && !fl && !P.dbg_sig) {
+          P.fb2_list[atomicAdd(P.fb2_cnt, 1)] = pidx;   // a ragged query window: corr_rcq_kernel takes it
         } else {
           P.fb_list[atomicAdd(P.fb_cnt, 1)] = pidx;
         }
@@ -1767,6 +2093,9 @@ cudaError_t prepare_kernels() {
   e = cudaFuncSetAttribute(corr_pair2_kernel<PAIR_LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)corr_pair2_smem_bytes());
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(corr_rcq_kernel<PAIR_LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)corr_rcq_smem_bytes());
+  if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(spec_kernel<PAIR_LOG2L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)spec_smem_bytes());
   if (e != cudaSuccess) return e;
@@ -1804,10 +2133,14 @@ cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t
     }();
     CorrParams q = p;
     q.count = npairs;
-    if (p.pair_form == 2)   // persistent: one CTA per SM strides over the pairs
+    if (p.pair_form == 2) {   // persistent: one CTA per SM strides over the pairs
       corr_pair2_kernel<PAIR_LOG2L><<<std::min(npairs, sms), NT_PAIR2, corr_pair2_smem_bytes(), s>>>(q);
-    else
+      if (p.fb2_list)   // the pairs with a ragged query window it handed on
+        corr_rcq_kernel<PAIR_LOG2L><<<std::min(npairs, sms), NT_PAIR2, corr_rcq_smem_bytes(), s>>>(q);
+    } else {
+      q.fb2_list = nullptr;
       corr_pair_kernel<PAIR_LOG2L><<<npairs, NT_PAIR, corr_pair_smem_bytes(PAIR_LOG2L), s>>>(q);
+    }
     grid.x = std::min(npairs, sms * (NT_CORR / nt));
   }
   const cudaError_t e = cudaGetLastError();
@@ -1827,6 +2160,8 @@ cudaError_t launch_corr_spec(const SpecParams& sp, const CorrParams& p, int npai
   CorrParams q = p;
   q.count = npairs;
   corr_spec_kernel<PAIR_LOG2L><<<std::min(npairs, sms), NT_PAIR2, corr_spec_smem_bytes(), s>>>(q);
+  if (p.fb2_list)   // the pairs with a ragged query window it handed on
+    corr_rcq_kernel<PAIR_LOG2L><<<std::min(npairs, sms), NT_PAIR2, corr_rcq_smem_bytes(), s>>>(q);
   // the pairs handed back: one wave of per-strand CTAs striding over the list
   CorrParams h = p;
   h.pair_chunk = nullptr;

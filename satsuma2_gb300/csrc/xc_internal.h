@@ -91,6 +91,8 @@ struct CorrParams {
   float2* acc;              // L > 2^MAX_SMEM_LOG2L: channel sums, [pair*2+strand][acc_stride(log2L)]
   int* fb_list;             // log2L == PAIR_LOG2L: both-strands kernel first; the pairs it
   int* fb_cnt;              //   hands back ([*fb_cnt], zeroed before) go to corr_kernel
+  int* fb2_list;            // optional: the A/C/G/T pairs with a ragged query window the
+  int* fb2_cnt;             //   persistent kernel hands to corr_rcq_kernel ([*fb2_cnt], zeroed before)
   int* strad_cnt;           // optional: near-threshold lags per [pair*2 + strand] (zeroed before)
   int* strad_list;          //   and the first STRAD_CAP of them, [pair*2 + strand][STRAD_CAP]
   int count;                // pairs of this launch (set by launch_corr)

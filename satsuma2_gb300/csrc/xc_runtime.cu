@@ -367,7 +367,7 @@ Batch::~Batch() {
     if (e) cudaEventDestroy(e);
   cudaFree(d_pool); cudaFree(d_desc); cudaFree(d_off); cudaFree(d_offcnt); cudaFree(d_flags);
   cudaFree(d_res); cudaFree(d_rescnt); cudaFree(d_ovf); cudaFree(d_misc); cudaFree(d_base);
-  cudaFree(d_dense); cudaFree(d_dbg); cudaFree(d_dbg_sig); cudaFree(d_dbg_xc); cudaFree(d_acc); cudaFree(d_fb);
+  cudaFree(d_dense); cudaFree(d_dbg); cudaFree(d_dbg_sig); cudaFree(d_dbg_xc); cudaFree(d_acc); cudaFree(d_fb); cudaFree(d_fb2);
   cudaFree(d_stradcnt); cudaFree(d_strad);
   cudaFree(d_chunks); cudaFree(d_pairchunk); cudaFree(d_spec); cudaFree(d_chunkflags);
   cudaFreeHost(h_pool); cudaFreeHost(h_desc); cudaFreeHost(h_base); cudaFreeHost(h_dense);
@@ -464,6 +464,7 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
     }
     return e.off;
   };
+  int ragged = 0;
   for (size_t d = 0; d < n; d++) {
     const xc_pair& p = pairs[b->order[d]];
     const int lg = b->log2L[b->order[d]];
@@ -485,7 +486,9 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
     D.off_base = (uint32_t)offl;
     D.pad = 0;
     offl += 2ull << lg;
+    if (lg == PAIR_LOG2L && p.qlen >= 1024 && p.qlen % 16 != 0) ragged++;
   }
+  b->ragged = ragged;
   if (pool >= (1ull << 32) || offl >= (1ull << 32)) return XC_ERR_ARG;
   const size_t nslots = 2 * n;
   const size_t slots = (size_t)b->slots;
@@ -502,6 +505,7 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   if ((r = dev_grow(b->d_ovf, b->cap_ovf, (size_t)b->ovf_cap)) != XC_OK) return r;
   if ((r = dev_grow(b->d_misc, b->cap_misc, 8)) != XC_OK) return r;
   if ((r = dev_grow(b->d_fb, b->cap_fb, n)) != XC_OK) return r;
+  if (ragged && (r = dev_grow(b->d_fb2, b->cap_fb2, (size_t)ragged)) != XC_OK) return r;
   if ((r = dev_grow(b->d_stradcnt, b->cap_stradcnt, nslots)) != XC_OK) return r;
   if ((r = dev_grow(b->d_strad, b->cap_strad, nslots * STRAD_CAP)) != XC_OK) return r;
   if ((r = dev_grow(b->d_base, b->cap_base, nslots + 1)) != XC_OK) return r;
@@ -606,6 +610,10 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
       cp.fb_list = b->d_fb;
       cp.fb_cnt = b->d_misc + 3;   // zeroed above
       cp.pair_form = c->pair_form;
+      if (c->pair_form == 2 && b->ragged) {
+        cp.fb2_list = b->d_fb2;
+        cp.fb2_cnt = b->d_misc + 6;   // zeroed above
+      }
     }
     cp.strand_threads = c->strand_threads[bk.log2L];
     cp.strad_cnt = b->d_stradcnt;
@@ -666,7 +674,10 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
 int batch_launch_count(const Ctx* c, const Batch* b) {
   int n = 2 * (int)b->buckets.size() + 2;
   for (const Bucket& bk : b->buckets)
-    if (bk.log2L == PAIR_LOG2L && c->pair_kernel) n += b->spec ? 2 : 1;   // (spectra,) pair kernel, hand-back
+    if (bk.log2L == PAIR_LOG2L && c->pair_kernel) {
+      n += b->spec ? 2 : 1;   // (spectra,) pair kernel, hand-back
+      if (c->pair_form == 2 && b->ragged) n++;   // ragged query windows
+    }
   return n;
 }
 

@@ -50,6 +50,8 @@ struct Batch {
   int* d_misc = nullptr;          size_t cap_misc = 0;   // [0] ovf count [1] err [2] dbg count
                                                          // [3] pairs corr_pair_kernel handed back
   int* d_fb = nullptr;            size_t cap_fb = 0;     // those pairs' indices
+  int* d_fb2 = nullptr;           size_t cap_fb2 = 0;    // A/C/G/T pairs with a ragged query window it handed on
+  int ragged = 0;                 // FFT-8192 pairs whose query is >= 1024 bases and not a multiple of 16
   int* d_stradcnt = nullptr;      size_t cap_stradcnt = 0;   // near-threshold lags per pair strand
   int* d_strad = nullptr;         size_t cap_strad = 0;      // the first STRAD_CAP of them
   // spectra path of the FFT-8192 bucket (its pairs share chunks): distinct

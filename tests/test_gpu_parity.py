@@ -522,6 +522,59 @@ def test_mixed_batch_both_kernels_vs_oracle(O):
     x.close()
 
 
+def test_ragged_query_kernel_vs_oracle(O, monkeypatch):
+    """A/C/G/T pairs whose query is at least 1024 bases and not a multiple of
+    the 16-base entropy window, so that the reverse complement's windows do
+    not line up with the forward query's: the both-strands kernel hands them
+    on to corr_rcq_kernel, one more launch.  Their offsets agree with the
+    oracle's FP64 correlation and with the per-strand kernel's except inside
+    the straddle band, and every pair's records equal the oracle's over the
+    batch's own offsets.  Aligned pairs (a 4096-base and a 1008-base query)
+    share the launch."""
+    import satsuma2_gb300 as sg
+    rng = np.random.default_rng(61)
+    qlens = [1025, 1031, 1039, 1503, 2047, 2049, 3001, 3333, 4081, 4089, 4095, 4096, 1008]
+    items = []
+    for k, ql in enumerate(qlens * 2):
+        t = W.random_bases(rng, 4096 if k % 3 else 4091)
+        a = int(rng.integers(0, 4096 - 1000))
+        seg = W.mutate(rng, t[a:a + min(ql, len(t) - a)], 0.85, indel_every=0)
+        q = np.concatenate([seg, W.random_bases(rng, ql - len(seg))])
+        q = W.revcomp(q) if k % 2 else q
+        items.append((t.tobytes(), q.tobytes()))
+    TT = 4096.0 * len(items)
+    x2 = sg.XCorr(target_total=TT)
+    monkeypatch.setenv("SATSUMA2_GB300_PAIR_KERNEL", "0")
+    x1 = sg.XCorr(target_total=TT)
+    monkeypatch.delenv("SATSUMA2_GB300_PAIR_KERNEL")
+    b = x2.upload(items)
+    # both-strands kernel, ragged-query kernel, hand-back, scan, two finalize kernels
+    assert b.launches() == 6
+    b.run()
+    res, counts = b.results(with_counts=True)
+    offs = b.offsets()
+    P = O.params(target_total=TT)
+    o = 0
+    n_rec = [0, 0]
+    for k, (t, q) in enumerate(items):
+        got = res[o:o + int(counts[k])]
+        o += int(counts[k])
+        n_rec[k % 2] += len(got)
+        want, _ = O.align_pair(P, O.pair(t, q), offsets_in=offs[k])
+        assert parity.same_results(got, want, target_total=TT), k
+        d1 = x1.debug_pair(t=t, q=q, signals=False)
+        _, det = O.align_pair(P, O.pair(t, q), want_detail=True)
+        case = dict(L=8192, cutoff=1.8, t=t)
+        for s, qq in enumerate((q, O.rc(q))):
+            band, _ = parity.straddles(O, case, qq, s)
+            parity.compare_offsets(offs[k][s], det["offsets"][s], band)
+            parity.compare_offsets(offs[k][s], d1["offsets"][s], band)
+    assert min(n_rec) > 0   # records on both strands' seeds
+    b.free()
+    x1.close()
+    x2.close()
+
+
 def test_strand_kernel_switch_vs_oracle(O, monkeypatch):
     """SATSUMA2_GB300_PAIR_KERNEL=0 at context creation runs every pair one
     CTA per strand; its records equal the oracle's over its own offsets, and
