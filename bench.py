@@ -742,8 +742,9 @@ def run_ours(args):
 
 def profile_case(args):
     """Fixed device-resident workload for profiler captures: uploads --pairs
-    seeded uniform 4096x4096 chunk pairs (FFT 8192), or with --case blocks
-    the pairs of 24x24 grid blocks of the genome workload, and runs the batch
+    seeded uniform 4096x4096 chunk pairs (FFT 8192), with --case blocks
+    the pairs of 24x24 grid blocks of the genome workload, with --case uneven
+    the uneven-length batch (FFT 1024..8192), and runs the batch
     --runs times without timing, so a profiler's launch list maps one-to-one
     onto runs (each run: the correlation kernels, the scan kernel and the
     two finalize kernels)."""
@@ -758,6 +759,9 @@ def profile_case(args):
             k += 1
         items = np.concatenate(items)[:args.pairs]
         x = sg.XCorr(target_total=float(len(tb)))
+    elif args.case == "uneven":   # uneven lengths over the FFT buckets 1024..8192
+        items = workloads.uneven_batch(args.pairs, seed=SEED)
+        x = sg.XCorr(fft_len=-1, target_total=float(sum(len(t) for t, _ in items)))
     else:
         items = workloads.uniform_batch(args.pairs, seed=SEED)
         x = sg.XCorr(target_total=TARGET_TOTAL)
@@ -782,8 +786,9 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="profiler workload only: upload --pairs pairs and run them --runs times, untimed")
     ap.add_argument("--pairs", type=int, default=N_PAIRS)
-    ap.add_argument("--case", default="uniform", choices=["uniform", "blocks"],
-                    help="profiler workload: uniform pairs, or 24x24 grid blocks of the genome workload")
+    ap.add_argument("--case", default="uniform", choices=["uniform", "blocks", "uneven"],
+                    help="profiler workload: uniform pairs, 24x24 grid blocks of the genome workload, "
+                         "or the uneven-length batch")
     ap.add_argument("--runs", type=int, default=3)
     args = ap.parse_args()
     if args.profile_case:
