@@ -149,6 +149,8 @@ struct ScanParams {
   double min_prob;
   double target_total;
   float screen_z;           // FP32 screen: reject when pm*N - hits > screen_z * sd (+inf keeps all)
+  uint32_t run_floor[8];    // bytes [r-1]: least equal-base count with which a run of r passing
+                            // checks can pass the screen (run_hits_floor; zeros: no floor)
   int min_len;
   int slots;                // result slots per pair strand
   DevResult* res;           // [pair*2+strand][slots]

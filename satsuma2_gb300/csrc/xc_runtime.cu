@@ -573,6 +573,38 @@ float screen_z(double min_prob, double target_total) {
   return (float)(hi + 0.02);
 }
 
+// Floors of the scan kernel's in-word runs.  A run of r passing checks
+// (r = 1..32) makes a segment of N = r + 45 bases with h equal bases; equal
+// bases agree in G+C, so the two sequences' G+C counts differ by at most
+// N - h, and pm = (gT gQ + (N-gT)(N-gQ)) / 2N^2 >= (1 - m^2) / 4 with
+// m = 1 - h/N (the minimum over that band).  For pm <= 1/2 and pm N < h,
+// z = (pm N - h) / sqrt(pm (1 - pm) N) grows with pm, so z >= z_min(h, N)
+// at pm = (1 - m^2) / 4.  Byte r-1 of out is the least h with
+// z_min(h, N) <= screen_z (+1e-6); every h below it has z > screen_z for
+// every composition, which the screen rejects (and the exact test after it).
+// Segments shorter than min_len get 255.  Zeros (no floor) when the screen
+// keeps everything or is not negative.
+void run_hits_floor(float screen_z, int min_len, uint32_t out[8]) {
+  for (int k = 0; k < 8; k++) out[k] = 0u;
+  if (!(screen_z < 0.f) || !std::isfinite(screen_z)) return;
+  const double sz = (double)screen_z + 1e-6;
+  for (int r = 1; r <= 32; r++) {
+    const int n = r + 45;
+    int floor_h = n + 1;
+    for (int h = 1; h <= n; h++) {
+      const double m = 1.0 - (double)h / n;
+      const double p = (1.0 - m * m) / 4.0;
+      const double z = p * n >= h ? 0.0 : (p * n - h) / sqrt(p * (1.0 - p) * n);
+      if (z <= sz) {
+        floor_h = h;
+        break;
+      }
+    }
+    if (n < min_len) floor_h = 255;
+    out[(r - 1) >> 2] |= (uint32_t)std::min(floor_h, 255) << (8 * ((r - 1) & 3));
+  }
+}
+
 
 // Enqueues the kernels of one batch on stream.
 static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
@@ -663,6 +695,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     sp.dbg = b->d_dbg;
     sp.dbg_cnt = b->d_misc + 2;
     sp.dbg_cap = b->dbg_cap;
+    if (!sp.dbg && !sp.ptable) run_hits_floor(sp.screen_z, sp.min_len, sp.run_floor);
     XC_CHECK(launch_scan(bk.log2L, sp, bk.count, s));
   }
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[2], s, evflags));

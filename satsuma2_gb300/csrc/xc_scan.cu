@@ -220,6 +220,7 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
   __shared__ int s_wsum[NWARP];
   __shared__ int s_next, s_res, s_qn, s_nsv;
   __shared__ int s_cy_start[2];
+  __shared__ uint32_t s_floor[8];   // P.run_floor
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int pidx = P.first + blockIdx.x;
@@ -245,6 +246,8 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
     s_res = 0;
     s_qn = 0;
     s_nsv = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s_floor[k] = P.run_floor[k];
   }
   if (generic) {
     // chunk bytes; strand 1 reverse-complements the query (DNAVector.cc:482-500)
@@ -698,6 +701,31 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
             gbits[i] = g;
             items[i] = it | (pb ? IT_PREV : 0u);
             runs_of(it, g, pb, fall, close);
+            // A run that starts and ends inside this word (checks a..b, r of
+            // them) makes the segment [a-45, b+1) of length r + 45, whose
+            // equal bases are at most window(b)'s count plus the r - 1
+            // positions before that window.  Below the floor for r no G+C
+            // composition lets it pass the probability screen, so the
+            // segment is dropped here instead of queued.
+            if (fall | close) {
+              const uint32_t rise = g & ~((g << 1) | pb);   // first checks of runs
+              const uint64_t U = ((uint64_t)e1 << 32) | e2;
+              const uint8_t* fl = reinterpret_cast<const uint8_t*>(s_floor);
+              auto hopeless = [&](int b) -> bool {
+                const uint32_t rs = rise & (0xffffffffu >> (31 - b));
+                if (!rs) return false;   // the run began in an earlier word
+                const int r = b - (31 - __clz((int)rs)) + 1;
+                const int wb = __popcll(U >> (b + 19)) + __popc(e0 & (0xffffffffu >> (31 - b)));
+                return wb + r - 1 < (int)fl[r - 1];
+              };
+              uint32_t f = fall & ~1u;   // bit 0: the run ended in the word before
+              while (f) {
+                const int u = __ffs(f) - 1;
+                f &= f - 1;
+                if (hopeless(u - 1)) fall &= ~(1u << u);
+              }
+              if (close && hopeless(hi)) close = false;
+            }
           }
           const int nseg = __popc(fall) + (close ? 1 : 0);
           const int sincl = warp_incl_sum(nseg, lane);
