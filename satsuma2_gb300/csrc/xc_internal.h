@@ -151,6 +151,7 @@ struct ScanParams {
   float screen_z;           // FP32 screen: reject when pm*N - hits > screen_z * sd (+inf keeps all)
   uint32_t run_floor[8];    // bytes [r-1]: least equal-base count with which a run of r passing
                             // checks can pass the screen (run_hits_floor; zeros: no floor)
+  int word_floor;           // the least of them (0: every screened word is marked)
   int min_len;
   int slots;                // result slots per pair strand
   DevResult* res;           // [pair*2+strand][slots]

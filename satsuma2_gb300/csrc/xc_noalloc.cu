@@ -190,7 +190,7 @@ int align_pair_noalloc(Ctx* c, const xc_pair& p, xc_result* out, size_t cap, siz
   sp.dbg = nullptr;
   sp.dbg_cnt = cnt + C_MISC + 2;
   sp.dbg_cap = 0;
-  if (!sp.ptable) run_hits_floor(sp.screen_z, sp.min_len, sp.run_floor);
+  if (!sp.ptable) sp.word_floor = run_hits_floor(sp.screen_z, sp.min_len, sp.run_floor);
   NA_CHECK(launch_scan(lg, sp, 1, s));
   NA_CHECK(launch_finalize(cnt + C_RESCNT, res, NA_SLOTS, 2, cnt + C_BASE, dense, nullptr, s));
 

@@ -583,10 +583,11 @@ float screen_z(double min_prob, double target_total) {
 // z_min(h, N) <= screen_z (+1e-6); every h below it has z > screen_z for
 // every composition, which the screen rejects (and the exact test after it).
 // Segments shorter than min_len get 255.  Zeros (no floor) when the screen
-// keeps everything or is not negative.
-void run_hits_floor(float screen_z, int min_len, uint32_t out[8]) {
+// keeps everything or is not negative.  Returns the least floor.
+int run_hits_floor(float screen_z, int min_len, uint32_t out[8]) {
   for (int k = 0; k < 8; k++) out[k] = 0u;
-  if (!(screen_z < 0.f) || !std::isfinite(screen_z)) return;
+  if (!(screen_z < 0.f) || !std::isfinite(screen_z)) return 0;
+  int least = 255;
   const double sz = (double)screen_z + 1e-6;
   for (int r = 1; r <= 32; r++) {
     const int n = r + 45;
@@ -601,8 +602,11 @@ void run_hits_floor(float screen_z, int min_len, uint32_t out[8]) {
       }
     }
     if (n < min_len) floor_h = 255;
-    out[(r - 1) >> 2] |= (uint32_t)std::min(floor_h, 255) << (8 * ((r - 1) & 3));
+    floor_h = std::min(floor_h, 255);
+    least = std::min(least, floor_h);
+    out[(r - 1) >> 2] |= (uint32_t)floor_h << (8 * ((r - 1) & 3));
   }
+  return least;
 }
 
 
@@ -695,7 +699,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     sp.dbg = b->d_dbg;
     sp.dbg_cnt = b->d_misc + 2;
     sp.dbg_cap = b->dbg_cap;
-    if (!sp.dbg && !sp.ptable) run_hits_floor(sp.screen_z, sp.min_len, sp.run_floor);
+    if (!sp.dbg && !sp.ptable) sp.word_floor = run_hits_floor(sp.screen_z, sp.min_len, sp.run_floor);
     XC_CHECK(launch_scan(bk.log2L, sp, bk.count, s));
   }
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[2], s, evflags));

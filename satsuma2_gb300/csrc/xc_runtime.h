@@ -161,7 +161,7 @@ int batch_rerun_overflow(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_
 int batch_launch_count(const Ctx* c, const Batch* b);
 // z-score threshold of the scan kernel's FP32 probability screen.
 float screen_z(double min_prob, double target_total);
-void run_hits_floor(float screen_z, int min_len, uint32_t out[8]);
+int run_hits_floor(float screen_z, int min_len, uint32_t out[8]);
 int ctx_align_pipelined(Ctx* c, const xc_pair* pairs, size_t n, xc_result* out, size_t cap, size_t* n_out,
                         size_t* pair_counts);
 void server_stop(Ctx* c);

@@ -151,8 +151,8 @@ __device__ __forceinline__ uint32_t nib_popc(uint32_t x) {
 // blocks 2j+1 in another, each count biased by 128 - MIN_HITS so that bit 7
 // of its byte is the test.  Every byte stays within 0..255 (counts <= 49,
 // nibble differences biased by 4, prefix sums <= 48).  Returns the test bits
-// (nonzero: the word is marked).
-__device__ __forceinline__ uint32_t screen_word(uint32_t e2, uint32_t e1, uint32_t e0) {
+// (nonzero: some block passes) and in edge those of blocks 0 and 7.
+__device__ __forceinline__ uint32_t screen_word(uint32_t e2, uint32_t e1, uint32_t e0, uint32_t& edge) {
   const uint32_t pl = nib_popc(__funnelshift_r(e2, e1, 19));   // nibble k: bits 19+4k.. leaving
   const uint32_t pe = nib_popc(e0 >> 4);                        // nibble k: bits 68+4k.. entering
   const uint32_t de = (pe & 0x0f0f0f0fu) + 0x04040404u - (pl & 0x0f0f0f0fu);                 // 4 + d(2j)
@@ -161,7 +161,25 @@ __device__ __forceinline__ uint32_t screen_word(uint32_t e2, uint32_t e1, uint32
   const uint32_t c0 = __popc(e2 >> 19) + __popc(e1) + __popc(e0 & 15u);
   const uint32_t x = sx + (c0 + (128 - MIN_HITS)) * 0x01010101u - 0x18100800u;   // 128 - 19 + c(2j)
   const uint32_t x2 = x + de - 0x04040404u;                                        // 128 - 19 + c(2j+1)
+  edge = (x & 0x80u) | (x2 & 0x80000000u);
   return (x | x2) & 0x80808080u;
+}
+
+// Pass-1 mark of one word: screen_word's test, except that a word whose
+// blocks 0 and 7 fail it and whose positions under checks 4..27 (the 69
+// positions of bits 23..91 of e2:e1:e0) hold fewer than word_floor equal
+// bases stays unmarked.  A passing check passes its block's test, so no run
+// of passing checks crosses such a word's edges; every run inside it makes
+// a segment within those 69 positions, and word_floor is the least run
+// floor (run_hits_floor), so none of its segments could pass the
+// probability screen.  Marked words still hold every check of every run
+// that crosses a word edge, which the run tracking of phases AB and C
+// relies on.
+__device__ __forceinline__ uint32_t mark_word(uint32_t e2, uint32_t e1, uint32_t e0, int word_floor) {
+  uint32_t edge;
+  const uint32_t m = screen_word(e2, e1, e0, edge);
+  const int h69 = __popc(e2 >> 23) + __popc(e1) + __popc(e0 & 0x0fffffffu);
+  return (edge || (m && h69 >= word_floor)) ? 1u : 0u;
 }
 
 // Exact window bits of one word: bit u set when check u's window holds
@@ -575,7 +593,7 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
             const uint2 nx = qp[q0 + q + 1], tw = tp[q0 + q];
             const uint32_t e0 = ~((tw.x ^ __funnelshift_r(a.x, nx.x, sh)) | (tw.y ^ __funnelshift_r(a.y, nx.y, sh)));
             a = nx;
-            acc = __funnelshift_r(acc, min(screen_word(e2, e1, e0), 1u), 1);   // in at bit 31
+            acc = __funnelshift_r(acc, mark_word(e2, e1, e0, P.word_floor), 1);   // in at bit 31
             e2 = e1;
             e1 = e0;
           }

@@ -101,3 +101,57 @@ def test_floor_drops_no_record(O, min_prob, target_total, min_len):
 def test_floor_off_when_screen_keeps_all():
     assert floors(float("inf"), 0) == [0] * 32
     assert floors(0.5, 0) == [0] * 32
+
+
+def _words_model(eq, w, F):
+    """(screened, marked) of word w of a diagonal, positions out of range
+    counted unequal: screened when some 4-check block's 49-position span holds
+    >= 19 equal bases; marked when, besides, block 0 or block 7 passes or the
+    69 positions under checks 4..27 hold >= F equal bases."""
+    def cnt(lo, hi):   # equal bases at positions lo..hi
+        lo, hi = max(lo, 0), min(hi, len(eq) - 1)
+        return int(eq[lo:hi + 1].sum()) if hi >= lo else 0
+    c = 32 * w
+    blocks = [cnt(c + 4 * b - 45, c + 4 * b + 3) >= 19 for b in range(8)]
+    screened = any(blocks)
+    edge = blocks[0] or blocks[7]
+    return screened, screened and (edge or cnt(c - 41, c + 27) >= F)
+
+
+@pytest.mark.parametrize("min_prob,target_total", [(0.99, 4096.0 ** 2), (0.99999, 2.0e7)])
+def test_word_floor_keeps_record_words(O, min_prob, target_total):
+    """Pass 1 leaves a screened word unmarked when its edge blocks fail and
+    the positions under its inner checks hold fewer equal bases than the least
+    run floor: every word holding a check of a segment that makes a record
+    stays marked, and a good share of the screened words go."""
+    fl = floors(screen_z(min_prob, target_total), 0)
+    F = min(fl)
+    items = W.uniform_batch(4, seed=29)
+    P = O.params(target_total=target_total, min_prob=min_prob)
+    n_screened = n_marked = n_rec = 0
+    for t, q in items:
+        _, det = O.align_pair(P, O.pair(t, q), want_detail=True)
+        ta = np.frombuffer(t, np.uint8)
+        for s, qq in enumerate((q, O.rc(q))):
+            qa = np.frombuffer(qq, np.uint8)
+            for off in det["offsets"][s][::4]:
+                pos = int(off) - 4096
+                eq = np.zeros(len(ta), bool)
+                lo, hi = max(0, -pos), min(len(ta), len(qa) - pos)
+                if hi > lo:
+                    eq[lo:hi] = ta[lo:hi] == qa[lo + pos:hi + pos]
+                marks = {}
+                for w in range(len(ta) // 32 + 1):
+                    sc, mk = _words_model(eq, w, F)
+                    n_screened += sc
+                    n_marked += mk
+                    marks[w] = mk
+                for s0, _, ln in O.doone(t, qq, pos):
+                    p, _ = O.match_prob(t, qq, s0, s0 + pos, ln, target_total)
+                    if p < min_prob:
+                        continue
+                    n_rec += 1
+                    for w in range((s0 + 45) >> 5, ((s0 + ln - 1) >> 5) + 1):
+                        assert marks[w], (pos, s0, ln, w)
+    assert n_rec > 0
+    assert n_marked < 0.8 * n_screened, (n_marked, n_screened)
