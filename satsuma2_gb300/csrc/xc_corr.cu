@@ -9,7 +9,11 @@
 //   spec_kernel<13> + corr_spec_kernel<13>  batches whose pairs share chunks:
 //                          each distinct chunk transformed once, each pair
 //                          correlated from the stored spectra.
-// Pairs outside the premise go on a hand-back list to
+// A/C/G/T pairs outside the premise (a query of >= 1024 bases whose length is
+// not a multiple of the entropy window) go on a second hand-back list to
+//   corr_rcq_kernel<13>    persistent, both strands per CTA, the reverse
+//                          complement's spectra computed;
+// the other pairs outside it go on a hand-back list to
 // corr_kernel<log2 L, NT>: one CTA per (chunk pair, strand), which also runs
 // every other FFT length.  Its steps:
 //   1. chunk bytes to shared memory; strand 1 reverse-complements the query
@@ -1418,8 +1422,8 @@ size_t spec_bytes_per_chunk() { return (size_t)4 * 4096 * sizeof(float2); }
 // query's even-bin signal and group 1 its odd-bin signal, and the reverse
 // sum takes the same formula.  12 forward and 2 inverse half-length
 // transforms per pair, where two corr_kernel CTAs take 16 and 2.  The pairs
-// come from corr_pair2_kernel's second hand-back list, already checked to be
-// A/C/G/T; CTAs stride over it.
+// come from the second hand-back list of corr_pair2_kernel or
+// corr_spec_kernel, already checked to be A/C/G/T; CTAs stride over it.
 // ---------------------------------------------------------------------------
 size_t corr_rcq_smem_bytes() {
   return corr_pair2_smem_bytes() + 256 * sizeof(float)   // reverse-complement window weights
