@@ -1282,11 +1282,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
     //      positions g + 256 r, one word per thread ----
     if (tid < 8) {
       const int len = (tid >> 2) ? Q : T;
-      const double off = len > 0 ? __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len) : 0.0;
-      s_wmo[0][tid] = __dsub_rn(0.0, off);
-      s_wmo[1][tid] = __dsub_rn(1.0, off);
-      s_wf[0][tid] = split3(s_wmo[0][tid]);
-      s_wf[1][tid] = split3(s_wmo[1][tid]);
+      mean_terms(s_cnt4[tid], len, s_wmo[0][tid], s_wmo[1][tid], s_wf[0][tid], s_wf[1][tid]);
     }
     {
       const uint32_t* cs = cwin + G * NWIN + (g >> 4);
@@ -1588,11 +1584,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams 
     //      (its counts are the forward counts of the complement bases) ----
     if (tid < 8) {
       const int len = (tid >> 2) ? Q : T;
-      const double off = len > 0 ? __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len) : 0.0;
-      s_wmo[0][tid] = __dsub_rn(0.0, off);
-      s_wmo[1][tid] = __dsub_rn(1.0, off);
-      s_wf[0][tid] = split3(s_wmo[0][tid]);
-      s_wf[1][tid] = split3(s_wmo[1][tid]);
+      mean_terms(s_cnt4[tid], len, s_wmo[0][tid], s_wmo[1][tid], s_wf[0][tid], s_wf[1][tid]);
     }
     {
       const uint32_t* cs = cwin + G * NWIN + (g >> 4);
@@ -1870,11 +1862,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
       continue;
     }
     if (tid < 4) {
-      const double off = len > 0 ? __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len) : 0.0;
-      s_wmo[0][tid] = __dsub_rn(0.0, off);
-      s_wmo[1][tid] = __dsub_rn(1.0, off);
-      s_wf[0][tid] = split3(s_wmo[0][tid]);
-      s_wf[1][tid] = split3(s_wmo[1][tid]);
+      mean_terms(s_cnt4[tid], len, s_wmo[0][tid], s_wmo[1][tid], s_wf[0][tid], s_wf[1][tid]);
     }
     if (tid >= 256) {   // the codes of positions g + 256 r, one word per g
       const int g = tid - 256;

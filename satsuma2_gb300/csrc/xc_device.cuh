@@ -413,6 +413,30 @@ __device__ __forceinline__ Split3 split3(double W) {
   return s;
 }
 
+// A channel's mean terms 0 - mean and 1 - mean, mean = count / len as the
+// reference forms it in double (CrossCorr.cc:109-123), with cnt4 = 4 count,
+// in double and split into three floats.  When len is a power of two and
+// count a whole number (a full 4096-base A/C/G/T chunk), count / len and
+// (len - count) / len are exact in FP32, so FP32 arithmetic gives the same
+// bits as the FP64 division and subtraction, and the split is (value, 0, 0).
+__device__ __forceinline__ void mean_terms(int cnt4, int len, double& w0, double& w1, Split3& f0, Split3& f1) {
+  if (len > 0 && (len & (len - 1)) == 0 && (cnt4 & 3) == 0 && len <= (1 << 24)) {
+    const float inv = __int_as_float((127 - (__ffs(len) - 1)) << 23);   // 2^-k, len = 2^k
+    const float m = (float)(cnt4 >> 2) * inv;
+    const float a = 0.f - m, b = (float)(len - (cnt4 >> 2)) * inv;
+    w0 = (double)a;
+    w1 = (double)b;
+    f0 = Split3{a, 0.f, 0.f};
+    f1 = Split3{b, 0.f, 0.f};
+    return;
+  }
+  const double off = len > 0 ? __ddiv_rn((double)cnt4 * 0.25, (double)len) : 0.0;
+  w0 = __dsub_rn(0.0, off);
+  w1 = __dsub_rn(1.0, off);
+  f0 = split3(w0);
+  f1 = split3(w1);
+}
+
 // __double2float_rn(__dmul_rn((double)E, W)) without FP64 in the common
 // case, for finite E and W with |E*W| >= 2^-100 or zero.  E*W = E*h + E*l +
 // E*r is formed as p1 + t to within 2^-45 |E*W| from FMA-exact products; the

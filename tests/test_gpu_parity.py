@@ -529,8 +529,9 @@ def test_ragged_query_kernel_vs_oracle(O, monkeypatch):
     on to corr_rcq_kernel, one more launch.  Their offsets agree with the
     oracle's FP64 correlation and with the per-strand kernel's except inside
     the straddle band, and every pair's records equal the oracle's over the
-    batch's own offsets.  Aligned pairs (a 4096-base and a 1008-base query)
-    share the launch."""
+    batch's own offsets.  Aligned pairs (a 4096-base and a 1008-base query),
+    short targets (all window weights 1) and a ragged query holding an N
+    (the per-strand kernel's) share the launch."""
     import satsuma2_gb300 as sg
     rng = np.random.default_rng(61)
     qlens = [1025, 1031, 1039, 1503, 2047, 2049, 3001, 3333, 4081, 4089, 4095, 4096, 1008]
@@ -542,6 +543,12 @@ def test_ragged_query_kernel_vs_oracle(O, monkeypatch):
         q = np.concatenate([seg, W.random_bases(rng, ql - len(seg))])
         q = W.revcomp(q) if k % 2 else q
         items.append((t.tobytes(), q.tobytes()))
+    for tl, ql in ((700, 2047), (1023, 3001)):
+        t = W.random_bases(rng, tl)
+        q = np.concatenate([W.mutate(rng, t, 0.9, indel_every=0), W.random_bases(rng, ql - tl)])
+        items.append((t.tobytes(), q.tobytes()))
+    t, q = items[5]
+    items.append((t, q[:1000] + b"N" + q[1001:]))
     TT = 4096.0 * len(items)
     x2 = sg.XCorr(target_total=TT)
     monkeypatch.setenv("SATSUMA2_GB300_PAIR_KERNEL", "0")
@@ -573,6 +580,7 @@ def test_ragged_query_kernel_vs_oracle(O, monkeypatch):
     b.free()
     x1.close()
     x2.close()
+    assert [len(q) % 16 != 0 for _, q in items[-3:]] == [True, True, True]
 
 
 def test_strand_kernel_switch_vs_oracle(O, monkeypatch):

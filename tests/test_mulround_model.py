@@ -101,3 +101,18 @@ def test_products_next_to_rounding_boundaries():
         assert got == f32(f64(E * W)), (E, W)
         fallbacks += fb
     assert fallbacks == 3000   # every one of them within the band takes FP64
+
+
+def test_mean_terms_power_of_two_lengths():
+    """mean_terms (xc_device.cuh): for a power-of-two length and a whole
+    count, FP32 gives count / len and (len - count) / len with the bits of
+    the FP64 division and subtractions, and split3 of those is (value, 0, 0)."""
+    for k in range(0, 15):
+        ln = 1 << k
+        for count in sorted({0, 1, ln // 3, ln // 2, ln - 1, ln} | set(range(0, ln + 1, max(1, ln // 64)))):
+            mean = f64(Fr(4 * count, 4) / ln)              # __ddiv_rn((double)cnt4 * 0.25, len)
+            for base, fast in ((0, f32(Fr(0) - f32(Fr(count, ln)))), (1, f32(Fr(ln - count, ln)))):
+                W = f64(base - mean)                          # __dsub_rn(base, mean)
+                assert fast == W                              # FP32 result, exact
+                h = f32(W)
+                assert h == W and f64(W - h) == 0            # split3: (h, 0, 0)
