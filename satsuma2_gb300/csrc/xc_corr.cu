@@ -465,22 +465,23 @@ __device__ __forceinline__ void corr_strand(const CorrParams& P, int pidx, int s
     const int which = tid >> 2, c = tid & 3;
     const int len = which ? Q : T;
     const int third = which ? th_q : th_t;
-    double off = 0.0;
-    if (len > 0) {
-      if (!third) {
-        off = __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len);
-      } else {
+    if (!third) {
+      mean_terms(s_cnt4[tid], len, s_wmo[0][tid], s_wmo[1][tid], s_wf[0][tid], s_wf[1][tid]);
+      s_off[tid] = __dsub_rn(0.0, s_wmo[0][tid]);   // the mean itself, exact
+    } else {
+      double off = 0.0;
+      if (len > 0) {
         const uint8_t* s = which ? sq : st;
         double sum = 0.0;
         for (int i = 0; i < len; i++) sum = __dadd_rn(sum, c_wd[c][s[i]]);
         off = __ddiv_rn(sum, (double)len);
       }
+      s_off[tid] = off;
+      s_wmo[0][tid] = __dsub_rn(0.0, off);
+      s_wmo[1][tid] = __dsub_rn(1.0, off);
+      s_wf[0][tid] = split3(s_wmo[0][tid]);
+      s_wf[1][tid] = split3(s_wmo[1][tid]);
     }
-    s_off[tid] = off;
-    s_wmo[0][tid] = __dsub_rn(0.0, off);
-    s_wmo[1][tid] = __dsub_rn(1.0, off);
-    s_wf[0][tid] = split3(s_wmo[0][tid]);
-    s_wf[1][tid] = split3(s_wmo[1][tid]);
   }
   __syncthreads();
 
@@ -839,11 +840,7 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
   __syncthreads();
   if (tid < 8) {
     const int len = (tid >> 2) ? Q : T;
-    const double off = len > 0 ? __ddiv_rn((double)s_cnt4[tid] * 0.25, (double)len) : 0.0;
-    s_wmo[0][tid] = __dsub_rn(0.0, off);
-    s_wmo[1][tid] = __dsub_rn(1.0, off);
-    s_wf[0][tid] = split3(s_wmo[0][tid]);
-    s_wf[1][tid] = split3(s_wmo[1][tid]);
+    mean_terms(s_cnt4[tid], len, s_wmo[0][tid], s_wmo[1][tid], s_wf[0][tid], s_wf[1][tid]);
   }
   __syncthreads();
 
