@@ -460,6 +460,7 @@ def test_edge_chunks_match_oracle(O):
         (b"", full), (full, b""), (b"", b""),
         (full[:5], full[:7]), (full[:45], full[:46]), (full[:47], full[:47]),
         (full[:1023], full[:1025]), (full[:1024], full[:3001]), (full[3:3004], full[:4096]),
+        (b"", full[:2001]), (full[:2001], b""),
         (b"N" * 4096, full), (full[:2000] + b"RYKMSWBDHVN" * 50 + full[2550:4096], full),
     ]
     TT = 4096.0 * 16
