@@ -720,11 +720,11 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
             items[i] = it | (pb ? IT_PREV : 0u);
             runs_of(it, g, pb, fall, close);
             // A run that starts and ends inside this word (checks a..b, r of
-            // them) makes the segment [a-45, b+1) of length r + 45, whose
-            // equal bases are at most window(b)'s count plus the r - 1
-            // positions before that window.  Below the floor for r no G+C
-            // composition lets it pass the probability screen, so the
-            // segment is dropped here instead of queued.
+            // them) makes the segment [a-45, b+1) of length r + 45, positions
+            // that bits a+19..b+64 of e2:e1:e0 cover, so its equal-base count
+            // is one popcount here.  Below the floor for r no G+C composition
+            // lets it pass the probability screen, so the segment is dropped
+            // here instead of queued.
             if (fall | close) {
               const uint32_t rise = g & ~((g << 1) | pb);   // first checks of runs
               const uint64_t U = ((uint64_t)e1 << 32) | e2;
@@ -732,9 +732,9 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
               auto hopeless = [&](int b) -> bool {
                 const uint32_t rs = rise & (0xffffffffu >> (31 - b));
                 if (!rs) return false;   // the run began in an earlier word
-                const int r = b - (31 - __clz((int)rs)) + 1;
-                const int wb = __popcll(U >> (b + 19)) + __popc(e0 & (0xffffffffu >> (31 - b)));
-                return wb + r - 1 < (int)fl[r - 1];
+                const int a = 31 - __clz((int)rs);
+                const int h = __popcll(U >> (a + 19)) + __popc(e0 & (0xffffffffu >> (31 - b)));
+                return h < (int)fl[b - a];
               };
               uint32_t f = fall & ~1u;   // bit 0: the run ended in the word before
               while (f) {

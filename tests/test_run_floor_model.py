@@ -1,11 +1,14 @@
-"""CPU model of the scan kernel's floor on in-word runs (xc_scan.cu phase AB,
-run_hits_floor in xc_runtime.cu): a run of r passing checks inside one
-32-check word makes a segment of r + 45 bases whose equal-base count is at
-most window(b)'s count plus r - 1; below the floor for r no G+C composition
-lets the segment pass the probability screen.  Restated here in double and
-checked against the oracle: every segment the floor drops has a match
-probability below min_prob (so it never makes a record), for the screen
-settings of the uniform, genome and strict workloads and with a min_len."""
+"""CPU model of the scan kernel's floors (xc_scan.cu, run_hits_floor in
+xc_runtime.cu).  Phase AB: a run of r passing checks inside one 32-check
+word makes a segment of r + 45 bases whose equal-base count the kernel takes
+from the word's equality bits; below the floor for r no G+C composition lets
+the segment pass the probability screen.  Pass 1: a screened word whose edge
+blocks fail and whose inner positions hold fewer equal bases than the least
+floor stays unmarked.  Restated here in double and checked against the
+oracle: every segment the floor drops has a match probability below
+min_prob (so it never makes a record), and every word of a record-making
+segment stays marked, for the screen settings of the uniform, genome and
+strict workloads and with a min_len."""
 import math
 
 import numpy as np
@@ -57,9 +60,7 @@ def _dropped(O, t, q, pos, fl):
             continue                          # not inside one word: kept
         r = b - a + 1
         eq = ta[s0:s0 + ln] == qa[s0 + pos:s0 + pos + ln]
-        wb = int(eq[ln - 46:].sum())
-        assert int(eq.sum()) <= wb + r - 1    # the bound itself
-        if wb + r - 1 < fl[r - 1]:
+        if int(eq.sum()) < fl[r - 1]:
             out.append((s0, ln))
     return out
 
@@ -95,7 +96,7 @@ def test_floor_drops_no_record(O, min_prob, target_total, min_len):
                         continue
                     p, _ = O.match_prob(t, qq, s0, s0 + pos, ln, target_total)
                     assert p < min_prob, (s0, ln, p)
-    assert n_drop > n_seg // 2   # most segments are short noise runs
+    assert n_drop > (3 * n_seg) // 4   # most segments are short noise runs
 
 
 def test_floor_off_when_screen_keeps_all():
