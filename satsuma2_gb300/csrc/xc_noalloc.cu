@@ -50,7 +50,9 @@ constexpr size_t NA_BYTES = NA_DENSE + align256((size_t)2 * NA_SLOTS * sizeof(De
 // counter words inside NA_CNT
 constexpr int C_OFFCNT = 0;   // [2] FindTop offsets per strand
 constexpr int C_FLAGS = 2;    // [1] pair flags
+constexpr int C_FB2 = 3;      // [1] the pair index it may hand on to the ragged-query kernel
 constexpr int C_WORK = 6;     // [1] the both-strands kernel's work counter
+constexpr int C_FB2CNT = 7;   // [1] pairs handed on to the ragged-query kernel
 constexpr int C_RESCNT = 4;   // [2] kept matches per strand
 constexpr int C_MISC = 8;     // [4] overflow count, error bits, debug count, pairs handed back
 constexpr int C_BASE = 12;    // [3] dense result bases
@@ -155,10 +157,16 @@ int align_pair_noalloc(Ctx* c, const xc_pair& p, xc_result* out, size_t cap, siz
   cp.pair_flags = reinterpret_cast<uint32_t*>(cnt + C_FLAGS);
   if (lg == PAIR_LOG2L && c->pair_kernel) {
     // the same correlation kernels as xc_align_pairs: both strands in one
-    // CTA, or the per-strand kernel for a pair it hands back
+    // CTA, the ragged-query kernel for an A/C/G/T query of >= 1024 bases
+    // that is not a multiple of 16, or the per-strand kernel for a pair
+    // handed back
     cp.fb_list = cnt + C_FB;
     cp.fb_cnt = cnt + C_MISC + 3;
     cp.pair_form = c->pair_form;
+    if (c->pair_form == 2 && p.qlen >= 1024 && p.qlen % 16 != 0) {
+      cp.fb2_list = cnt + C_FB2;
+      cp.fb2_cnt = cnt + C_FB2CNT;
+    }
   }
   cp.work = cnt + C_WORK;
   cp.strand_threads = c->strand_threads[lg];

@@ -46,6 +46,8 @@ def pairs():
     g[100:140] = b"N" * 40                                          # byte-table path
     items.append((bytes(g), W.plain_pair(8)[1]))
     items.append((W.random_bases(rng, 1500).tobytes(), W.random_bases(rng, 900).tobytes()))  # short
+    # a 3001-base query (not a multiple of the 16-base window): the ragged-query kernel
+    items.append((t.tobytes(), W.mutate(rng, t[500:3501], 0.9, indel_every=0).tobytes()))
     return items
 
 
