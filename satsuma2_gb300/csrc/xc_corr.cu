@@ -1231,7 +1231,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
       } else if (nv > 0) {
         int a4 = 0, c4 = 0, g4 = 0, t4 = 0;
         for (int j = 0; j < nv; j++) {
-          const uchar4 q = c_w4q[sb[16 * g + j]];
+          const uchar4 q = c_w4q[sb[16 * g + j] & 127u];   // a byte >= 128 voids the pair
           a4 += q.x; c4 += q.y; g4 += q.z; t4 += q.w;
         }
         const double* et = P.tab.ent + nv * (4 * WIN + 1);
@@ -1542,7 +1542,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams 
         int a4 = 0, c4 = 0, g4 = 0, t4 = 0;
         for (int j = 0; j < n; j++) {
           const unsigned b = bytes[j];
-          const uchar4 q = c_w4q[rc ? c_rc[b] : b];
+          const uchar4 q = c_w4q[(rc ? c_rc[b] : b) & 127u];   // a byte >= 128 voids the pair
           a4 += q.x; c4 += q.y; g4 += q.z; t4 += q.w;
         }
         const double* et = P.tab.ent + n * (4 * WIN + 1);
@@ -1827,7 +1827,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
       } else if (nv > 0) {
         int a4 = 0, c4 = 0, g4 = 0, t4 = 0;
         for (int j = 0; j < nv; j++) {
-          const uchar4 q = c_w4q[sb[16 * g + j]];
+          const uchar4 q = c_w4q[sb[16 * g + j] & 127u];   // a byte >= 128 voids the pair
           a4 += q.x; c4 += q.y; g4 += q.z; t4 += q.w;
         }
         const double* et = S.tab.ent + nv * (4 * WIN + 1);
