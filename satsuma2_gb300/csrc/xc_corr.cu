@@ -2112,8 +2112,9 @@ cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t
   dim3 grid(npairs, 2);
   const int nt = strand_threads_ok(log2L, p.strand_threads) ? p.strand_threads : NT_CORR;
   if (p.fb_list) {
-    // both strands per CTA, then corr_kernel over the pairs handed back:
-    // one wave of CTAs striding over the list (*fb_cnt starts at zero)
+    // both strands per CTA, corr_rcq_kernel over the ragged query windows
+    // (fb2_list), then corr_kernel over the pairs handed back: one wave of
+    // CTAs striding over each list (the counts start at zero)
     if (log2L != PAIR_LOG2L) return cudaErrorInvalidValue;
     static const int sms = [] {
       int dev = 0, n = 152;

@@ -168,7 +168,8 @@ struct ScanParams {
 // Launchers (xc_corr.cu, xc_scan.cu).
 cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t s);
 // FFT 8192 with shared chunks: spec_kernel over the distinct chunks, then the
-// pair kernel from their spectra, then corr_kernel over the pairs handed back.
+// pair kernel from their spectra, corr_rcq_kernel over the ragged query
+// windows (fb2_list), then corr_kernel over the pairs handed back.
 cudaError_t launch_corr_spec(const SpecParams& sp, const CorrParams& p, int npairs, cudaStream_t s);
 size_t spec_bytes_per_chunk();
 // Thread counts per strand the per-strand correlation kernel is built for.

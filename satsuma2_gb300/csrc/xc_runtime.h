@@ -48,7 +48,8 @@ struct Batch {
   int* d_rescnt = nullptr;        size_t cap_rescnt = 0;
   DevResultX* d_ovf = nullptr;    size_t cap_ovf = 0;
   int* d_misc = nullptr;          size_t cap_misc = 0;   // [0] ovf count [1] err [2] dbg count
-                                                         // [3] pairs corr_pair_kernel handed back
+                                                         // [3] pairs the both-strands kernel handed back
+                                                         // [4] [5] work counters [6] ragged query windows
   int* d_fb = nullptr;            size_t cap_fb = 0;     // those pairs' indices
   int* d_fb2 = nullptr;           size_t cap_fb2 = 0;    // A/C/G/T pairs with a ragged query window it handed on
   int ragged = 0;                 // FFT-8192 pairs whose query is >= 1024 bases and not a multiple of 16
