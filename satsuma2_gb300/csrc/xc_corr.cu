@@ -9,8 +9,9 @@
 //   spec_kernel<13> + corr_spec_kernel<13>  batches whose pairs share chunks:
 //                          each distinct chunk transformed once, each pair
 //                          correlated from the stored spectra.
-// A/C/G/T pairs outside the premise (a query of >= 1024 bases whose length is
-// not a multiple of the entropy window) go on a second hand-back list to
+// Pairs whose query is >= 1024 bases and not a multiple of the entropy window
+// (outside the premise) are placed last in the bucket by the host, or go on
+// a second hand-back list, to
 //   corr_rcq_kernel<13>    persistent, both strands per CTA, the reverse
 //                          complement's spectra computed;
 // the other pairs outside it go on a hand-back list to
@@ -660,7 +661,13 @@ __global__ void __launch_bounds__(NT, corr_min_blocks(LOG2L, NT)) corr_kernel(co
   // back, CTA columns striding over the list.
   const int cnt = P.fb_list ? *P.fb_cnt : (int)blockIdx.x + 1;
   for (int j = blockIdx.x; j < cnt; j += gridDim.x) {
-    corr_strand<LOG2L, NT>(P, P.fb_list ? P.fb_list[j] : P.first + j, j, blockIdx.y, smem);
+    const int pidx = P.fb_list ? P.fb_list[j] : P.first + j;
+    if (P.fb_list && P.strad_cnt && threadIdx.x == 0) {
+      // a pair corr_rcq_kernel passed on after a void pass may hold its count
+      P.strad_cnt[pidx * 2 + blockIdx.y] = 0;
+    }
+    __syncthreads();
+    corr_strand<LOG2L, NT>(P, pidx, j, blockIdx.y, smem);
     __syncthreads();
   }
 }
@@ -1415,8 +1422,11 @@ size_t spec_bytes_per_chunk() { return (size_t)4 * 4096 * sizeof(float2); }
 // query's even-bin signal and group 1 its odd-bin signal, and the reverse
 // sum takes the same formula.  12 forward and 2 inverse half-length
 // transforms per pair, where two corr_kernel CTAs take 16 and 2.  The pairs
-// come from the second hand-back list of corr_pair2_kernel or
-// corr_spec_kernel, already checked to be A/C/G/T; CTAs stride over it.
+// are the FFT-8192 bucket's last ones, placed there by the host (its
+// ragged query windows), or the list corr_spec_kernel (or, without a
+// range, corr_pair2_kernel) hands on; CTAs stride over them.  A pair with a
+// byte >= 128 is voided after the pass and one with other letters is handed
+// on to the per-strand kernel.
 // ---------------------------------------------------------------------------
 size_t corr_rcq_smem_bytes() {
   return corr_pair2_smem_bytes() + 256 * sizeof(float)   // reverse-complement window weights
@@ -1484,6 +1494,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams 
   float4* vr = reinterpret_cast<float4*>(Er + NWIN);          // its window values
   uint32_t* cr = reinterpret_cast<uint32_t*>(vr + NWIN);      // its codes of positions g + 256 r
   __shared__ int s_cnt4[8];
+  __shared__ unsigned s_flags;     // bit 0: a byte >= 128; bit 1: a byte other than A, C, G, T
   __shared__ double s_wmo[2][8];   // 0 - mean and 1 - mean per (sequence, channel)
   __shared__ Split3 s_wf[2][8];    // the same as three floats each
   __shared__ int s_warp[2][2 * 256 / 32];
@@ -1492,7 +1503,9 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams 
   const int G = tid >> 8;
   const int g = tid & 255;
   const GroupBarrier gb{1 + G, 256};
-  const int count = *P.fb2_cnt;
+  // the list the spectra kernel filled, or the bucket's range of them
+  const int count = P.fb2_list ? *P.fb2_cnt : P.rcq_count;
+  auto pair_at = [&](int k) { return P.fb2_list ? P.fb2_list[k] : P.rcq_first + k; };
 
   for (int i = tid; i < NH; i += NT_PAIR2) {
     twNh[i] = P.tab.twN_hi[i];
@@ -1502,14 +1515,15 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams 
     twNl[tid] = P.tab.twN_lo[tid];
     twLl[tid] = P.tab.twL_lo[tid];
   }
-  if ((int)blockIdx.x < count) pair2_prefetch(P, P.fb2_list[blockIdx.x], st, sq, tid);
+  if ((int)blockIdx.x < count) pair2_prefetch(P, pair_at(blockIdx.x), st, sq, tid);
 
   for (int p = blockIdx.x; p < count; p += gridDim.x) {
-    const int pidx = P.fb2_list[p];
-    const int next = p + (int)gridDim.x < count ? P.fb2_list[p + gridDim.x] : -1;
+    const int pidx = pair_at(p);
+    const int next = p + (int)gridDim.x < count ? pair_at(p + gridDim.x) : -1;
     const int T = P.pairs[pidx].tlen, Q = P.pairs[pidx].qlen;
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     if (tid < 8) s_cnt4[tid] = 0;
+    if (tid == 0) s_flags = 0u;
     __syncthreads();   // the chunk bytes are in; the counters are zero
 
     // ---- 1. thread (G, g): bytes 16g..16g+15 of sequence G (entropy window
@@ -1524,6 +1538,22 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams 
       const uint8_t* sb = G ? sq : st;
       const uint4 v = *reinterpret_cast<const uint4*>(sb + 16 * g);
       const uint32_t x[4] = {v.x, v.y, v.z, v.w};
+      {
+        // byte checks, as corr_pair2_kernel's (a range of ragged query
+        // windows is not checked before)
+        auto nz = [](uint32_t y) { return (((y & 0x7f7f7f7fu) + 0x7f7f7f7fu) | y) & 0x80808080u; };
+        uint32_t high = 0u, bad = 0u;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const int vk = min(max(valid - 4 * k, 0), 4);
+          const uint32_t m = vk >= 4 ? 0xffffffffu : (1u << (8 * vk)) - 1u;
+          high |= x[k] & m & 0x80808080u;
+          bad |= nz(x[k] ^ 0x41414141u) & nz(x[k] ^ 0x43434343u) & nz(x[k] ^ 0x47474747u) &
+                 nz(x[k] ^ 0x54545454u) & m & 0x80808080u;   // bit 7: byte is not A, C, G or T
+        }
+        const unsigned fl = (high ? 1u : 0u) | (bad ? 2u : 0u);
+        if (fl) atomicOr(&s_flags, fl);
+      }
       uint32_t p0 = 0u, p1 = 0u, codes = 0u;
 #pragma unroll
       for (int k = 0; k < 4; k++) {
@@ -1715,6 +1745,22 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams 
     find_top<LOG2L, 256, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, G, buf, g, s_warp[G], gb,
                                        1.0f / (float)(4 * N));
     __syncthreads();   // buffers and per-pair words are reused by the next pair
+    if (tid == 0 && s_flags) {
+      // bytes outside the premise (rare): the pass above is void.  A byte
+      // >= 128 voids the pair; other letters send it to the per-strand
+      // kernel, which redoes its offsets and near-threshold lags.
+      if (s_flags & 1u) {
+        P.off_cnt[pidx * 2] = 0;
+        P.off_cnt[pidx * 2 + 1] = 0;
+        P.pair_flags[pidx] = PF_INVALID;
+        if (P.strad_cnt) {
+          P.strad_cnt[pidx * 2] = 0;
+          P.strad_cnt[pidx * 2 + 1] = 0;
+        }
+      } else {
+        P.fb_list[atomicAdd(P.fb_cnt, 1)] = pidx;
+      }
+    }
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
@@ -2124,11 +2170,17 @@ cudaError_t launch_corr(int log2L, const CorrParams& p, int npairs, cudaStream_t
     CorrParams q = p;
     q.count = npairs;
     if (p.pair_form == 2) {   // persistent: one CTA per SM strides over the pairs
-      corr_pair2_kernel<PAIR_LOG2L><<<std::min(npairs, sms), NT_PAIR2, corr_pair2_smem_bytes(), s>>>(q);
-      if (p.fb2_list)   // the pairs with a ragged query window it handed on
-        corr_rcq_kernel<PAIR_LOG2L><<<std::min(npairs, sms), NT_PAIR2, corr_rcq_smem_bytes(), s>>>(q);
+      // (the bucket's ragged query windows, when given as a range, come last
+      // and go to corr_rcq_kernel alone)
+      q.count = npairs - (p.fb2_list ? 0 : p.rcq_count);
+      if (q.count > 0)
+        corr_pair2_kernel<PAIR_LOG2L><<<std::min(q.count, sms), NT_PAIR2, corr_pair2_smem_bytes(), s>>>(q);
+      if (p.fb2_list || p.rcq_count > 0)   // the pairs with a ragged query window
+        corr_rcq_kernel<PAIR_LOG2L><<<std::min(p.fb2_list ? npairs : p.rcq_count, sms), NT_PAIR2,
+                                      corr_rcq_smem_bytes(), s>>>(q);
     } else {
       q.fb2_list = nullptr;
+      q.rcq_count = 0;
       corr_pair_kernel<PAIR_LOG2L><<<npairs, NT_PAIR, corr_pair_smem_bytes(PAIR_LOG2L), s>>>(q);
     }
     grid.x = std::min(npairs, sms * (NT_CORR / nt));

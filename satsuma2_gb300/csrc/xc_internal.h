@@ -93,6 +93,8 @@ struct CorrParams {
   int* fb_cnt;              //   hands back ([*fb_cnt], zeroed before) go to corr_kernel
   int* fb2_list;            // optional: the A/C/G/T pairs with a ragged query window the
   int* fb2_cnt;             //   persistent kernel hands to corr_rcq_kernel ([*fb2_cnt], zeroed before)
+  int rcq_first, rcq_count; // without fb2_list: corr_rcq_kernel takes pairs rcq_first.. (+rcq_count),
+                            //   the bucket's ragged query windows, placed after the pair kernel's
   int* strad_cnt;           // optional: near-threshold lags per [pair*2 + strand] (zeroed before)
   int* strad_list;          //   and the first STRAD_CAP of them, [pair*2 + strand][STRAD_CAP]
   int count;                // pairs of this launch (set by launch_corr)

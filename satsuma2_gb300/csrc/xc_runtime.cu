@@ -393,16 +393,28 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
     b->log2L[i] = lg;
     counts[lg]++;
   }
-  // bucket order
+  // bucket order; in the FFT-8192 bucket the pairs whose query is >= 1024
+  // bases and not a multiple of the 16-base entropy window come last, a
+  // range corr_rcq_kernel takes without the both-strands kernel
+  auto ragged_q = [](const xc_pair& p) { return p.qlen >= 1024 && p.qlen % 16 != 0; };
+  int ragged = 0;
+  for (size_t i = 0; i < n; i++)
+    if (b->log2L[i] == PAIR_LOG2L && ragged_q(pairs[i])) ragged++;
+  b->ragged = ragged;
   b->buckets.clear();
   int start = 0;
   int fill[MAX_LOG2L + 1];
+  int fill_ragged = 0;
   for (int lg = MIN_LOG2L; lg <= MAX_LOG2L; lg++) {
     fill[lg] = start;
+    if (lg == PAIR_LOG2L) fill_ragged = start + counts[lg] - ragged;
     if (counts[lg]) b->buckets.push_back({lg, start, counts[lg]});
     start += counts[lg];
   }
-  for (size_t i = 0; i < n; i++) b->order[fill[b->log2L[i]]++] = (int)i;
+  for (size_t i = 0; i < n; i++) {
+    const int lg = b->log2L[i];
+    b->order[lg == PAIR_LOG2L && ragged_q(pairs[i]) ? fill_ragged++ : fill[lg]++] = (int)i;
+  }
   // pool and offset-list layout; a chunk that several pairs pass by the same
   // pointer and length (a block's target and query chunks) is stored once.
   // The distinct chunks of the FFT-8192 bucket are numbered as they appear
@@ -464,7 +476,6 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
     }
     return e.off;
   };
-  int ragged = 0;
   for (size_t d = 0; d < n; d++) {
     const xc_pair& p = pairs[b->order[d]];
     const int lg = b->log2L[b->order[d]];
@@ -486,9 +497,7 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
     D.off_base = (uint32_t)offl;
     D.pad = 0;
     offl += 2ull << lg;
-    if (lg == PAIR_LOG2L && p.qlen >= 1024 && p.qlen % 16 != 0) ragged++;
   }
-  b->ragged = ragged;
   if (pool >= (1ull << 32) || offl >= (1ull << 32)) return XC_ERR_ARG;
   const size_t nslots = 2 * n;
   const size_t slots = (size_t)b->slots;
@@ -647,8 +656,13 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
       cp.fb_cnt = b->d_misc + 3;   // zeroed above
       cp.pair_form = c->pair_form;
       if (c->pair_form == 2 && b->ragged) {
-        cp.fb2_list = b->d_fb2;
-        cp.fb2_cnt = b->d_misc + 6;   // zeroed above
+        if (b->spec) {   // the spectra kernel hands them on by their chunk flags
+          cp.fb2_list = b->d_fb2;
+          cp.fb2_cnt = b->d_misc + 6;   // zeroed above
+        } else if (!b->d_dbg_sig) {   // the bucket's last pairs (signal output: the per-strand kernel)
+          cp.rcq_first = bk.first + bk.count - b->ragged;
+          cp.rcq_count = b->ragged;
+        }
       }
     }
     cp.strand_threads = c->strand_threads[bk.log2L];
@@ -713,7 +727,11 @@ int batch_launch_count(const Ctx* c, const Batch* b) {
   for (const Bucket& bk : b->buckets)
     if (bk.log2L == PAIR_LOG2L && c->pair_kernel) {
       n += b->spec ? 2 : 1;   // (spectra,) pair kernel, hand-back
-      if (c->pair_form == 2 && b->ragged) n++;   // ragged query windows
+      if (c->pair_form == 2 && b->ragged) {
+        n++;   // ragged query windows
+        if (!b->spec && b->d_dbg_sig) n--;                         // ragged pairs handed back instead
+        else if (!b->spec && b->ragged == bk.count) n--;   // no pair for the both-strands kernel
+      }
     }
   return n;
 }

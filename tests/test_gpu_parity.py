@@ -151,6 +151,17 @@ def test_rejects_non_ascii():
     with pytest.raises(sg.XCError) as e:
         x.align([(bytes(t), b"ACGT" * 300)])
     assert e.value.code == -5
+    # a query of 1201 bases (not a multiple of the 16-base window) goes to the
+    # ragged-query kernel, which finds the byte itself; alone, and beside
+    # pairs that stay valid
+    q = bytearray(b"ACGT" * 300 + b"A")
+    q[1190] = 0xC3
+    ok = (b"ACGT" * 500, b"ACGT" * 300 + b"C")
+    for items in ([(b"ACGT" * 500, bytes(q))], [ok, (b"ACGT" * 500, bytes(q)), ok]):
+        with pytest.raises(sg.XCError) as e:
+            x.align(items)
+        assert e.value.code == -5
+    assert len(x.align([ok, ok])) >= 0
 
 
 def test_batch_equals_single_pairs(O):
