@@ -365,6 +365,9 @@ Batch::~Batch() {
   if (graph_exec_timed) cudaGraphExecDestroy(graph_exec_timed);
   for (auto& e : ev)
     if (e) cudaEventDestroy(e);
+  if (fork_ev) cudaEventDestroy(fork_ev);
+  if (join_ev) cudaEventDestroy(join_ev);
+  if (side) cudaStreamDestroy(side);
   cudaFree(d_pool); cudaFree(d_desc); cudaFree(d_off); cudaFree(d_offcnt); cudaFree(d_flags);
   cudaFree(d_res); cudaFree(d_rescnt); cudaFree(d_ovf); cudaFree(d_misc); cudaFree(d_base);
   cudaFree(d_dense); cudaFree(d_dbg); cudaFree(d_dbg_sig); cudaFree(d_dbg_xc); cudaFree(d_acc); cudaFree(d_fb); cudaFree(d_fb2);
@@ -414,6 +417,11 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   for (size_t i = 0; i < n; i++) {
     const int lg = b->log2L[i];
     b->order[lg == PAIR_LOG2L && ragged_q(pairs[i]) ? fill_ragged++ : fill[lg]++] = (int)i;
+  }
+  if (b->buckets.size() > 1 && !b->side) {   // made here, outside any stream capture
+    XC_CHECK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+    XC_CHECK(cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
+    XC_CHECK(cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming));
   }
   // pool and offset-list layout; a chunk that several pairs pass by the same
   // pointer and length (a block's target and query chunks) is stored once.
@@ -686,6 +694,17 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     XC_CHECK(launch_corr(bk.log2L, cp, bk.count, s));
   }
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[1], s, evflags));
+  // The buckets' scans are independent: the largest runs on s, the others
+  // beside it on the batch's side stream (a small bucket's launch leaves
+  // most SMs idle), joined before the finalize kernels.
+  const Bucket* big = nullptr;
+  for (const Bucket& bk : b->buckets)
+    if (!big || bk.count > big->count) big = &bk;
+  const bool fork = b->buckets.size() > 1 && b->side;
+  if (fork) {
+    XC_CHECK(cudaEventRecord(b->fork_ev, s));
+    XC_CHECK(cudaStreamWaitEvent(b->side, b->fork_ev, 0));
+  }
   for (const Bucket& bk : b->buckets) {
     ScanParams sp{};
     sp.pairs = b->d_desc;
@@ -714,7 +733,11 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     sp.dbg_cnt = b->d_misc + 2;
     sp.dbg_cap = b->dbg_cap;
     if (!sp.dbg && !sp.ptable) sp.word_floor = run_hits_floor(sp.screen_z, sp.min_len, sp.run_floor);
-    XC_CHECK(launch_scan(bk.log2L, sp, bk.count, s));
+    XC_CHECK(launch_scan(bk.log2L, sp, bk.count, fork && &bk != big ? b->side : s));
+  }
+  if (fork) {
+    XC_CHECK(cudaEventRecord(b->join_ev, b->side));
+    XC_CHECK(cudaStreamWaitEvent(s, b->join_ev, 0));
   }
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[2], s, evflags));
   XC_CHECK(launch_finalize(b->d_rescnt, b->d_res, b->slots, nslots, b->d_base, b->d_dense, nullptr, s));

@@ -90,6 +90,8 @@ struct Batch {
   cudaStream_t graph_stream = nullptr;
   // stage-timing variant: events between the correlation, scan and finalize launches
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t side = nullptr;     // several FFT buckets: their scans beside the largest one's
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   cudaGraphExec_t graph_exec_timed = nullptr;
   bool graph_timed_valid = false;
   cudaStream_t graph_timed_stream = nullptr;
