@@ -637,7 +637,7 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
   XC_CHECK(cudaMemsetAsync(b->d_misc, 0, 8 * sizeof(int), s));   // counters, error words, work counters
   XC_CHECK(cudaMemsetAsync(b->d_stradcnt, 0, nslots * sizeof(int), s));
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[0], s, evflags));
-  for (const Bucket& bk : b->buckets) {
+  auto corr_bucket = [&](const Bucket& bk, cudaStream_t st) -> int {
     const DevTables& t = c->tab[bk.log2L];
     CorrParams cp{};
     cp.pairs = b->d_desc;
@@ -688,24 +688,13 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
       cp.pair_chunk = b->d_pairchunk;
       cp.spec = b->d_spec;
       cp.chunk_flags = b->d_chunkflags;
-      XC_CHECK(launch_corr_spec(spp, cp, bk.count, s));
-      continue;
+      XC_CHECK(launch_corr_spec(spp, cp, bk.count, st));
+      return XC_OK;
     }
-    XC_CHECK(launch_corr(bk.log2L, cp, bk.count, s));
-  }
-  if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[1], s, evflags));
-  // The buckets' scans are independent: the largest runs on s, the others
-  // beside it on the batch's side stream (a small bucket's launch leaves
-  // most SMs idle), joined before the finalize kernels.
-  const Bucket* big = nullptr;
-  for (const Bucket& bk : b->buckets)
-    if (!big || bk.count > big->count) big = &bk;
-  const bool fork = b->buckets.size() > 1 && b->side;
-  if (fork) {
-    XC_CHECK(cudaEventRecord(b->fork_ev, s));
-    XC_CHECK(cudaStreamWaitEvent(b->side, b->fork_ev, 0));
-  }
-  for (const Bucket& bk : b->buckets) {
+    XC_CHECK(launch_corr(bk.log2L, cp, bk.count, st));
+    return XC_OK;
+  };
+  auto scan_bucket = [&](const Bucket& bk, cudaStream_t st) -> int {
     ScanParams sp{};
     sp.pairs = b->d_desc;
     sp.pool = b->d_pool;
@@ -733,11 +722,52 @@ static int batch_enqueue(Ctx* c, Batch* b, cudaStream_t s, bool timed) {
     sp.dbg_cnt = b->d_misc + 2;
     sp.dbg_cap = b->dbg_cap;
     if (!sp.dbg && !sp.ptable) sp.word_floor = run_hits_floor(sp.screen_z, sp.min_len, sp.run_floor);
-    XC_CHECK(launch_scan(bk.log2L, sp, bk.count, fork && &bk != big ? b->side : s));
-  }
-  if (fork) {
+    XC_CHECK(launch_scan(bk.log2L, sp, bk.count, st));
+    return XC_OK;
+  };
+  int r;
+  const bool multi = b->buckets.size() > 1 && b->side;
+  if (multi && !timed) {
+    // Buckets are independent: each runs its correlation and then its scan,
+    // the FFT-8192 bucket (or else the largest) on s and the others beside
+    // it on the batch's side stream (small launches leave most SMs idle),
+    // joined before the finalize kernels.
+    const Bucket* main_bk = nullptr;
+    for (const Bucket& bk : b->buckets)
+      if (bk.log2L == PAIR_LOG2L) main_bk = &bk;
+    if (!main_bk)
+      for (const Bucket& bk : b->buckets)
+        if (!main_bk || bk.count > main_bk->count) main_bk = &bk;
+    XC_CHECK(cudaEventRecord(b->fork_ev, s));
+    XC_CHECK(cudaStreamWaitEvent(b->side, b->fork_ev, 0));
+    for (const Bucket& bk : b->buckets) {
+      if (&bk == main_bk) continue;
+      if ((r = corr_bucket(bk, b->side)) != XC_OK) return r;
+      if ((r = scan_bucket(bk, b->side)) != XC_OK) return r;
+    }
+    if ((r = corr_bucket(*main_bk, s)) != XC_OK) return r;
+    if ((r = scan_bucket(*main_bk, s)) != XC_OK) return r;
     XC_CHECK(cudaEventRecord(b->join_ev, b->side));
     XC_CHECK(cudaStreamWaitEvent(s, b->join_ev, 0));
+  } else {
+    // timed: the stages one after another, so that the stage events bracket
+    // them; the buckets' scans still run beside one another
+    for (const Bucket& bk : b->buckets)
+      if ((r = corr_bucket(bk, s)) != XC_OK) return r;
+    if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[1], s, evflags));
+    const Bucket* big = nullptr;
+    for (const Bucket& bk : b->buckets)
+      if (!big || bk.count > big->count) big = &bk;
+    if (multi) {
+      XC_CHECK(cudaEventRecord(b->fork_ev, s));
+      XC_CHECK(cudaStreamWaitEvent(b->side, b->fork_ev, 0));
+    }
+    for (const Bucket& bk : b->buckets)
+      if ((r = scan_bucket(bk, multi && &bk != big ? b->side : s)) != XC_OK) return r;
+    if (multi) {
+      XC_CHECK(cudaEventRecord(b->join_ev, b->side));
+      XC_CHECK(cudaStreamWaitEvent(s, b->join_ev, 0));
+    }
   }
   if (timed) XC_CHECK(cudaEventRecordWithFlags(b->ev[2], s, evflags));
   XC_CHECK(launch_finalize(b->d_rescnt, b->d_res, b->slots, nslots, b->d_base, b->d_dense, nullptr, s));
