@@ -675,3 +675,60 @@ def test_scan_queue_overflow_vs_oracle(O):
     want, _ = O.align_pair(P, O.pair(t, q), offsets_in=d["offsets"])
     assert parity.same_results(res, want, target_total=TT)
     x.close()
+
+
+def test_randomized_batch_vs_oracle(O):
+    """A seeded mix in one batch: lengths spread over the FFT buckets (many
+    queries not a multiple of the 16-base window), homology on either
+    strand, N runs, IUPAC letters, tandem repeats and empty chunks; every
+    pair's records equal the oracle's over the GPU's own offsets, and the
+    same items one at a time give the same records."""
+    import satsuma2_gb300 as sg
+    rng = np.random.default_rng(2024)
+    items = []
+    for k in range(96):
+        tl = int(rng.integers(0, 4097)) if k % 11 else 0
+        ql = int(rng.integers(300, 4097)) if k % 13 else 0
+        t = W.random_bases(rng, tl, gc=float(rng.uniform(0.35, 0.6)))
+        if tl > 600 and ql > 600 and k % 4:
+            a = int(rng.integers(0, tl - 500))
+            n = min(ql, tl - a)
+            q = W.mutate(rng, t[a:a + n], float(rng.uniform(0.75, 0.95)), indel_every=400)[:ql]
+            q = np.concatenate([q, W.random_bases(rng, ql - len(q))]) if len(q) < ql else q
+            if k % 3 == 0:
+                q = W.revcomp(q)
+        else:
+            q = W.random_bases(rng, ql)
+        t, q = bytearray(t.tobytes()), bytearray(q.tobytes())
+        if k % 7 == 0 and len(q) > 300:
+            i = int(rng.integers(0, len(q) - 200))
+            q[i:i + 150] = b"N" * 150
+        if k % 9 == 0 and len(t) > 300:
+            i = int(rng.integers(0, len(t) - 100))
+            t[i:i + 40] = b"RYKMSWBDHV" * 4
+        if k % 5 == 0 and len(t) > 400 and len(q) > 400:
+            unit = bytes(b"ACGT"[j] for j in rng.integers(0, 4, int(rng.integers(2, 7))))
+            rep = (unit * 100)[:200]
+            i, j = int(rng.integers(0, len(t) - 200)), int(rng.integers(0, len(q) - 200))
+            t[i:i + 200] = rep
+            q[j:j + 200] = rep
+        items.append((bytes(t), bytes(q)))
+    assert sum(1 for _, q in items if len(q) >= 1024 and len(q) % 16) > 20
+    TT = float(sum(len(t) for t, _ in items)) + 1.0
+    x = sg.XCorr(fft_len=-1, target_total=TT)
+    res, counts = x.align(items, with_counts=True)
+    P = O.params(target_total=TT, fft_len=0)
+    o = 0
+    n_rec = 0
+    for k, (t, q) in enumerate(items):
+        got = res[o:o + int(counts[k])]
+        o += int(counts[k])
+        n_rec += len(got)
+        d = x.debug_pair(t=t, q=q, signals=False)
+        Pk = O.params(target_total=TT, fft_len=d["L"])
+        want, _ = O.align_pair(Pk, O.pair(t, q), offsets_in=d["offsets"])
+        assert parity.same_results(got, want, target_total=TT), k
+        if k % 8 == 0:
+            assert parity.same_results(x.align([(t, q)]), got, target_total=TT), k
+    assert n_rec > 50
+    x.close()
