@@ -431,8 +431,10 @@ def genome_serving(local, rates=(5000.0, 50000.0, 200000.0, 1000000.0, 2000000.0
     import satsuma2_gb300 as sg
     tb, qb, tc, qc, blocks = genome_workload(seed)
     x = sg.XCorr(target_total=float(len(tb)), max_batch=4096, device=local)
-    warm = sg.block_pairs(tb, tc, qb, qc, *blocks[0])
-    x.wait(x.submit(warm), timeout_ms=120000)
+    # warm with several blocks (their shapes differ: tails, spectra, yields)
+    warm = [x.submit(sg.block_pairs(tb, tc, qb, qc, *blocks[-1 - i])) for i in range(8)]
+    for tk in warm:
+        x.wait(tk, timeout_ms=120000)
     out = {"workload": "20 Mb target, 80%% identity query (%d bp) with inversions, duplications, insertions; "
                        "%d target x %d query chunks; requests = 24x24 grid blocks in grid-search order "
                        "(%d blocks, %d pairs), Poisson arrivals" % (len(qb), len(tc), len(qc), len(blocks),

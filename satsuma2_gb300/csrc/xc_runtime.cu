@@ -522,7 +522,7 @@ int batch_pack(Ctx* c, Batch* b, const xc_pair* pairs, size_t n, cudaStream_t st
   if ((r = dev_grow(b->d_ovf, b->cap_ovf, (size_t)b->ovf_cap)) != XC_OK) return r;
   if ((r = dev_grow(b->d_misc, b->cap_misc, 8)) != XC_OK) return r;
   if ((r = dev_grow(b->d_fb, b->cap_fb, n)) != XC_OK) return r;
-  if (ragged && (r = dev_grow(b->d_fb2, b->cap_fb2, (size_t)ragged)) != XC_OK) return r;
+  if ((r = dev_grow(b->d_fb2, b->cap_fb2, n)) != XC_OK) return r;   // sized for any later batch of n
   if ((r = dev_grow(b->d_stradcnt, b->cap_stradcnt, nslots)) != XC_OK) return r;
   if ((r = dev_grow(b->d_strad, b->cap_strad, nslots * STRAD_CAP)) != XC_OK) return r;
   if ((r = dev_grow(b->d_base, b->cap_base, nslots + 1)) != XC_OK) return r;
