@@ -985,31 +985,39 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
 // ---------------------------------------------------------------------------
 // corr_pair2_kernel<13>: the persistent both-strands form.  One CTA of 512
 // threads per SM strides over the FFT-8192 pairs of a launch; the next pair's
-// chunk bytes arrive by cp.async while the current one is transformed.  Each
-// thread carries two butterflies per pass (the even-bin and odd-bin
-// transforms of one packed signal) and generates their twiddles once.  The
+// chunk bytes arrive by cp.async while the current one is transformed.  The
 // same premise as corr_pair_kernel (reverse strand from the forward spectra),
 // with these changes to the work per pair:
+//  - the channels are transformed in the basis u = s_A - s_T,
+//    v = s_C - s_G, w = s_A + s_T = -(s_C + s_G): at an A/C/G/T position
+//    one channel holds entropy * (1 - mean) and the others
+//    entropy * (0 - mean), the means sum to one, so the four channels sum to
+//    zero and three signals carry them.  u + i v of each sequence takes two
+//    half-length transforms (its even-bin and odd-bin halves) and wt + i wq
+//    two, six in all where the four channels of two sequences take eight;
+//  - in stage 1 (u + i v) each thread carries two butterflies per pass (both
+//    halves of its group's transform) and generates their twiddles once; in
+//    stage 2 (wt + i wq) group 0 transforms the even-bin half and group 1 the
+//    odd-bin half, one butterfly per thread;
 //  - the transform input is built in registers inside the first pass: thread
 //    g of a group takes positions g + 256 r (r < 16) from one word of 2-bit
-//    codes and the windows' channel values, so no input buffer is written;
-//  - the per-bin step forms the sums without separating the channels:
-//    with A = Zt(m), B = Zt(N-m), C = Zq(m), D = Zq(N-m) (Zt, Zq the
-//    transforms of t_c0 + i t_c1 and q_c0 + i q_c1),
-//      2 sum_c conj(T_c) Q_c = conj(A) C + B conj(D)
-//      2i (T_c0 Q_c1 + T_c1 Q_c0) = A C - conj(B D),
-//    and the reverse strand's sum W_L^((Q-1)k) conj(R) becomes
-//    W_L^((Q-1)k) (i conj(2i R)) / 2, i conj(x + iy) = y + ix;
-//  - the factors of two are left in (exact powers of two) and removed by
-//    FindTop's scale 1/(4N).
-// Pairs outside the premise go on P.fb_list for corr_kernel, as there.
+//    codes and the windows' channel values (the reference's rounded values,
+//    combined by one FP32 add), so no input buffer is written;
+//  - the per-bin steps (pair_bin_uv, pair_bin_w) form 4 sum_c conj(T_c) Q_c
+//    and 4i sum_c T_c Q_comp(c) from the packed spectra without separating
+//    the signals; the reverse strand's sum W_L^((Q-1)k) conj(R) becomes
+//    W_L^((Q-1)k) (i conj(4i R)) / 4, i conj(x + iy) = y + ix, and the
+//    target-only bins N-1 and N (sum_c T_c, zero) are written as zero;
+//  - the factors are left in (exact powers of two) and removed by FindTop's
+//    scale 1/(8N).
+// Pairs outside the premise go elsewhere, as in corr_pair_kernel.
 // ---------------------------------------------------------------------------
 size_t corr_pair2_smem_bytes() {
   constexpr size_t N = 4096, NH = N / 64;
   return (6 * N + 16 + 2 * (NH + 64)) * sizeof(float2)   // 4 transforms, F and R sums, twiddles
          + 2 * N                                           // chunk bytes (target, query)
          + 2 * 256 * sizeof(float)                         // entropy weight per window
-         + 2 * 256 * sizeof(float4)                        // window values of a channel pair
+         + 2 * 256 * sizeof(float4)                        // window values of a channel pair (pair2: A, T)
          + 2 * 256 * sizeof(uint32_t);                     // 2-bit codes of positions g + 256 r
 }
 
@@ -1047,6 +1055,27 @@ __device__ __forceinline__ void pair_bin(float2 A, float2 B, float2 C, float2 D,
   const float2 ac = cmul(A, C), bd = cmul(B, D);
   r = make_float2(ac.x - bd.x, ac.y + bd.y);
 }
+// corr_pair2_kernel's per-bin steps in the basis u = s_A - s_T,
+// v = s_C - s_G, w = s_A + s_T.  Stage 1, from the spectra A = Zt(m),
+// B = Zt(N-m), C = Zq(m), D = Zq(N-m) of u + i v:
+//   f = conj(A) C + B conj(D) = 2 (conj(Ut) Uq + conj(Vt) Vq)
+//   r = -i (A conj(D) + conj(B) C) = -2i (Ut Uq + Vt Vq).
+// Stage 2, from E = Y(m), H = Y(N-m) of wt + i wq
+// (Wt = (E + conj H) / 2, Wq = (E - conj H) / 2i):
+//   f = 2 Im(H E) - i (|E|^2 - |H|^2) = 4 conj(Wt) Wq
+//   r = E^2 - conj(H)^2 = 4i Wt Wq.
+// Summed: 4 sum_c conj(T_c) Q_c and 4i sum_c T_c Q_comp(c).
+__device__ __forceinline__ void pair_bin_uv(float2 A, float2 B, float2 C, float2 D, float2& f, float2& r) {
+  f = cadd(cmulc(C, A), cmulc(B, D));
+  const float2 s = cadd(cmulc(A, D), cmulc(C, B));
+  r = make_float2(s.y, -s.x);
+}
+__device__ __forceinline__ void pair_bin_w(float2 E, float2 H, float2& f, float2& r) {
+  const float he = H.x * E.y + H.y * E.x;
+  f = make_float2(he + he, (H.x * H.x + H.y * H.y) - (E.x * E.x + E.y * E.y));
+  const float exy = E.x * E.y, hxy = H.x * H.y;
+  r = make_float2((E.x * E.x - E.y * E.y) - (H.x * H.x - H.y * H.y), 2.f * (exy + hxy));
+}
 // Target-only bins, which the reference's loop leaves unmultiplied: Nyquist
 // (bin N: A = Zt(N/2) of the even-bin transform) 2 (T_c0 + T_c1), real; bin
 // N-1 (A = Zt(N/2-1), B = Zt(N/2) of the odd-bin transform)
@@ -1056,25 +1085,20 @@ __device__ __forceinline__ float2 pair_bin_nm1(float2 A, float2 B) {
   return make_float2((A.x + B.x) + (A.y + B.y), (A.y - B.y) - (A.x - B.x));
 }
 
-// First forward pass of one sequence's packed signal z = s_c0 + i s_c1 at
-// FFT 8192 (N = 4096), its input built in registers: thread g takes
-// x_E[r] = z[g + 256 r] and x_O[r] = z[g + 256 r] W_L^(g + 256 r),
-// W_L^(256 r) = exp(-i pi r / 16), from the word of 2-bit codes of those
-// positions and the windows' channel values vw[16 r] (window (g >> 4) + 16 r:
-// c0 at weight 0, 1, then c1), then the radix-16 butterflies of span N with
+// First forward pass of a packed signal z at FFT 8192 (N = 4096), its input
+// built in registers: thread g takes x_E[r] = z[g + 256 r] and
+// x_O[r] = z[g + 256 r] W_L^(g + 256 r), W_L^(256 r) = exp(-i pi r / 16),
+// with z[g + 256 r] = zf(r), then the radix-16 butterflies of span N with
 // their twiddles W_N^(g r), generated once for both transforms.
-__device__ __forceinline__ void first_pass_from_codes(uint32_t codes, int len, const float4* __restrict__ vw, int g,
-                                                      int c0, int c1, const float2* twLh, const float2* twLl,
-                                                      const float2* twNh, const float2* twNl,
-                                                      float2* __restrict__ bE, float2* __restrict__ bO) {
+template <class ZF>
+__device__ __forceinline__ void first_pass_x2(ZF zf, int g, const float2* twLh, const float2* twLl,
+                                              const float2* twNh, const float2* twNl, float2* __restrict__ bE,
+                                              float2* __restrict__ bO) {
   const float2 wg = tw2(twLh, twLl, g);
   float2 xe[16], xo[16];
 #pragma unroll
   for (int r = 0; r < 16; r++) {
-    const float4 v = vw[16 * r];
-    const uint32_t code = (codes >> (2 * r)) & 3u;
-    float2 z = make_float2(0.f, 0.f);
-    if (g + 256 * r < len) z = make_float2(code == (uint32_t)c0 ? v.y : v.x, code == (uint32_t)c1 ? v.w : v.z);
+    const float2 z = zf(r);
     xe[r] = z;
     xo[r] = cmul(cmul(z, wg), make_float2(cos_pi16(r), -sin_pi16(r)));
   }
@@ -1093,6 +1117,48 @@ __device__ __forceinline__ void first_pass_from_codes(uint32_t codes, int len, c
     bE[sb ^ swz(256 * r)] = xe[r];
     bO[sb ^ swz(256 * r)] = xo[r];
   }
+}
+
+// The same pass for one of the two transforms: the even-bin one (odd false)
+// or the odd-bin one, with the same arithmetic per transform.
+template <class ZF>
+__device__ __forceinline__ void first_pass_x1(ZF zf, bool odd, int g, const float2* twLh, const float2* twLl,
+                                              const float2* twNh, const float2* twNl, float2* __restrict__ buf) {
+  float2 x[16];
+  if (odd) {
+    const float2 wg = tw2(twLh, twLl, g);
+#pragma unroll
+    for (int r = 0; r < 16; r++) x[r] = cmul(cmul(zf(r), wg), make_float2(cos_pi16(r), -sin_pi16(r)));
+  } else {
+#pragma unroll
+    for (int r = 0; r < 16; r++) x[r] = zf(r);
+  }
+  DFT<16, -1>::run(x);
+  const Tw16 tw = tw16(twNh, twNl, g);
+#pragma unroll
+  for (int r = 1; r < 16; r++) x[r] = cmul(x[r], tw16_r(tw, r));
+  const int sb = swz(g);
+#pragma unroll
+  for (int r = 0; r < 16; r++) buf[sb ^ swz(256 * r)] = x[r];
+}
+
+// first_pass_x2 of one sequence's channel pair z = s_c0 + i s_c1: position
+// g + 256 r from the word of 2-bit codes of those positions and the windows'
+// channel values vw[16 r] (window (g >> 4) + 16 r: c0 at weight 0, 1, then
+// c1), zero past len.
+__device__ __forceinline__ void first_pass_from_codes(uint32_t codes, int len, const float4* __restrict__ vw, int g,
+                                                      int c0, int c1, const float2* twLh, const float2* twLl,
+                                                      const float2* twNh, const float2* twNl,
+                                                      float2* __restrict__ bE, float2* __restrict__ bO) {
+  first_pass_x2(
+      [&](int r) {
+        const float4 v = vw[16 * r];
+        const uint32_t code = (codes >> (2 * r)) & 3u;
+        float2 z = make_float2(0.f, 0.f);
+        if (g + 256 * r < len) z = make_float2(code == (uint32_t)c0 ? v.y : v.x, code == (uint32_t)c1 ? v.w : v.z);
+        return z;
+      },
+      g, twLh, twLl, twNh, twNl, bE, bO);
 }
 
 // Per-window channel values float(entropy * (weight - mean)) (CrossCorr.cc:123)
@@ -1145,9 +1211,9 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
   float2* ZO = ZE + N;                            // z * W_L^n, odd-bin transform
   float2* WE = ZO + N;                            // w = q_c0 + i q_c1
   float2* WO = WE + N;
-  float2* aFE = WO + N;                           // 2 x forward-strand sum, bins 2m, m <= N/2
+  float2* aFE = WO + N;                           // 4 x forward-strand sum, bins 2m, m <= N/2
   float2* aFO = aFE + (N / 2 + 8);                // bins 2m+1
-  float2* aRE = aFO + N / 2;                      // 2i x R, bins 2m (m < N/2)
+  float2* aRE = aFO + N / 2;                      // 4i x R, bins 2m (m < N/2)
   float2* aRO = aRE + (N / 2 + 8);                // bins 2m+1
   float2* twNh = aRO + N / 2;
   float2* twNl = twNh + NH;
@@ -1157,7 +1223,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
   uint8_t* sq = st + N;
   float* Et = reinterpret_cast<float*>(sq + N);
   float* Eq = Et + NWIN;
-  float4* vv = reinterpret_cast<float4*>(Eq + NWIN);   // [sequence][window]: c0 (w=0, w=1), c1 (w=0, w=1)
+  float4* vv = reinterpret_cast<float4*>(Eq + NWIN);   // [sequence][window]: w by base code
   uint32_t* cw = reinterpret_cast<uint32_t*>(vv + 2 * NWIN);   // [sequence][g]
   __shared__ int s_cnt4[8];
   __shared__ unsigned s_flags;     // bit 0: a byte >= 128; bit 1: a byte other than A, C, G, T
@@ -1298,75 +1364,140 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
     }
     __syncthreads();
 
-    // one stage per channel pair, (A, T) then (C, G); a loop the compiler
-    // keeps rolled, so nothing of one stage stays live into the other
-#pragma unroll 1
-    for (int stg = 0; stg < 2; stg++) {
-      const int c0 = stg ? 1 : 0, c1 = stg ? 2 : 3;
-      const bool first = stg == 0;
-      // ---- 3a. per-window channel values float(entropy * (weight - mean))
-      //      (CrossCorr.cc:123), weight 0 or 1; group G writes sequence G's ----
-      vv[G * NWIN + g] = window_values((G ? Eq : Et)[g], s_wf, s_wmo, G * 4 + c0, G * 4 + c1);
-      gb();
-      // ---- 3b. first forward pass with its input built in registers ----
-      first_pass_from_codes(cw[tid], G ? Q : T, vv + G * NWIN + (g >> 4), g, c0, c1, twLh, twLl, twNh, twNl,
-                            G ? WE : ZE, (G ? WE : ZE) + N);
-      gb();
-      // ---- 3c. the other two passes, both transforms of the group at once ----
-      {
-        float2* bE = G ? WE : ZE;
-        fft_pass16_x2<N, N / 16>(bE, bE + N, twNh, twNl, g);
-        gb();
-        fft_pass16_x2<N, N / 256>(bE, bE + N, twNh, twNl, g);
-      }
-      __syncthreads();   // the per-bin step reads both groups' spectra
-      // ---- 3d. per-bin step (CrossCorrelation::DoOne, CrossCorr.cc:477-492):
-      //      bin 0 is the product of real values (the general formula with
-      //      B = A, D = C); bins N-1 and N keep the targets' own values, which
-      //      the reference's loop leaves unmultiplied, for both strands.
-      //      Group 0: even bins, group 1: odd bins. ----
-      if (G == 0) {
-        const int la = lp<LOG2N>(g);
-        const int lb = lp<LOG2N>((256 - g) & 255);
-#pragma unroll
-        for (int it = 0; it <= N / 512; it++) {
-          const int m = g + 256 * it;
-          if (m > N / 2) break;
-          const int pa = la ^ lp<LOG2N>(256 * it);
-          // partner N-m = (N - 256(it+1)) | (256 - g) for g >= 1
-          const int pb = g ? (lb ^ lp<LOG2N>(N - 256 * (it + 1))) : lp<LOG2N>((N - 256 * it) & (N - 1));
-          const float2 A = ZE[pa], B = ZE[pb], C = WE[pa], D = WE[pb];
-          if (m == N / 2) {
-            const float2 f = pair_bin_nyquist(A);
-            aFE[m] = first ? f : cadd(aFE[m], f);
-          } else {
-            float2 f, r;
-            pair_bin(A, B, C, D, f, r);
-            aFE[m] = first ? f : cadd(aFE[m], f);
-            aRE[m] = first ? r : cadd(aRE[m], r);
-          }
-        }
-      } else {
-        const int la = lp<LOG2N>(g);
-#pragma unroll
-        for (int it = 0; it < N / 512; it++) {
-          const int m = g + 256 * it;
-          const int pa = la ^ lp<LOG2N>(256 * it);
-          const int pb = pa ^ lp<LOG2N>(N - 1);   // N-1-m = m ^ (N-1)
-          const float2 A = ZO[pa], B = ZO[pb], C = WO[pa], D = WO[pb];
-          if (m == N / 2 - 1) {
-            const float2 f = pair_bin_nm1(A, B);
-            aFO[m] = first ? f : cadd(aFO[m], f);
-          } else {
-            float2 f, r;
-            pair_bin(A, B, C, D, f, r);
-            aFO[m] = first ? f : cadd(aFO[m], f);
-            aRO[m] = first ? r : cadd(aRO[m], r);
-          }
-        }
-      }
-      __syncthreads();
+    // ---- 3. the channels in the basis u = s_A - s_T, v = s_C - s_G and
+    //      w = s_A + s_T = -(s_C + s_G) (an A/C/G/T position holds one base
+    //      and the channel means sum to one, so the four channels sum to
+    //      zero).  With U, V, W their spectra, per bin
+    //        sum_c conj(T_c) Q_c = conj(Wt) Wq + (conj(Ut) Uq + conj(Vt) Vq) / 2
+    //        sum_c T_c Q_comp(c) = Wt Wq - (Ut Uq + Vt Vq) / 2,
+    //      and the target-only bins N-1 and N (sum_c T_c) are zero.  Stage 1
+    //      transforms u + i v of sequence G in group G (both halves), stage 2
+    //      wt + i wq (group 0 the even-bin half, group 1 the odd-bin half):
+    //      six half-length forward transforms per pair. ----
+    // 3a. per-window signal values by base code, from the channel values
+    //     float(entropy * (weight - mean)) (CrossCorr.cc:123) at weight 0 or 1
+    //     with one FP32 add each: (u, v) into uvt (stage 1; the sums overwrite
+    //     it after stage 1's first pass), w into vv (stage 2)
+    float2* uvt = reinterpret_cast<float2*>(aFE);   // [sequence][window][code]
+    {
+      const float E = (G ? Eq : Et)[g];
+      const float4 at = window_values(E, s_wf, s_wmo, G * 4 + 0, G * 4 + 3);   // A at 0, 1; T at 0, 1
+      const float4 cg = window_values(E, s_wf, s_wmo, G * 4 + 1, G * 4 + 2);   // C at 0, 1; G at 0, 1
+      const float u0 = __fsub_rn(at.x, at.z), v0 = __fsub_rn(cg.x, cg.z), w0 = __fadd_rn(at.x, at.z);
+      float4* o = reinterpret_cast<float4*>(uvt + (G * NWIN + g) * 4);
+      o[0] = make_float4(__fsub_rn(at.y, at.z), v0, u0, __fsub_rn(cg.y, cg.z));   // A, C
+      o[1] = make_float4(u0, __fsub_rn(cg.x, cg.w), __fsub_rn(at.x, at.w), v0);   // G, T
+      vv[G * NWIN + g] = make_float4(__fadd_rn(at.y, at.z), w0, w0, __fadd_rn(at.x, at.w));
     }
+    gb();
+    // 3b. stage 1: first pass of u + i v with its input built in registers,
+    //     then the other two passes, both halves of the group's transform at once
+    {
+      const uint32_t codes = cw[tid];
+      const int len = G ? Q : T;
+      const float2* ub = uvt + (G * NWIN + (g >> 4)) * 4;
+      float2* bE = G ? WE : ZE;
+      first_pass_x2(
+          [&](int r) {
+            const float2 z = ub[64 * r + ((codes >> (2 * r)) & 3u)];
+            return g + 256 * r < len ? z : make_float2(0.f, 0.f);
+          },
+          g, twLh, twLl, twNh, twNl, bE, bE + N);
+      gb();
+      fft_pass16_x2<N, N / 16>(bE, bE + N, twNh, twNl, g);
+      gb();
+      fft_pass16_x2<N, N / 256>(bE, bE + N, twNh, twNl, g);
+    }
+    __syncthreads();   // the per-bin step reads both groups' spectra
+    // 3c. stage 1 per-bin step (CrossCorrelation::DoOne, CrossCorr.cc:477-492):
+    //     group 0 even bins, group 1 odd bins; bin 0 by the general formula
+    //     (B = A, D = C: products of real values)
+    if (G == 0) {
+      const int la = lp<LOG2N>(g);
+      const int lb = lp<LOG2N>((256 - g) & 255);
+#pragma unroll
+      for (int it = 0; it <= N / 512; it++) {
+        const int m = g + 256 * it;
+        if (m > N / 2) break;
+        const int pa = la ^ lp<LOG2N>(256 * it);
+        // partner N-m = (N - 256(it+1)) | (256 - g) for g >= 1
+        const int pb = g ? (lb ^ lp<LOG2N>(N - 256 * (it + 1))) : lp<LOG2N>((N - 256 * it) & (N - 1));
+        if (m == N / 2) {
+          aFE[m] = make_float2(0.f, 0.f);
+        } else {
+          float2 f, r;
+          pair_bin_uv(ZE[pa], ZE[pb], WE[pa], WE[pb], f, r);
+          aFE[m] = f;
+          aRE[m] = r;
+        }
+      }
+    } else {
+      const int la = lp<LOG2N>(g);
+#pragma unroll
+      for (int it = 0; it < N / 512; it++) {
+        const int m = g + 256 * it;
+        const int pa = la ^ lp<LOG2N>(256 * it);
+        const int pb = pa ^ lp<LOG2N>(N - 1);   // N-1-m = m ^ (N-1)
+        if (m == N / 2 - 1) {
+          aFO[m] = make_float2(0.f, 0.f);
+        } else {
+          float2 f, r;
+          pair_bin_uv(ZO[pa], ZO[pb], WO[pa], WO[pb], f, r);
+          aFO[m] = f;
+          aRO[m] = r;
+        }
+      }
+    }
+    gb();   // stage 2 overwrites the buffer the group's per-bin step read (group 0 ZE, group 1 WO)
+    // 3d. stage 2: wt + i wq, the even-bin half in group 0, the odd-bin half in group 1
+    float2* bw = G ? WO : ZE;
+    {
+      const uint32_t ct = cw[g], cq = cw[NWIN + g];
+      const float* wb = reinterpret_cast<const float*>(vv) + (g >> 4) * 4;
+      first_pass_x1(
+          [&](int r) {
+            const float wt = wb[64 * r + ((ct >> (2 * r)) & 3u)];
+            const float wq = wb[NWIN * 4 + 64 * r + ((cq >> (2 * r)) & 3u)];
+            return make_float2(g + 256 * r < T ? wt : 0.f, g + 256 * r < Q ? wq : 0.f);
+          },
+          G == 1, g, twLh, twLl, twNh, twNl, bw);
+      gb();
+      fft_pass<16, N, N / 16, false>(bw, twNh, twNl, g, 256);
+      gb();
+      fft_pass<16, N, N / 256, false>(bw, twNh, twNl, g, 256);
+    }
+    gb();
+    // 3e. stage 2 per-bin step, each group over its own half: E = Y(m), H = Y(N-m)
+    //     (partly unrolled: fully unrolled, its loads push the kernel past 128 registers)
+    if (G == 0) {
+      const int la = lp<LOG2N>(g);
+      const int lb = lp<LOG2N>((256 - g) & 255);
+#pragma unroll 3
+      for (int it = 0; it <= N / 512; it++) {
+        const int m = g + 256 * it;
+        if (m >= N / 2) break;
+        const int pa = la ^ lp<LOG2N>(256 * it);
+        const int pb = g ? (lb ^ lp<LOG2N>(N - 256 * (it + 1))) : lp<LOG2N>((N - 256 * it) & (N - 1));
+        float2 f, r;
+        pair_bin_w(ZE[pa], ZE[pb], f, r);
+        aFE[m] = cadd(aFE[m], f);
+        aRE[m] = cadd(aRE[m], r);
+      }
+    } else {
+      const int la = lp<LOG2N>(g);
+#pragma unroll 3
+      for (int it = 0; it < N / 512; it++) {
+        const int m = g + 256 * it;
+        if (m == N / 2 - 1) break;
+        const int pa = la ^ lp<LOG2N>(256 * it);
+        const int pb = pa ^ lp<LOG2N>(N - 1);
+        float2 f, r;
+        pair_bin_w(WO[pa], WO[pb], f, r);
+        aFO[m] = cadd(aFO[m], f);
+        aRO[m] = cadd(aRO[m], r);
+      }
+    }
+    __syncthreads();
 
     // ---- 4. inverses: group 0 the forward strand into ZE, group 1 the
     //      reverse strand S_r(k) = W_L^((Q-1)k) i conj(2i R(k)) into WE; the two
@@ -1386,7 +1517,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
 
     // ---- 5. FindTop, one strand per group ----
     find_top<LOG2L, 256, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, G, buf, g, s_warp[G], gb,
-                                       1.0f / (float)(4 * N));
+                                       1.0f / (float)(8 * N));
     if (tid == 0) s_take = take;
     __syncthreads();   // buffers and per-pair words are reused by the next pair
     p = np;
