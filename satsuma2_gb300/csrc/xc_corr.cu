@@ -1012,13 +1012,18 @@ __global__ void __launch_bounds__(NT_PAIR, 1) corr_pair_kernel(const CorrParams 
 //    scale 1/(8N).
 // Pairs outside the premise go elsewhere, as in corr_pair_kernel.
 // ---------------------------------------------------------------------------
-size_t corr_pair2_smem_bytes() {
+// The layout corr_pair2_kernel and corr_rcq_kernel share (the rcq kernel
+// adds its own arrays after it).
+static size_t pair_base_smem_bytes() {
   constexpr size_t N = 4096, NH = N / 64;
   return (6 * N + 16 + 2 * (NH + 64)) * sizeof(float2)   // 4 transforms, F and R sums, twiddles
          + 2 * N                                           // chunk bytes (target, query)
          + 2 * 256 * sizeof(float)                         // entropy weight per window
-         + 2 * 256 * sizeof(float4)                        // window values of a channel pair (pair2: A, T)
+         + 2 * 256 * sizeof(float4)                        // window values (pair2: w by base code)
          + 2 * 256 * sizeof(uint32_t);                     // 2-bit codes of positions g + 256 r
+}
+size_t corr_pair2_smem_bytes() {
+  return pair_base_smem_bytes() + 16 * TW16_ROW * sizeof(float2);   // twiddles of the span-256 passes
 }
 
 // Bins k and N-k (k <= N/2) of the reverse strand's packed sum in the
@@ -1219,7 +1224,8 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
   float2* twNl = twNh + NH;
   float2* twLh = twNl + 64;
   float2* twLl = twLh + NH;
-  uint8_t* st = reinterpret_cast<uint8_t*>(twLl + 64);
+  float2* tw16t = twLl + 64;   // twiddles of the span-256 passes (build_tw16_table)
+  uint8_t* st = reinterpret_cast<uint8_t*>(tw16t + 16 * TW16_ROW);
   uint8_t* sq = st + N;
   float* Et = reinterpret_cast<float*>(sq + N);
   float* Eq = Et + NWIN;
@@ -1246,6 +1252,8 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
     twLl[tid] = P.tab.twL_lo[tid];
   }
   if ((int)blockIdx.x < P.count) pair2_prefetch(P, P.first + blockIdx.x, st, sq, tid);
+  __syncthreads();
+  build_tw16_table(tw16t, twNh, twNl, N / 256, tid);   // read after the first barrier of the loop
   // Pairs in the order take_item gives, each taken one pair ahead (the next
   // pair's bytes are prefetched while this one is worked on; thread 0 uses a
   // counter result one pair after taking it).
@@ -1404,7 +1412,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
           },
           g, twLh, twLl, twNh, twNl, bE, bE + N);
       gb();
-      fft_pass16_x2<N, N / 16>(bE, bE + N, twNh, twNl, g);
+      fft_pass16_x2_tab<N, N / 16>(bE, bE + N, tw16t, g);
       gb();
       fft_pass16_x2<N, N / 256>(bE, bE + N, twNh, twNl, g);
     }
@@ -1462,7 +1470,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
           },
           G == 1, g, twLh, twLl, twNh, twNl, bw);
       gb();
-      fft_pass<16, N, N / 16, false>(bw, twNh, twNl, g, 256);
+      fft_pass16_tab<N, N / 16>(bw, tw16t, g);
       gb();
       fft_pass<16, N, N / 256, false>(bw, twNh, twNl, g, 256);
     }
@@ -1513,7 +1521,12 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
           twLh, twLl, g, 1.0f);
     }
     gb();
-    fft_inverse<LOG2N, Plan<LOG2N>, Plan<LOG2N>::n - 1, GroupBarrier>(buf, twNh, twNl, g, 256, gb);
+    fft_pass<16, N, 16, true>(buf, twNh, twNl, g, 256);
+    gb();
+    fft_pass16_inv_tab<N, 256>(buf, tw16t, g);
+    gb();
+    fft_pass<16, N, N, true>(buf, twNh, twNl, g, 256);
+    gb();
 
     // ---- 5. FindTop, one strand per group ----
     find_top<LOG2L, 256, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, G, buf, g, s_warp[G], gb,
@@ -1560,7 +1573,7 @@ size_t spec_bytes_per_chunk() { return (size_t)4 * 4096 * sizeof(float2); }
 // on to the per-strand kernel.
 // ---------------------------------------------------------------------------
 size_t corr_rcq_smem_bytes() {
-  return corr_pair2_smem_bytes() + 256 * sizeof(float)   // reverse-complement window weights
+  return pair_base_smem_bytes() + 256 * sizeof(float)   // reverse-complement window weights
          + 256 * sizeof(float4)                          // its window values
          + 256 * sizeof(uint32_t);                       // its codes of positions g + 256 r
 }

@@ -284,6 +284,25 @@ __device__ __forceinline__ void fft_pass16_x2_tab(float2* __restrict__ bufA, flo
   }
 }
 
+// fft_pass<16, N, S, false> for span S = 256 (j < 16), butterfly b, with the
+// twiddles from the table.
+template <int N, int S>
+__device__ __forceinline__ void fft_pass16_tab(float2* __restrict__ buf, const float2* __restrict__ tab, int b) {
+  constexpr int d = S / 16;
+  static_assert(d == 16, "table rows are j < 16");
+  const int j = b & (d - 1);
+  const int sb = swz((b - j) * 16 + j);
+  float2 x[16];
+#pragma unroll
+  for (int r = 0; r < 16; r++) x[r] = buf[sb ^ swz(r * d)];
+  DFT<16, -1>::run(x);
+  const float2* tr = tab + j * TW16_ROW;
+#pragma unroll
+  for (int r = 1; r < 16; r++) x[r] = cmul(x[r], tr[r]);
+#pragma unroll
+  for (int r = 0; r < 16; r++) buf[sb ^ swz(r * d)] = x[r];
+}
+
 // The inverse radix-16 pass of span S = 256 (fft_pass<16, N, 256, true>) for
 // butterfly b, its twiddles from the table.
 template <int N, int S>
