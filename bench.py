@@ -547,7 +547,7 @@ def run_ours(args):
     cap = max(64, 32 * len(items))
     out = np.zeros(cap, sg.RESULT_DTYPE)
     n_out = ctypes.c_size_t()
-    for _ in range(2):
+    for _ in range(max(args.warmup, 3)):
         sg._check(x.lib.xc_align_pairs(x.ctx, arr, len(arr), out.ctypes.data, cap, ctypes.byref(n_out), None), "e2e")
     e2e_t = []
     for _ in range(args.steps):
