@@ -309,14 +309,18 @@ def _block_items(tchunks, qchunks, tf, qf, n=24):
             for qi in range(qf, qf + n) for ti in range(tf, tf + n)]
 
 
-def test_spectra_path_equals_pair_kernel(O, monkeypatch):
+def test_spectra_path_matches_pair_kernel(O, monkeypatch):
     """Grid blocks of chunk pairs share their chunks: the spectra path
     (spec_kernel once per distinct chunk, then the pair kernel from stored
-    spectra) forms each pair's sums with the same operations as the
-    both-strands kernel, so its offsets and records are identical to it,
-    and to the oracle over those offsets.  The chunks include an N run
-    (handed back to the per-strand kernel), an empty chunk and a short last
-    query chunk whose length is not a multiple of the entropy window."""
+    spectra) and the both-strands kernel form each pair's sums by different
+    FP32 operations (the four channels as two packed pairs, against the
+    basis A - T, C - G, A + T with the two sequences' A + T in one
+    transform).  Their FindTop offsets agree except at lags that one of them
+    lists as near its threshold; where a pair's offsets agree its records
+    are identical; the records of both equal the oracle's over their own
+    offsets.  The chunks include an N run (handed back to the per-strand
+    kernel), an empty chunk and a short last query chunk whose length is not
+    a multiple of the entropy window."""
     import satsuma2_gb300 as sg
     rng = np.random.default_rng(93)
     t = W.random_bases(rng, 3072 * 12 + 1024)
@@ -339,23 +343,38 @@ def test_spectra_path_equals_pair_kernel(O, monkeypatch):
     b_off.run()
     r_on, c_on = b_on.results(with_counts=True)
     r_off, c_off = b_off.results(with_counts=True)
-    assert np.array_equal(c_on, c_off)
-    assert parity.same_results(r_on, r_off, prob_rtol=0.0, target_total=0.0)
     o_on, o_off = b_on.offsets(), b_off.offsets()
+    n_on, l_on = b_on.straddles()
+    n_off, l_off = b_off.straddles()
+    s_on = np.concatenate([[0], np.cumsum(c_on.astype(np.int64))])
+    s_off = np.concatenate([[0], np.cumsum(c_off.astype(np.int64))])
+    n_diff = n_same = 0
     for k in range(len(items)):
+        same = True
         for s2 in range(2):
-            assert np.array_equal(o_on[k][s2], o_off[k][s2]), (k, s2)
+            d = set(o_on[k][s2].tolist()) ^ set(o_off[k][s2].tolist())
+            if d:
+                same = False
+                n_diff += len(d)
+                assert n_on[k, s2] <= sg.STRAD_CAP and n_off[k, s2] <= sg.STRAD_CAP
+                near = set(l_on[k, s2][:n_on[k, s2]].tolist()) | set(l_off[k, s2][:n_off[k, s2]].tolist())
+                assert d <= near, (k, s2, sorted(d - near))
+        if same:
+            n_same += 1
+            assert parity.same_results(r_on[s_on[k]:s_on[k + 1]], r_off[s_off[k]:s_off[k + 1]], prob_rtol=0.0,
+                                       target_total=0.0), k
+    assert n_diff <= 4 and n_same >= len(items) - 4, (n_diff, n_same)
     assert len(r_on) > 0
     P = O.params(target_total=TT)
-    starts = np.concatenate([[0], np.cumsum(c_on.astype(np.int64))])
     tb, qb = t.tobytes(), q.tobytes()
     for k in range(0, len(items), 7):
         it = items[k]
         ts, qs = int(it["t_chunk_start"]), int(it["q_chunk_start"])
         pr = O.pair(tb[ts:ts + int(it["tlen"])], qb[qs:qs + int(it["qlen"])], t_chunk_start=ts, q_chunk_start=qs,
                     query_size=len(qb))
-        want, _ = O.align_pair(P, pr, offsets_in=o_on[k])
-        assert parity.same_results(r_on[starts[k]:starts[k + 1]], want, target_total=TT), k
+        for o, r, st in ((o_on, r_on, s_on), (o_off, r_off, s_off)):
+            want, _ = O.align_pair(P, pr, offsets_in=o[k])
+            assert parity.same_results(r[st[k]:st[k + 1]], want, target_total=TT), k
     b_on.free()
     b_off.free()
     x_on.close()
