@@ -182,6 +182,22 @@ __device__ __forceinline__ uint32_t mark_word(uint32_t e2, uint32_t e1, uint32_t
   return (edge || (m && h69 >= word_floor)) ? 1u : 0u;
 }
 
+// Pass-1 mark with the floors on, without the full screen: a word is marked
+// when block 0 or block 7 passes the block test (their spans are bits
+// 19..67 and 47..95 of e2:e1:e0, the counts screen_word forms for them) or
+// its 69 inner positions hold at least word_floor equal bases.  That marks
+// every word mark_word marks and some more (words at the floor none of
+// whose blocks passes), whose exact window bits in phase AB hold no passing
+// check; it costs about half of screen_word's instructions.  With the
+// floors off (word_floor 0) it would mark every word: mark_word then.
+__device__ __forceinline__ uint32_t mark_word_floor(uint32_t e2, uint32_t e1, uint32_t e0, int word_floor) {
+  const int p1 = __popc(e1);
+  const int h69 = __popc(e2 >> 23) + p1 + __popc(e0 & 0x0fffffffu);
+  const int c0 = __popc(e2 >> 19) + p1 + __popc(e0 & 15u);
+  const int c7 = __popc(e1 >> 15) + __popc(e0);
+  return (max(c0, c7) >= MIN_HITS || h69 >= word_floor) ? 1u : 0u;
+}
+
 // Exact window bits of one word: bit u set when check u's window holds
 // >= MIN_HITS equal bases.  Four byte lanes (checks 8j + s) step s = 0..7
 // together: count(u+1) = count(u) + bit u+65 - bit u+19 of e2:e1:e0.  Each
@@ -580,6 +596,7 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
         // The query word pair of target word w is (w + qd, w + qd + 1) at bit
         // shift sh: one new query word per step.
         const int qd = (pos + 32 * QPAD) >> 5, sh = (pos + 32 * QPAD) & 31;
+        const bool floor_on = P.word_floor > 0;   // off: every screened word is marked (mark_word)
         uint32_t e2 = eword(pos, wfirst - 2), e1 = eword(pos, wfirst - 1);
         const uint2* qp = qb + wfirst + qd;
         const uint2* tp = tb + wfirst;
@@ -593,7 +610,8 @@ __global__ void __launch_bounds__(NT_SCAN, SCAN_CTAS_PER_SM) scan_kernel(const S
             const uint2 nx = qp[q0 + q + 1], tw = tp[q0 + q];
             const uint32_t e0 = ~((tw.x ^ __funnelshift_r(a.x, nx.x, sh)) | (tw.y ^ __funnelshift_r(a.y, nx.y, sh)));
             a = nx;
-            acc = __funnelshift_r(acc, mark_word(e2, e1, e0, P.word_floor), 1);   // in at bit 31
+            const uint32_t mk = floor_on ? mark_word_floor(e2, e1, e0, P.word_floor) : mark_word(e2, e1, e0, 0);
+            acc = __funnelshift_r(acc, mk, 1);   // in at bit 31
             e2 = e1;
             e1 = e0;
           }
