@@ -4,7 +4,8 @@ word makes a segment of r + 45 bases whose equal-base count the kernel takes
 from the word's equality bits; below the floor for r no G+C composition lets
 the segment pass the probability screen.  Pass 1: a screened word whose edge
 blocks fail and whose inner positions hold fewer equal bases than the least
-floor stays unmarked.  Restated here in double and checked against the
+floor stays unmarked; with the floors on, pass 1 marks by exactly those two
+tests, without the eight-block screen (a superset of the screened marks).  Restated here in double and checked against the
 oracle: every segment the floor drops has a match probability below
 min_prob (so it never makes a record), and every word of a record-making
 segment stays marked, for the screen settings of the uniform, genome and
@@ -105,10 +106,13 @@ def test_floor_off_when_screen_keeps_all():
 
 
 def _words_model(eq, w, F):
-    """(screened, marked) of word w of a diagonal, positions out of range
-    counted unequal: screened when some 4-check block's 49-position span holds
-    >= 19 equal bases; marked when, besides, block 0 or block 7 passes or the
-    69 positions under checks 4..27 hold >= F equal bases."""
+    """(screened, marked, marked_by_floor) of word w of a diagonal, positions
+    out of range counted unequal: screened when some 4-check block's
+    49-position span holds >= 19 equal bases; marked (the screened form) when
+    screened and, besides, block 0 or block 7 passes or the 69 positions under
+    checks 4..27 hold >= F equal bases; marked_by_floor (pass 1's form with
+    the floors on) when block 0 or block 7 passes or those 69 positions hold
+    >= F equal bases."""
     def cnt(lo, hi):   # equal bases at positions lo..hi
         lo, hi = max(lo, 0), min(hi, len(eq) - 1)
         return int(eq[lo:hi + 1].sum()) if hi >= lo else 0
@@ -116,20 +120,22 @@ def _words_model(eq, w, F):
     blocks = [cnt(c + 4 * b - 45, c + 4 * b + 3) >= 19 for b in range(8)]
     screened = any(blocks)
     edge = blocks[0] or blocks[7]
-    return screened, screened and (edge or cnt(c - 41, c + 27) >= F)
+    floor = cnt(c - 41, c + 27) >= F
+    return screened, screened and (edge or floor), edge or floor
 
 
 @pytest.mark.parametrize("min_prob,target_total", [(0.99, 4096.0 ** 2), (0.99999, 2.0e7)])
 def test_word_floor_keeps_record_words(O, min_prob, target_total):
-    """Pass 1 leaves a screened word unmarked when its edge blocks fail and
-    the positions under its inner checks hold fewer equal bases than the least
+    """Pass 1 leaves a word unmarked when its edge blocks fail and the
+    positions under its inner checks hold fewer equal bases than the least
     run floor: every word holding a check of a segment that makes a record
-    stays marked, and a good share of the screened words go."""
+    stays marked, in both forms, and the marks stay a small share of the
+    words (the floor form marks every word the screened form marks)."""
     fl = floors(screen_z(min_prob, target_total), 0)
     F = min(fl)
     items = W.uniform_batch(4, seed=29)
     P = O.params(target_total=target_total, min_prob=min_prob)
-    n_screened = n_marked = n_rec = 0
+    n_words = n_screened = n_marked = n_floor = n_rec = 0
     for t, q in items:
         _, det = O.align_pair(P, O.pair(t, q), want_detail=True)
         ta = np.frombuffer(t, np.uint8)
@@ -143,9 +149,12 @@ def test_word_floor_keeps_record_words(O, min_prob, target_total):
                     eq[lo:hi] = ta[lo:hi] == qa[lo + pos:hi + pos]
                 marks = {}
                 for w in range(len(ta) // 32 + 1):
-                    sc, mk = _words_model(eq, w, F)
+                    sc, mk, mf = _words_model(eq, w, F)
+                    assert mf or not mk
+                    n_words += 1
                     n_screened += sc
                     n_marked += mk
+                    n_floor += mf
                     marks[w] = mk
                 for s0, _, ln in O.doone(t, qq, pos):
                     p, _ = O.match_prob(t, qq, s0, s0 + pos, ln, target_total)
@@ -156,3 +165,4 @@ def test_word_floor_keeps_record_words(O, min_prob, target_total):
                         assert marks[w], (pos, s0, ln, w)
     assert n_rec > 0
     assert n_marked < 0.8 * n_screened, (n_marked, n_screened)
+    assert n_floor < 0.1 * n_words, (n_floor, n_words)
