@@ -981,14 +981,16 @@ int batch_rerun_overflow(Ctx* c, Batch* b, cudaStream_t s, xc_result* out, size_
 // batches and two streams, so the host packing and the host-to-device copy of
 // one sub-batch overlap the kernels of the one before; results are collected
 // in order.  Sub-batch sizes count in waves of the FFT-8192 correlation kernel
-// (one CTA per SM): a first one of 3 waves so the GPU starts early, then
+// (one CTA per SM): a first one of 4 waves so the GPU starts early, then
 // equal ones of at most 12 waves and max_batch pairs.  On GB300 a 4096-pair
 // call took 2.28 ms as 456 + 2 x 1820 pairs, 2.57 ms as 512 + 4 x 896 and
-// 2.59 ms in one batch.
+// 2.59 ms in one batch; after the kernels got faster the host's packing of
+// the second sub-batch outlasted a 3-wave first one on the GPU, and 608 +
+// 2 x 1744 took 1.53 ms against 1.55-1.57 ms as 456 + 2 x 1820.
 int ctx_align_pipelined(Ctx* c, const xc_pair* pairs, size_t n, xc_result* out, size_t cap, size_t* n_out,
                         size_t* pair_counts) {
   const size_t maxb = c->prm.max_batch > 0 ? (size_t)c->prm.max_batch : 4096;
-  const size_t first = std::min(maxb, (size_t)3 * c->sms), size = std::min(maxb, (size_t)12 * c->sms);
+  const size_t first = std::min(maxb, (size_t)4 * c->sms), size = std::min(maxb, (size_t)12 * c->sms);
   std::vector<size_t> bound{0};
   if (n <= 2 * first && n <= maxb) {
     bound.push_back(n);
