@@ -1578,33 +1578,6 @@ size_t corr_rcq_smem_bytes() {
          + 256 * sizeof(uint32_t);                       // its codes of positions g + 256 r
 }
 
-// First forward pass of one transform of the packed signal z = s_c0 + i s_c1
-// (ODD: the odd-bin transform, input z W_L^n), input built in registers as in
-// first_pass_from_codes; thread g takes butterfly g.
-template <bool ODD>
-__device__ __forceinline__ void first_pass_one(uint32_t codes, int len, const float4* __restrict__ vw, int g, int c0,
-                                               int c1, const float2* twLh, const float2* twLl, const float2* twNh,
-                                               const float2* twNl, float2* __restrict__ buf) {
-  float2 x[16];
-  float2 wg = make_float2(1.f, 0.f);
-  if (ODD) wg = tw2(twLh, twLl, g);
-#pragma unroll
-  for (int r = 0; r < 16; r++) {
-    const float4 v = vw[16 * r];
-    const uint32_t code = (codes >> (2 * r)) & 3u;
-    float2 z = make_float2(0.f, 0.f);
-    if (g + 256 * r < len) z = make_float2(code == (uint32_t)c0 ? v.y : v.x, code == (uint32_t)c1 ? v.w : v.z);
-    x[r] = ODD ? cmul(cmul(z, wg), make_float2(cos_pi16(r), -sin_pi16(r))) : z;
-  }
-  DFT<16, -1>::run(x);
-  const Tw16 tw = tw16(twNh, twNl, g);
-#pragma unroll
-  for (int r = 1; r < 16; r++) x[r] = cmul(x[r], tw16_r(tw, r));
-  const int sb = swz(g);
-#pragma unroll
-  for (int r = 0; r < 16; r++) buf[sb ^ swz(256 * r)] = x[r];
-}
-
 template <int LOG2L>
 __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams P) {
   constexpr int L = 1 << LOG2L;
@@ -1620,9 +1593,9 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams 
   float2* ZO = ZE + N;                            // z * W_L^n, odd-bin transform
   float2* WE = ZO + N;                            // w = q_c0 + i q_c1, then the reverse complement's
   float2* WO = WE + N;
-  float2* aFE = WO + N;                           // 2 x forward-strand sum, bins 2m, m <= N/2
+  float2* aFE = WO + N;                           // 4 x forward-strand sum, bins 2m, m <= N/2
   float2* aFO = aFE + (N / 2 + 8);                // bins 2m+1
-  float2* aRE = aFO + N / 2;                      // 2 x reverse-strand sum, bins 2m (m < N/2)
+  float2* aRE = aFO + N / 2;                      // 4 x reverse-strand sum, bins 2m (m < N/2)
   float2* aRO = aRE + (N / 2 + 8);                // bins 2m+1 (m < N/2 - 1)
   float2* twNh = aRO + N / 2;
   float2* twNl = twNh + NH;
@@ -1632,10 +1605,10 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams 
   uint8_t* sq = st + N;
   float* Et = reinterpret_cast<float*>(sq + N);
   float* Eq = Et + NWIN;
-  float4* vv = reinterpret_cast<float4*>(Eq + NWIN);   // [sequence][window]: c0 (w=0, w=1), c1 (w=0, w=1)
+  float4* vv = reinterpret_cast<float4*>(Eq + NWIN);   // [sequence][window]: w by base code
   uint32_t* cw = reinterpret_cast<uint32_t*>(vv + 2 * NWIN);   // [sequence][g]
   float* Er = reinterpret_cast<float*>(cw + 2 * NWIN);        // reverse complement: window weights
-  float4* vr = reinterpret_cast<float4*>(Er + NWIN);          // its window values
+  float4* vr = reinterpret_cast<float4*>(Er + NWIN);          // its w by base code
   uint32_t* cr = reinterpret_cast<uint32_t*>(vr + NWIN);      // its codes of positions g + 256 r
   __shared__ int s_cnt4[8];
   __shared__ unsigned s_flags;     // bit 0: a byte >= 128; bit 1: a byte other than A, C, G, T
@@ -1786,95 +1759,160 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams 
     }
     __syncthreads();
 
+    // ---- 3. the channels in the basis u = s_A - s_T, v = s_C - s_G,
+    //      w = s_A + s_T = -(s_C + s_G), as corr_pair2_kernel (the reverse
+    //      complement is A/C/G/T too, its channel means the forward query's
+    //      of the complement channels, so its channels also sum to zero).
+    //      Stage 1: u + i v of the target (group 0) and the query (group 1),
+    //      both halves, the forward per-bin step, then u + i v of the reverse
+    //      complement (group 0 its even-bin half, group 1 its odd-bin half)
+    //      and the reverse per-bin step.  Stage 2: wt + i wq, then wt + i wr,
+    //      each split between the groups, with per-bin steps over each
+    //      group's own half.  Ten half-length forward transforms per pair.
+    // 3a. per-window signal values by base code: (u, v) of the target and
+    //     query into the forward sums' space, of the reverse complement into
+    //     the reverse sums' space (each overwritten only after its first
+    //     pass); w into vv (target, query) and vr (reverse complement)
+    float2* uvt = reinterpret_cast<float2*>(aFE);   // [sequence][window][code]
+    float2* uvr = reinterpret_cast<float2*>(aRE);   // [window][code]
+    auto tables = [&](float E, int k0, int k1, int k2, int k3, float2* uvo, float4* wo) {
+      const float4 at = window_values(E, s_wf, s_wmo, k0, k3);   // A at 0, 1; T at 0, 1
+      const float4 cg = window_values(E, s_wf, s_wmo, k1, k2);   // C at 0, 1; G at 0, 1
+      const float u0 = __fsub_rn(at.x, at.z), v0 = __fsub_rn(cg.x, cg.z), w0 = __fadd_rn(at.x, at.z);
+      float4* o = reinterpret_cast<float4*>(uvo);
+      o[0] = make_float4(__fsub_rn(at.y, at.z), v0, u0, __fsub_rn(cg.y, cg.z));   // A, C
+      o[1] = make_float4(u0, __fsub_rn(cg.x, cg.w), __fsub_rn(at.x, at.w), v0);   // G, T
+      *wo = make_float4(__fadd_rn(at.y, at.z), w0, w0, __fadd_rn(at.x, at.w));
+    };
+    tables((G ? Eq : Et)[g], G * 4 + 0, G * 4 + 1, G * 4 + 2, G * 4 + 3, uvt + (G * NWIN + g) * 4, vv + G * NWIN + g);
+    // the reverse complement's channel c has the forward query's mean of 3 - c
+    if (G == 0) tables(Er[g], 4 + 3, 4 + 2, 4 + 1, 4 + 0, uvr + g * 4, vr + g);
+    __syncthreads();
+    // 3b. stage 1: u + i v of the target and the query, both halves
+    {
+      const uint32_t codes = cw[tid];
+      const int len = G ? Q : T;
+      const float2* ub = uvt + (G * NWIN + (g >> 4)) * 4;
+      float2* bE = G ? WE : ZE;
+      first_pass_x2(
+          [&](int r) {
+            const float2 z = ub[64 * r + ((codes >> (2 * r)) & 3u)];
+            return g + 256 * r < len ? z : make_float2(0.f, 0.f);
+          },
+          g, twLh, twLl, twNh, twNl, bE, bE + N);
+      gb();
+      fft_pass16_x2<N, N / 16>(bE, bE + N, twNh, twNl, g);
+      gb();
+      fft_pass16_x2<N, N / 256>(bE, bE + N, twNh, twNl, g);
+    }
+    __syncthreads();
+    // 3c. per-bin step of stage 1 against the target's spectra in ZE / ZO:
+    //     f = conj(A) C + B conj(D) = 2 (conj(Ut) Xu + conj(Vt) Xv); the
+    //     target-only bins N-1 and N are zero in this basis
+    auto per_bin_uv = [&](const float2* VE, const float2* VO, float2* oE, float2* oO) {
+      if (G == 0) {
+        const int la = lp<LOG2N>(g);
+        const int lb = lp<LOG2N>((256 - g) & 255);
+#pragma unroll
+        for (int it = 0; it <= N / 512; it++) {
+          const int m = g + 256 * it;
+          if (m > N / 2) break;
+          const int pa = la ^ lp<LOG2N>(256 * it);
+          const int pb = g ? (lb ^ lp<LOG2N>(N - 256 * (it + 1))) : lp<LOG2N>((N - 256 * it) & (N - 1));
+          oE[m] = m == N / 2 ? make_float2(0.f, 0.f) : cadd(cmulc(VE[pa], ZE[pa]), cmulc(ZE[pb], VE[pb]));
+        }
+      } else {
+        const int la = lp<LOG2N>(g);
+#pragma unroll
+        for (int it = 0; it < N / 512; it++) {
+          const int m = g + 256 * it;
+          const int pa = la ^ lp<LOG2N>(256 * it);
+          const int pb = pa ^ lp<LOG2N>(N - 1);
+          oO[m] = m == N / 2 - 1 ? make_float2(0.f, 0.f) : cadd(cmulc(VO[pa], ZO[pa]), cmulc(ZO[pb], VO[pb]));
+        }
+      }
+    };
+    per_bin_uv(WE, WO, aFE, aFO);
+    __syncthreads();
+    // 3d. u + i v of the reverse complement: the even-bin half in group 0
+    //     (into WE), the odd-bin half in group 1 (into WO)
+    {
+      float2* b = G ? WO : WE;
+      const uint32_t codes = cr[g];
+      const float2* ub = uvr + (g >> 4) * 4;
+      first_pass_x1(
+          [&](int r) {
+            const float2 z = ub[64 * r + ((codes >> (2 * r)) & 3u)];
+            return g + 256 * r < Q ? z : make_float2(0.f, 0.f);
+          },
+          G == 1, g, twLh, twLl, twNh, twNl, b);
+      gb();
+      fft_pass<16, N, N / 16, false>(b, twNh, twNl, g, 256);
+      gb();
+      fft_pass<16, N, N / 256, false>(b, twNh, twNl, g, 256);
+    }
+    __syncthreads();
+    // 3e. the reverse strand's per-bin step of stage 1
+    per_bin_uv(WE, WO, aRE, aRO);
+    gb();   // stage 2 overwrites what the group's per-bin step read (group 0 ZE, group 1 WO)
+    // 3f. stage 2: wt + i wq, then wt + i wr; each group transforms its half
+    //     and adds f = 2 Im(H E) - i (|E|^2 - |H|^2) = 4 conj(Wt) Wx over it
+    float2* bw = G ? WO : ZE;
+    const uint32_t ct = cw[g];
+    const float* wt_tab = reinterpret_cast<const float*>(vv) + (g >> 4) * 4;
 #pragma unroll 1
     for (int stg = 0; stg < 2; stg++) {
-      const int c0 = stg ? 1 : 0, c1 = stg ? 2 : 3;
-      const bool first = stg == 0;
-      // ---- 3a. window values; the reverse complement's channel c has the
-      //      forward query's mean of comp(c) = 3 - c ----
-      vv[G * NWIN + g] = window_values((G ? Eq : Et)[g], s_wf, s_wmo, G * 4 + c0, G * 4 + c1);
-      if (G == 0) vr[g] = window_values(Er[g], s_wf, s_wmo, 4 + 3 - c0, 4 + 3 - c1);
-      __syncthreads();
-      // ---- 3b. target (group 0) and forward query (group 1), both
-      //      transforms of each ----
-      first_pass_from_codes(cw[tid], G ? Q : T, vv + G * NWIN + (g >> 4), g, c0, c1, twLh, twLl, twNh, twNl,
-                            G ? WE : ZE, (G ? WE : ZE) + N);
+      const uint32_t cx = stg ? cr[g] : cw[NWIN + g];
+      const float* wx_tab = stg ? reinterpret_cast<const float*>(vr) + (g >> 4) * 4
+                                : reinterpret_cast<const float*>(vv) + NWIN * 4 + (g >> 4) * 4;
+      first_pass_x1(
+          [&](int r) {
+            const float wt = wt_tab[64 * r + ((ct >> (2 * r)) & 3u)];
+            const float wx = wx_tab[64 * r + ((cx >> (2 * r)) & 3u)];
+            return make_float2(g + 256 * r < T ? wt : 0.f, g + 256 * r < Q ? wx : 0.f);
+          },
+          G == 1, g, twLh, twLl, twNh, twNl, bw);
       gb();
-      {
-        float2* bE = G ? WE : ZE;
-        fft_pass16_x2<N, N / 16>(bE, bE + N, twNh, twNl, g);
-        gb();
-        fft_pass16_x2<N, N / 256>(bE, bE + N, twNh, twNl, g);
-      }
-      __syncthreads();
-      // ---- 3c. forward sum f = conj(A) C + B conj(D); bins N-1 and N keep
-      //      the targets' own values (as corr_pair2_kernel) ----
-      auto per_bin = [&](const float2* VE, const float2* VO, float2* oE, float2* oO, bool fwd) {
-        if (G == 0) {
-          const int la = lp<LOG2N>(g);
-          const int lb = lp<LOG2N>((256 - g) & 255);
-#pragma unroll
-          for (int it = 0; it <= N / 512; it++) {
-            const int m = g + 256 * it;
-            if (m > N / 2) break;
-            const int pa = la ^ lp<LOG2N>(256 * it);
-            const int pb = g ? (lb ^ lp<LOG2N>(N - 256 * (it + 1))) : lp<LOG2N>((N - 256 * it) & (N - 1));
-            const float2 A = ZE[pa];
-            if (m == N / 2) {
-              if (fwd) {
-                const float2 f = pair_bin_nyquist(A);
-                oE[m] = first ? f : cadd(oE[m], f);
-              }
-            } else {
-              const float2 B = ZE[pb], C = VE[pa], D = VE[pb];
-              const float2 f = cadd(cmulc(C, A), cmulc(B, D));
-              oE[m] = first ? f : cadd(oE[m], f);
-            }
-          }
-        } else {
-          const int la = lp<LOG2N>(g);
-#pragma unroll
-          for (int it = 0; it < N / 512; it++) {
-            const int m = g + 256 * it;
-            const int pa = la ^ lp<LOG2N>(256 * it);
-            const int pb = pa ^ lp<LOG2N>(N - 1);
-            const float2 A = ZO[pa], B = ZO[pb];
-            if (m == N / 2 - 1) {
-              if (fwd) {
-                const float2 f = pair_bin_nm1(A, B);
-                oO[m] = first ? f : cadd(oO[m], f);
-              }
-            } else {
-              const float2 C = VO[pa], D = VO[pb];
-              const float2 f = cadd(cmulc(C, A), cmulc(B, D));
-              oO[m] = first ? f : cadd(oO[m], f);
-            }
-          }
+      fft_pass<16, N, N / 16, false>(bw, twNh, twNl, g, 256);
+      gb();
+      fft_pass<16, N, N / 256, false>(bw, twNh, twNl, g, 256);
+      gb();
+      float2* oE = stg ? aRE : aFE;
+      float2* oO = stg ? aRO : aFO;
+      if (G == 0) {
+        const int la = lp<LOG2N>(g);
+        const int lb = lp<LOG2N>((256 - g) & 255);
+#pragma unroll 3
+        for (int it = 0; it <= N / 512; it++) {
+          const int m = g + 256 * it;
+          if (m >= N / 2) break;
+          const int pa = la ^ lp<LOG2N>(256 * it);
+          const int pb = g ? (lb ^ lp<LOG2N>(N - 256 * (it + 1))) : lp<LOG2N>((N - 256 * it) & (N - 1));
+          float2 f, r;
+          pair_bin_w(ZE[pa], ZE[pb], f, r);
+          oE[m] = cadd(oE[m], f);
         }
-      };
-      per_bin(WE, WO, aFE, aFO, true);
-      __syncthreads();
-      // ---- 3d. the reverse complement's even-bin (group 0) and odd-bin
-      //      (group 1) transforms, one per group ----
-      {
-        float2* b = G ? WO : WE;
-        if (G) first_pass_one<true>(cr[g], Q, vr + (g >> 4), g, c0, c1, twLh, twLl, twNh, twNl, b);
-        else first_pass_one<false>(cr[g], Q, vr + (g >> 4), g, c0, c1, twLh, twLl, twNh, twNl, b);
-        gb();
-        fft_pass<16, N, N / 16, false>(b, twNh, twNl, g, 256);
-        gb();
-        fft_pass<16, N, N / 256, false>(b, twNh, twNl, g, 256);
+      } else {
+        const int la = lp<LOG2N>(g);
+#pragma unroll 3
+        for (int it = 0; it < N / 512; it++) {
+          const int m = g + 256 * it;
+          if (m == N / 2 - 1) break;
+          const int pa = la ^ lp<LOG2N>(256 * it);
+          const int pb = pa ^ lp<LOG2N>(N - 1);
+          float2 f, r;
+          pair_bin_w(WO[pa], WO[pb], f, r);
+          oO[m] = cadd(oO[m], f);
+        }
       }
-      __syncthreads();
-      // ---- 3e. reverse sum, the same formula over the reverse complement ----
-      per_bin(WE, WO, aRE, aRO, false);
-      __syncthreads();
+      gb();   // the next stage overwrites the group's buffer
     }
+    __syncthreads();
 
     // ---- 4. inverses: group 0 the forward strand into ZE, group 1 the
-    //      reverse strand into WE (bins N-1 and N: the targets' own values,
-    //      the same for both strands).  Sums and the pack carry factors 2
-    //      and 2: FindTop scales by 1/(4N). ----
+    //      reverse strand into WE (bins N-1 and N: zero for both strands).
+    //      Sums and the pack carry factors 4 and 2: FindTop scales by
+    //      1/(8N). ----
     float2* buf = G ? WE : ZE;
     auto SF = [&](int k) -> float2 { return (k & 1) ? aFO[k >> 1] : aFE[k >> 1]; };
     auto SRc = [&](int k) -> float2 {
@@ -1887,7 +1925,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_rcq_kernel(const CorrParams 
     fft_inverse<LOG2N, Plan<LOG2N>, Plan<LOG2N>::n - 1, GroupBarrier>(buf, twNh, twNl, g, 256, gb);
     // ---- 5. FindTop, one strand per group ----
     find_top<LOG2L, 256, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, G, buf, g, s_warp[G], gb,
-                                       1.0f / (float)(4 * N));
+                                       1.0f / (float)(8 * N));
     __syncthreads();   // buffers and per-pair words are reused by the next pair
     if (tid == 0 && s_flags) {
       // bytes outside the premise (rare): the pass above is void.  A byte
