@@ -1559,13 +1559,17 @@ size_t spec_bytes_per_chunk() { return (size_t)4 * 4096 * sizeof(float2); }
 // the reverse strand's query signal is its own (CCSignal over the reverse
 // complement, as the reference builds it), and the spectra cannot be shared
 // the way corr_pair2_kernel shares them.  The target is still transformed
-// once for both strands (two per-strand CTAs transform it twice): per channel
-// pair, group 0 transforms the target and group 1 the forward query (two
-// transforms each, as corr_pair2_kernel), the forward sum takes
-// f = conj(A) C + B conj(D); then group 0 transforms the reverse-complemented
-// query's even-bin signal and group 1 its odd-bin signal, and the reverse
-// sum takes the same formula.  12 forward and 2 inverse half-length
-// transforms per pair, where two corr_kernel CTAs take 16 and 2.  The pairs
+// once for both strands (two per-strand CTAs transform it twice).  The
+// channels go in corr_pair2_kernel's basis u = A - T, v = C - G, w = A + T
+// (the reverse complement is A/C/G/T too, so its channels also sum to
+// zero): group 0 transforms the target's u + i v and group 1 the forward
+// query's (two transforms each), the forward sum takes
+// f = conj(A) C + B conj(D); then group 0 transforms the reverse
+// complement's even-bin half and group 1 its odd-bin half, and the reverse
+// sum takes the same formula; then wt + i wq and wt + i wr, each split
+// between the groups, add 4 conj(Wt) Wq and 4 conj(Wt) Wr (pair_bin_w).
+// 10 forward and 2 inverse half-length transforms per pair (12 with the
+// four channels), where two corr_kernel CTAs take 16 and 2.  The pairs
 // are the FFT-8192 bucket's last ones, placed there by the host (its
 // ragged query windows), or the list corr_spec_kernel (or, without a
 // range, corr_pair2_kernel) hands on; CTAs stride over them.  A pair with a
