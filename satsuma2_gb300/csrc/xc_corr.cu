@@ -1956,8 +1956,9 @@ static size_t spec_smem_bytes() {
   return (4 * N + 2 * (NH + 64) + 16 * TW16_ROW) * sizeof(float2)   // 4 transforms, twiddles
          + N                                        // chunk bytes
          + 256 * sizeof(float)                      // entropy weight per window
-         + 2 * 256 * sizeof(float4)                 // window values per channel pair
-         + 256 * sizeof(uint32_t);                  // 2-bit codes of positions g + 256 r
+         + 2 * 256 * sizeof(float4)                 // (u, v) by base code per window
+         + 256 * sizeof(uint32_t)                   // 2-bit codes of positions g + 256 r
+         + 256 * sizeof(float4);                    // w by base code per window
 }
 
 __device__ __forceinline__ void spec_prefetch(const SpecParams& S, int u, uint8_t* sb, int tid) {
@@ -1987,8 +1988,9 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
   float2* tw16t = twLl + 64;   // twiddles of the span-256 pass (build_tw16_table)
   uint8_t* sb = reinterpret_cast<uint8_t*>(tw16t + 16 * TW16_ROW);
   float* Es = reinterpret_cast<float*>(sb + N);
-  float4* vv = reinterpret_cast<float4*>(Es + NWIN);     // [channel pair][window]
+  float4* vv = reinterpret_cast<float4*>(Es + NWIN);     // (u, v) by base code per window
   uint32_t* cw = reinterpret_cast<uint32_t*>(vv + 2 * NWIN);
+  float4* wv = reinterpret_cast<float4*>(cw + NWIN);      // w by base code per window
   __shared__ int s_cnt4[4];
   __shared__ unsigned s_flags;   // bit 0: a byte >= 128; bit 1: a byte other than A, C, G, T
   __shared__ int s_take;         // the CTA's next chunk
@@ -1996,7 +1998,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
   __shared__ Split3 s_wf[2][8];
 
   const int tid = threadIdx.x;
-  const int G = tid >> 8;   // channel pair: 0 (A, T), 1 (C, G)
+  const int G = tid >> 8;   // signal: 0 u + i v, 1 w
   const int g = tid & 255;
   const GroupBarrier gb{1 + G, 256};
   for (int i = tid; i < NH; i += NT_PAIR2) {
@@ -2103,26 +2105,56 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) spec_kernel(const SpecParams S) {
       cw[g] = w;
     }
     __syncthreads();
-    // group G transforms channel pair G: (A, T) or (C, G)
-    const int c0 = G ? 1 : 0, c1 = G ? 2 : 3;
+    // group 0 transforms u + i v (u = A - T, v = C - G), group 1 w + 0 i
+    // (w = A + T = -(C + G)): the signal values by base code per window from
+    // the channel values float(entropy * (weight - mean)) (CrossCorr.cc:123)
+    // with one FP32 add each, as corr_pair2_kernel forms them
     float2* bE = buf + 2 * G * N;
     float2* bO = bE + N;
-    vv[G * NWIN + g] = window_values(Es[g], s_wf, s_wmo, c0, c1);
+    float2* uvt = reinterpret_cast<float2*>(vv);   // [window][code]
+    {
+      const float4 at = window_values(Es[g], s_wf, s_wmo, 0, 3);   // A at 0, 1; T at 0, 1
+      const float w0 = __fadd_rn(at.x, at.z);
+      if (G == 0) {
+        const float4 cg = window_values(Es[g], s_wf, s_wmo, 1, 2);   // C at 0, 1; G at 0, 1
+        const float u0 = __fsub_rn(at.x, at.z), v0 = __fsub_rn(cg.x, cg.z);
+        float4* o = reinterpret_cast<float4*>(uvt + g * 4);
+        o[0] = make_float4(__fsub_rn(at.y, at.z), v0, u0, __fsub_rn(cg.y, cg.z));   // A, C
+        o[1] = make_float4(u0, __fsub_rn(cg.x, cg.w), __fsub_rn(at.x, at.w), v0);   // G, T
+      } else {
+        wv[g] = make_float4(__fadd_rn(at.y, at.z), w0, w0, __fadd_rn(at.x, at.w));
+      }
+    }
     gb();
-    first_pass_from_codes(cw[g], len, vv + G * NWIN + (g >> 4), g, c0, c1, twLh, twLl, twNh, twNl, bE, bO);
+    {
+      const uint32_t codes = cw[g];
+      const float2* ub = uvt + (g >> 4) * 4;
+      const float* wb = reinterpret_cast<const float*>(wv) + (g >> 4) * 4;
+      first_pass_x2(
+          [&](int r) {
+            const uint32_t k = (codes >> (2 * r)) & 3u;
+            const float2 z = G ? make_float2(wb[64 * r + k], 0.f) : ub[64 * r + k];
+            return g + 256 * r < len ? z : make_float2(0.f, 0.f);
+          },
+          g, twLh, twLl, twNh, twNl, bE, bO);
+    }
     gb();
     fft_pass16_x2_tab<N, N / 16>(bE, bO, tw16t, g);
     gb();
     fft_pass16_x2<N, N / 256>(bE, bO, twNh, twNl, g);
     gb();
-    // out in bin order: bin m of the even-bin transform at [2G][m], odd at [2G + 1][m]
+    // out in bin order: bin m of the even-bin transform at [2G][m], odd at
+    // [2G + 1][m]; of w's spectrum (real signal: W(L - k) = conj W(k)) only
+    // the bins the pair kernel reads, m <= N/2 of each half
     float2* out = S.spec + ((size_t)u * 4 + 2 * G) * N;
     const int la = lp<LOG2L - 1>(g);
 #pragma unroll 4
     for (int it = 0; it < N / 256; it++) {
+      const int m = g + 256 * it;
+      if (G && m > N / 2) break;
       const int pa = la ^ lp<LOG2L - 1>(256 * it);
-      out[g + 256 * it] = bE[pa];
-      out[N + g + 256 * it] = bO[pa];
+      out[m] = bE[pa];
+      out[N + m] = bO[pa];
     }
     if (tid == 0) {
       S.chunk_flags[u] = 0u;
@@ -2205,46 +2237,51 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
       continue;
     }
     if (tid == 0) P.pair_flags[pidx] = P.pairs[pidx].flags & PF_FAST;
-    // ---- per-bin step from the stored spectra, both channel pairs summed in
-    //      the order corr_pair2_kernel accumulates them ----
+    // ---- per-bin step from the stored spectra (u + i v both halves, W of
+    //      the real signal w = A + T): with A, B, C, D the u + i v spectra of
+    //      target and query at m and N-m,
+    //        4 sum_c conj(T_c) Q_c = conj(A) C + B conj(D) + 4 conj(Wt) Wq
+    //        4i sum_c T_c Q_comp(c) = -i (A conj(D) + conj(B) C) + 4i Wt Wq,
+    //      and the target-only bins N-1 and N are zero (the basis of
+    //      corr_pair2_kernel, which forms W from a joint transform) ----
     const float2* __restrict__ Ts = P.spec + (size_t)tc * 4 * N;
     const float2* __restrict__ Qs = P.spec + (size_t)qc * 4 * N;
+    auto bin = [](float2 A, float2 B, float2 C, float2 D, float2 Wt, float2 Wq, float2& f, float2& r) {
+      const float2 s = cadd(cmulc(A, D), cmulc(C, B));
+      const float2 fw = cmulc(Wq, Wt), rw = cmul(Wt, Wq);
+      f = cadd(cadd(cmulc(C, A), cmulc(B, D)), make_float2(4.f * fw.x, 4.f * fw.y));
+      r = cadd(make_float2(s.y, -s.x), make_float2(-4.f * rw.y, 4.f * rw.x));
+    };
     if (G == 0) {
 #pragma unroll 3
       for (int it = 0; it <= N / 512; it++) {
         const int m = g + 256 * it;
         if (m > N / 2) break;
-        const int mb = (N - m) & (N - 1);
-        const float2 A0 = __ldg(Ts + m), B0 = __ldg(Ts + mb), C0 = __ldg(Qs + m), D0 = __ldg(Qs + mb);
-        const float2 A1 = __ldg(Ts + 2 * N + m), B1 = __ldg(Ts + 2 * N + mb);
-        const float2 C1 = __ldg(Qs + 2 * N + m), D1 = __ldg(Qs + 2 * N + mb);
         if (m == N / 2) {
-          aFE[m] = cadd(pair_bin_nyquist(A0), pair_bin_nyquist(A1));
-        } else {
-          float2 f0, r0, f1, r1;
-          pair_bin(A0, B0, C0, D0, f0, r0);
-          pair_bin(A1, B1, C1, D1, f1, r1);
-          aFE[m] = cadd(f0, f1);
-          aRE[m] = cadd(r0, r1);
+          aFE[m] = make_float2(0.f, 0.f);
+          continue;
         }
+        const int mb = (N - m) & (N - 1);
+        float2 f, r;
+        bin(__ldg(Ts + m), __ldg(Ts + mb), __ldg(Qs + m), __ldg(Qs + mb), __ldg(Ts + 2 * N + m),
+            __ldg(Qs + 2 * N + m), f, r);
+        aFE[m] = f;
+        aRE[m] = r;
       }
     } else {
 #pragma unroll 4
       for (int it = 0; it < N / 512; it++) {
         const int m = g + 256 * it;
-        const int mb = N - 1 - m;
-        const float2 A0 = __ldg(Ts + N + m), B0 = __ldg(Ts + N + mb), C0 = __ldg(Qs + N + m), D0 = __ldg(Qs + N + mb);
-        const float2 A1 = __ldg(Ts + 3 * N + m), B1 = __ldg(Ts + 3 * N + mb);
-        const float2 C1 = __ldg(Qs + 3 * N + m), D1 = __ldg(Qs + 3 * N + mb);
         if (m == N / 2 - 1) {
-          aFO[m] = cadd(pair_bin_nm1(A0, B0), pair_bin_nm1(A1, B1));
-        } else {
-          float2 f0, r0, f1, r1;
-          pair_bin(A0, B0, C0, D0, f0, r0);
-          pair_bin(A1, B1, C1, D1, f1, r1);
-          aFO[m] = cadd(f0, f1);
-          aRO[m] = cadd(r0, r1);
+          aFO[m] = make_float2(0.f, 0.f);
+          continue;
         }
+        const int mb = N - 1 - m;
+        float2 f, r;
+        bin(__ldg(Ts + N + m), __ldg(Ts + N + mb), __ldg(Qs + N + m), __ldg(Qs + N + mb), __ldg(Ts + 3 * N + m),
+            __ldg(Qs + 3 * N + m), f, r);
+        aFO[m] = f;
+        aRO[m] = r;
       }
     }
     __syncthreads();
@@ -2266,7 +2303,7 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_spec_kernel(const CorrParams
     fft_pass<16, N, N, true>(buf, twNh, twNl, g, 256);
     gb();
     find_top<LOG2L, 256, GroupBarrier>(P, P.pairs[pidx].flags, P.pairs[pidx].off_base, pidx, G, buf, g, s_warp[G], gb,
-                                       1.0f / (float)(4 * N));
+                                       1.0f / (float)(8 * N));
     if (tid == 0) s_take = take;
     __syncthreads();
     p = np;
