@@ -1543,12 +1543,15 @@ __global__ void __launch_bounds__(NT_PAIR2, 1) corr_pair2_kernel(const CorrParam
 // 24 x 24 chunks is 576 pairs of 48 distinct chunks) every chunk takes part in
 // many pairs; the reference builds each chunk's signals once per block
 // (HomologyByXCorrSlave.cc:284-299).  spec_kernel transforms each distinct
-// chunk once -- both channel pairs, even-bin and odd-bin transforms, exactly
-// as corr_pair2_kernel transforms a sequence -- and stores the spectra in bin
-// order (128 KB per chunk, L2-resident for a batch of blocks);
+// chunk once in corr_pair2_kernel's channel basis -- u + i v (u = A - T,
+// v = C - G) and w + 0 i (w = A + T), even-bin and odd-bin transforms -- and
+// stores the spectra in bin order (128 KB per chunk, of w's real spectrum
+// the bins the pair kernel reads; L2-resident for a batch of blocks);
 // corr_spec_kernel then forms each pair's sums from the two chunks' spectra,
-// in the same operations and order as corr_pair2_kernel, so its results are
-// the same bit for bit, and runs the inverses and FindTop.
+// u + i v at m and N - m and W at m, and runs the inverses and FindTop.  Its
+// sums differ from corr_pair2_kernel's in rounding only (that kernel
+// transforms the two sequences' w jointly), so the two agree on every
+// FindTop offset outside the near-threshold lags.
 // ---------------------------------------------------------------------------
 size_t spec_bytes_per_chunk() { return (size_t)4 * 4096 * sizeof(float2); }
 
