@@ -23,8 +23,10 @@ to zero only up to their rounding, so the sums are checked against the
 channel-separated form the reference computes (CrossCorr.cc:477-492) to
 within that residual, and the whole strand -- Hermitian pack without its
 halves, N-point inverse, scale 1/(8N) -- against the direct FP64
-correlation, for both strands.  Signals come from the oracle's CCSignal
-restatement."""
+correlation, for both strands.  The spectra path (spec_kernel,
+corr_spec_kernel) stores u + i v and w's real spectrum per chunk and forms
+4 conj(Wt) Wq and 4i Wt Wq at each bin alone; its sums are checked against
+the same two forms.  Signals come from the oracle's CCSignal restatement."""
 import numpy as np
 import pytest
 
@@ -145,3 +147,51 @@ def test_both_strands_equal_the_direct_correlation(O, k):
         # FP32 kernels differ from FP64 by ~5e-7 of max |xc|; the basis's
         # rounding residual contributes ~2e-9
         assert np.abs(got - want).max() <= 2e-8 * max(1.0, np.abs(want).max())
+
+
+def spectra_sums(st, sq):
+    """F' and R' as corr_spec_kernel forms them from chunk-wise stored
+    spectra (spec_kernel): u + i v of each chunk (even-bin and odd-bin
+    halves) and W, the spectrum of the real signal w = A + T, at each bin
+    alone (no partner): 4 conj(Wt) Wq and 4i Wt Wq in place of the joint
+    transform's E, H formulas."""
+    n = np.arange(N)
+    wl = np.exp(-2j * np.pi * n / L)
+    F = np.zeros(N + 1, complex)
+    R = np.zeros(N + 1, complex)
+    z = (st[0] - st[3] + 1j * (st[1] - st[2]))[:N]
+    w = (sq[0] - sq[3] + 1j * (sq[1] - sq[2]))[:N]
+    Wt = np.fft.fft(st[0] + st[3])   # L-point spectra of the real signals
+    Wq = np.fft.fft(sq[0] + sq[3])
+    for odd in (0, 1):
+        Zt, Zq = (np.fft.fft(z * wl), np.fft.fft(w * wl)) if odd else (np.fft.fft(z), np.fft.fft(w))
+        m = np.arange(N // 2) if odd else np.arange(N // 2 + 1)
+        mb = (N - 1 - m) if odd else (N - m) % N
+        A, B, C, D = Zt[m], Zt[mb], Zq[m], Zq[mb]
+        k = 2 * m + odd
+        f = np.conj(A) * C + B * np.conj(D) + 4 * np.conj(Wt[k]) * Wq[k]
+        r = -1j * (A * np.conj(D) + np.conj(B) * C) + 4j * Wt[k] * Wq[k]
+        F[k], R[k] = f, r
+    F[N - 1:] = 0   # target-only bins: sum_c T_c = 0
+    R[N - 1:] = 0
+    return F, R
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_spectra_path_sums(O, k):
+    """The spectra path's sums equal the channel-separated form to within the
+    FP32 channel values' rounding residual, and the pair kernel's joint form
+    to FP64 rounding."""
+    t, q = pairs()[k]
+    st = O.signal(t, L).astype(np.float64)
+    sq = O.signal(q, L).astype(np.float64)
+    F, R = spectra_sums(st, sq)
+    F2, R2 = kernel_sums(st, sq)
+    scale = np.abs(F2).max()
+    assert np.abs(F[:N - 1] - F2[:N - 1]).max() <= 1e-9 * scale
+    assert np.abs(R[:N - 1] - R2[:N - 1]).max() <= 1e-9 * scale
+    T = np.fft.rfft(st, axis=1)
+    Qf = np.fft.rfft(sq, axis=1)
+    want_F = np.sum(np.conj(T) * Qf, axis=0)
+    tol = 1e-9 * scale + 4 * np.sqrt(L) * max(residual(st)[0], residual(sq)[0]) * np.abs(np.concatenate([T, Qf])).max()
+    assert np.abs(F[1:N - 1] / 4 - want_F[1:N - 1]).max() <= tol
